@@ -1,0 +1,380 @@
+"""Benchmark of the LightGraph multiple-scattering frame on GB300.
+
+Workload (one "step" = one frame): the 512^3 sparse cumulus (8^3 leaves, ~14%
+active, 6-octave fBm seed 1, extinction 20 / world unit, RGB scattering scale
+1.0/1.1/1.25) with a temperature grid through a 4-key ramp, one directional
+and one point light, one LightGraph of 4096 points (a 64 MB FP32 distance
+matrix), 1024x1024 at 4 spp, FP32 throughout. Inputs are seeded synthetic
+stand-ins for the reference's VDB assets. The density grid in its brick layout
+(~575 MB) is larger than L2, so no L2 flush is needed between steps.
+
+  value : ms per frame with the grids and points resident in HBM (CUDA events on
+          the library's stream around K frames); a frame is graph build, edge
+          march, Floyd-Warshall, vertex light, diffusion, splat and render.
+  e2e   : ms per frame through the public C ABI (lg_render_frame) with the points
+          copied in from pinned host memory and the four films copied back.
+  --impl reference : the reference's CPU path as restated by the oracle (FP64,
+          OpenMP over all host cores), on a bounded sample scaled to ms/frame.
+
+Multi-GPU: graphs and frames are independent, so N ranks run N replicas (one
+frame each per step, no collective); value = wall ms per frame of the job.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+STAGES = ["build_graph", "edge_march", "floyd_warshall", "vertex_light", "diffuse", "splat", "render"]
+NOMINAL_FP32_TFLOPS = 152 * 128 * 2 * 2.070  # GB300: SMs x FP32 lanes x 2 (FMA) x max clock (GHz)
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--small", action="store_true", help="the 128^3 / 1024-point / 256^2 case instead")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def make_scene(small: bool):
+    from lightgraph_gb300 import scenes
+    if small:
+        return scenes.small()
+    return scenes.production()
+
+
+def workload_config(sc, small):
+    o = sc.opts
+    return {"workload": ("small 128^3 sphere-fBm" if small else "production 512^3 sparse cumulus") +
+            f", {len(sc.points[0])}-point LightGraph, {o.width}x{o.height} at {o.samples} spp",
+            "grid": f"{sc.info['res']}^3, voxel {sc.info['voxel']:.5g}, active voxels {sc.info['active_voxels']}",
+            "graph_points": len(sc.points[0]), "connect_radius": sc.radius[0], "max_connect": sc.max_connect,
+            "image": [o.width, o.height], "spp": o.samples, "lights": [l.spec for l in sc.lights],
+            "steps_per_frame": list(o.step), "precision": "fp32 grids, fp32 math",
+            "l2": "inputs larger than L2 (density bricks ~575 MB > 129 MB), no flush" if not small else
+                  "small case: grid fits L2",
+            "parallelism": "replicas (independent frames per GPU)"}
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    FIELDS = ["clocks.sm", "clocks.max.sm", "power.draw", "clocks_event_reasons.hw_slowdown",
+              "clocks_event_reasons.hw_thermal_slowdown", "clocks_event_reasons.sw_thermal_slowdown",
+              "clocks_event_reasons.sw_power_cap"]
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.lines = []
+        self.t = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + ",".join(self.FIELDS),
+                 "--format=csv,noheader,nounits", "-lms", "200"], stdout=subprocess.PIPE,
+                stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+            return
+        self.t = threading.Thread(target=self._read, daemon=True)
+        self.t.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        if self.t:
+            self.t.join(timeout=2)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[3:7]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except Exception:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+def profile_traffic(name: str):
+    """dram bytes per launch of a kernel from the committed ncu summary, if any."""
+    p = os.path.join(ROOT, "profiles", name)
+    try:
+        with open(p) as f:
+            for line in f:
+                if line.startswith("dram_bytes_per_frame_launch:"):
+                    return float(line.split(":", 1)[1].strip())
+    except Exception:
+        pass
+    return None
+
+
+# ---------------------------------------------------------------------------
+# CPU baseline: the oracle (the reference's loops in FP64, OpenMP) on a sample
+# ---------------------------------------------------------------------------
+
+def cpu_sample(sc, fw_rounds: int, row_stride: int):
+    """Times the reference's stages on the host cores on a bounded sample and
+    scales each to the full frame. Returns (ms_per_frame, detail)."""
+    import ctypes as C
+    from oracle import pyoracle as po
+    lib = po.load()
+    lib.lgo_fw_maxtimes_rounds.argtypes = [C.c_int, C.c_void_p, C.c_int, C.c_int]
+    o = po.Oracle(sc.density, sc.shader, sc.opts, sc.lights, temperature=sc.temperature, env_map=sc.env_map)
+    pts = sc.points[0]
+    n = len(pts)
+    det = {}
+    t = time.perf_counter()
+    adj, _ = o.build_graph(pts, sc.radius_sq[0], sc.max_connect)
+    det["build_graph"] = (time.perf_counter() - t) * 1e3
+    t = time.perf_counter()
+    T, S = o.march_edges(pts, adj)
+    det["edge_march"] = (time.perf_counter() - t) * 1e3
+    T2 = np.ascontiguousarray(T.copy())
+    k1 = min(n, fw_rounds)
+    t = time.perf_counter()
+    lib.lgo_fw_maxtimes_rounds(n, T2.ctypes.data, 0, k1)
+    det["floyd_warshall"] = (time.perf_counter() - t) * 1e3 * (n / k1)
+    # the rest of the chain needs the solved matrix: solve it outside the timer
+    # with the FP64 min-plus form (same result)
+    a = -np.array(sc.shader.getExtinction())
+    Sd = po.fw_minplus_f64(S)
+    Tsol = np.exp(-a[None, None, :] * Sd[:, :, None])
+    idx = np.arange(n)
+    Tsol[idx, idx, :] = 1.0
+    t = time.perf_counter()
+    L = o.vertex_light(pts)
+    det["vertex_light"] = (time.perf_counter() - t) * 1e3
+    t = time.perf_counter()
+    D = o.diffuse(Tsol, L)
+    det["diffuse"] = (time.perf_counter() - t) * 1e3
+    from lightgraph_gb300 import _capi
+    hp = _capi.load().lg_point_voxel_size(n, pts.ctypes.data, 8)
+    t = time.perf_counter()
+    lo, dims, sg, _ = o.splat(pts, D, hp)
+    det["splat"] = (time.perf_counter() - t) * 1e3
+    H = sc.opts.height
+    rows = list(range(0, H, row_stride))
+    t = time.perf_counter()
+    for r in rows:
+        o.render((lo, dims, sg), rows=(r, r + 1))
+    det["render"] = (time.perf_counter() - t) * 1e3 * (H / len(rows))
+    total = sum(det.values())
+    sample = (f"all of build/march/light/diffuse/splat; Floyd-Warshall rounds 0..{k1} of {n} scaled x{n / k1:.0f}; "
+              f"render rows every {row_stride} ({len(rows)} of {H}) scaled x{H / len(rows):.0f}")
+    return total, det, sample, o.threads()
+
+
+def run_reference(args):
+    rank, world, local = dist_env()
+    if rank != 0:
+        return 0
+    sc = make_scene(args.small)
+    fw_rounds, stride = (32, 256) if not args.small else (64, 32)
+    vals = []
+    for _ in range(args.warmup):
+        cpu_sample(sc, fw_rounds, stride)
+    det_acc = None
+    threads = 1
+    for _ in range(args.steps):
+        v, det, sample, threads = cpu_sample(sc, fw_rounds, stride)
+        vals.append(v)
+        det_acc = det
+    value = float(np.mean(vals))
+    line = {"metric": "ms/frame", "value": value, "unit": "ms", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": value, "higher_is_better": False, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
+            "config": workload_config(sc, args.small),
+            "cpu_baseline": {"value": value, "unit": "ms/frame", "cores": threads, "kind": "port",
+                             "sample": sample, "stages_ms": det_acc},
+            "e2e": {"value": value, "unit": "ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------
+
+def run_ours(args):
+    import torch
+    import torch.distributed as dist
+    from lightgraph_gb300 import Context, scenes
+
+    rank, world, local = dist_env()
+    if world > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    torch.cuda.set_device(local)
+    sc = make_scene(args.small)
+    ctx = Context(local)
+    scenes.load_into(ctx, sc)
+    ctx.build_graphs(sc.points, sc.radius_sq, sc.max_connect)
+    lib = ctx.lib
+    stream = torch.cuda.ExternalStream(ctx.stream)
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+
+    for _ in range(max(3, args.warmup)):
+        ctx.frame_device(sc.opts, sc.max_connect)
+    torch.cuda.synchronize()
+    prim, shad = ctx.render_stats()
+
+    # timed region: K frames, grids and points resident
+    lib.lg_set_profiling(ctx.h, 1)
+    import ctypes as C
+    stage_ms = np.zeros(len(STAGES))
+    launches0 = ctx.kernel_launches()
+    clocks = ClockSampler(local)
+    barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    buf = (C.c_double * len(STAGES))()
+    for _ in range(args.steps):
+        ctx.frame_device(sc.opts, sc.max_connect)
+        st = lib.lg_stage_times(ctx.h, buf, len(STAGES))
+        if st == 0:
+            stage_ms += np.array(buf[:])
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    clk = clocks.stop()
+    launches = ctx.kernel_launches() - launches0
+    lib.lg_set_profiling(ctx.h, 0)
+    t_ms = ev0.elapsed_time(ev1)
+    if world > 1:
+        tt = torch.tensor([t_ms], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_ms = float(tt.item())
+    ms_per_step = t_ms / args.steps
+    value = ms_per_step / world
+    stage_ms /= args.steps
+
+    # e2e through the C ABI from pinned host memory
+    pts = sc.points[0]
+    n = len(pts)
+    W, H = sc.opts.width, sc.opts.height
+    pin_pts = torch.from_numpy(np.ascontiguousarray(pts)).pin_memory()
+    offs = torch.tensor([0, n], dtype=torch.int64).pin_memory()
+    r2 = torch.tensor([float(sc.radius_sq[0])], dtype=torch.float32).pin_memory()
+    films = [torch.empty((H, W, 4), dtype=torch.float32).pin_memory() for _ in range(4)]
+    cam = sc.opts.camera_c()
+    for _ in range(1):
+        lib.lg_render_frame(ctx.h, 1, pin_pts.data_ptr(), offs.data_ptr(), r2.data_ptr(), sc.max_connect, 0.0,
+                            C.byref(cam), *[f.data_ptr() for f in films])
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        st = lib.lg_render_frame(ctx.h, 1, pin_pts.data_ptr(), offs.data_ptr(), r2.data_ptr(), sc.max_connect, 0.0,
+                                 C.byref(cam), *[f.data_ptr() for f in films])
+        if st != 0:
+            raise RuntimeError(lib.lg_last_error(ctx.h).decode())
+    e2e_ms = (time.perf_counter() - t0) * 1e3 / args.steps
+    if world > 1:
+        tt = torch.tensor([e2e_ms], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        e2e_ms = float(tt.item())
+    e2e_value = e2e_ms / world
+    h2d = pin_pts.numel() * 4 + offs.numel() * 8 + r2.numel() * 4
+    d2h = sum(f.numel() * 4 for f in films)
+
+    peaks, peak_kind = measured_peaks()
+    # dominant kernel: the render (k_render). Algorithmic bytes per launch:
+    # 8 taps x 4 B per density sample (primary + shadow) + 4 films x 16 B / px.
+    render_ms = stage_ms[6]
+    render_bytes = (prim + shad) * 32.0 + W * H * 64.0
+    achieved = render_bytes / (render_ms * 1e-3) / 1e9
+    ld = (len(pts) + 127) // 128 * 128  # the solve runs on the 128-padded matrix
+    fw_flops = 2.0 * ld ** 3
+    fw_tflops = fw_flops / (stage_ms[2] * 1e-3) / 1e12
+    line = {
+        "metric": "ms/frame", "value": value, "unit": "ms", "n_gpus": world, "steps": args.steps,
+        "warmup": max(3, args.warmup), "ms_per_step": ms_per_step, "higher_is_better": False, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded fBm volumes, uniform interior points)",
+        "config": workload_config(sc, args.small),
+        "e2e": {"value": e2e_value, "unit": "ms", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+        "gpu_launches": int(launches),
+        "clocks": clk,
+        "stages_ms": {k: round(float(v), 4) for k, v in zip(STAGES, stage_ms)},
+        "roofline": {"kernel": "k_render", "bound": "hbm", "achieved": achieved,
+                     "peak": peaks.get("hbm_gbs"), "unit": "GB/s",
+                     "frac": achieved / peaks.get("hbm_gbs"), "peak_kind": peak_kind,
+                     "traffic": profile_traffic("k_render_production.txt"),
+                     "algorithmic_bytes": render_bytes, "samples": {"primary": prim, "shadow": shad}},
+        "fw_roofline": {"kernel": "k_fw_update+k_fw_panels", "bound": "fp32_alu", "n": int(ld),
+                        "achieved": fw_tflops, "unit": "TFLOP/s", "peak": NOMINAL_FP32_TFLOPS,
+                        "peak_kind": "nominal (152 SMs x 128 lanes x 2 x 2.07 GHz)",
+                        "frac": fw_tflops / NOMINAL_FP32_TFLOPS},
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        fw_rounds, stride = (128, 64) if not args.small else (256, 16)
+        v, det, sample, threads = cpu_sample(sc, fw_rounds, stride)
+        line["cpu_baseline"] = {"value": v, "unit": "ms/frame", "cores": threads, "kind": "port",
+                                "sample": sample, "stages_ms": {k: round(x, 3) for k, x in det.items()}}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    if world > 1:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,332 @@
+/*
+ * lightgraph_c.h -- C ABI of the GB300-native LightGraph multiple-scattering path.
+ *
+ * The reference (asiroisvigneux/LightGraph) exposes its hot path as three C++
+ * classes compiled into one executable: LightGraph (src/LightGraph.h:32-153),
+ * ScatterGrid (src/ScatterGrid.h:20-56) and VolumeRender (src/Renderer.h:403-448).
+ * Every entry point below replaces one of their member functions; the comment on
+ * each names the reference function (file:line) it stands in for.
+ *
+ * Conventions
+ *  - Every call returns an lg_status (LG_OK == 0). On failure lg_last_error()
+ *    returns a NUL-terminated description owned by the context.
+ *  - Plain pointers and sizes only. Unless a name ends in _device, pointers are
+ *    HOST memory owned by the caller; the library copies in/out.
+ *  - A context owns one CUDA stream on one device. Calls on one context are
+ *    serialised by an internal mutex; use one context per host thread for
+ *    concurrency (the serving entry points overlap requests internally).
+ *  - All work is deterministic: the same inputs give bit-identical outputs,
+ *    independent of how many other requests share the GPU.
+ *  - World/index convention (OpenVDB linear transform, uniform voxels):
+ *      world = index * voxel_size + world_origin
+ *    Voxel centres sit at integer index coordinates. Leaves are the aligned
+ *    8^3 bricks of index space (index >> 3).
+ */
+#ifndef LIGHTGRAPH_C_H_
+#define LIGHTGRAPH_C_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int lg_status;
+#define LG_OK            0
+#define LG_ERR_INVALID   1  /* bad argument (null pointer, size, range)        */
+#define LG_ERR_CUDA      2  /* CUDA runtime failure                            */
+#define LG_ERR_NOMEM     3  /* device allocation failed or HBM budget exceeded */
+#define LG_ERR_STATE     4  /* call order (e.g. render before a grid upload)   */
+#define LG_ERR_TIMEOUT   5  /* a bounded device-side wait expired              */
+#define LG_ERR_NODEVICE  6  /* no CUDA device / extension built without GPU    */
+#define LG_ERR_BUSY      7  /* serving queue full                              */
+
+typedef struct lg_ctx lg_ctx;
+
+/* ------------------------------------------------------------------------- */
+/* Grids                                                                     */
+/* ------------------------------------------------------------------------- */
+
+#define LG_GRID_DENSITY      0
+#define LG_GRID_TEMPERATURE  1
+
+#define LG_DTYPE_F32   0
+#define LG_DTYPE_F16   1
+#define LG_DTYPE_BF16  2
+
+/* A FloatGrid handed over as a dense box of voxels.
+ * values[(z*dims[1] + y)*dims[0] + x] is the voxel at index
+ * (origin[0]+x, origin[1]+y, origin[2]+z). Voxels outside the box are the
+ * background value 0, as in a sparse VDB. origin must be a multiple of 8 so the
+ * box is made of whole leaves.
+ * leaf_mask (optional) marks which 8^3 leaves exist, one byte per leaf over
+ * ceil(dims/8), x fastest; NULL means "a leaf exists iff one of its voxels is
+ * non-zero", which is what converting a dense grid to a VDB produces. */
+typedef struct lg_grid_desc {
+    int32_t dims[3];
+    int32_t origin[3];
+    double  voxel_size;
+    double  world_origin[3];
+    const uint8_t* leaf_mask;
+} lg_grid_desc;
+
+/* Uploads a grid once into the device brick layout (8^3 bricks, one padding
+ * brick on every side, stored as storage_dtype; FP32 math on read). Replaces
+ * the openvdb::io::File::readGrid + GridSampler set-up at src/main.cc:486-502.
+ * Re-uploading replaces the previous grid of that kind. */
+lg_status lg_upload_grid(lg_ctx* ctx, int which, const lg_grid_desc* desc,
+                         const float* values, int storage_dtype);
+
+/* Drops the temperature grid (samples then read 0, like the empty grid the
+ * reference creates at src/main.cc:500). */
+lg_status lg_clear_temperature(lg_ctx* ctx);
+
+/* ------------------------------------------------------------------------- */
+/* Scene description                                                         */
+/* ------------------------------------------------------------------------- */
+
+#define LG_MAX_RAMP_KEYS 16
+#define LG_MAX_LIGHTS    8
+
+/* Shader (src/Shader.h:100-274). albedo and extinction are the derived values
+ * (Shader::recomputeAlbedo/recomputeExtinction, src/Shader.h:205-211); the
+ * caller computes them, exactly as the reference setters do. */
+typedef struct lg_shader {
+    double density_scale;
+    double density_max;
+    double shadow_density_scale;
+    double scatter_density_scale;
+    double scatter_density_min;
+    double scattering[3];
+    double albedo[3];
+    double extinction[3];          /* <= 0 per channel: -(scattering+absorption) */
+    double emission_scale;
+    double scatter_scale;
+    double scatter_density_mask_power;
+    int32_t ramp_n;                /* 0: ColorRamp with no keys (black)          */
+    int32_t _pad0;
+    double ramp_pos[LG_MAX_RAMP_KEYS];
+    double ramp_color[LG_MAX_RAMP_KEYS][3];
+    double ramp_in;
+    double ramp_out;
+} lg_shader;
+
+#define LG_LIGHT_DISTANT 0
+#define LG_LIGHT_POINT   1
+#define LG_LIGHT_ENV     2
+
+/* One light (src/Light.h:26-235) with its transform already applied:
+ *  DISTANT: dir = normalised xform.transform(0,0,-1) (DistantLight::mDir)
+ *  POINT:   pos = xform.transform(pos)               (PointLight::mPos)
+ *  ENV:     rot = 3x3 row-vector rotation applied to sampled directions
+ *           (EnvLight::mXform); the map comes from lg_set_lights. */
+typedef struct lg_light {
+    int32_t type;
+    int32_t samples;               /* Light::mSamples (1 for distant/point)      */
+    double  color[3];
+    double  intensity;             /* Light::mIntensity (a float in the reference) */
+    double  dir[3];
+    double  pos[3];
+    double  rot[9];
+} lg_light;
+
+/* Sets the lights. env_rgb (optional, env_h rows x env_w cols x RGB, row 0 at
+ * phi = 0) is the environment map shared by ENV lights; its importance-sampling
+ * CDFs (src/Sampling.h:76-167, src/Light.h:150-177) are built on the device
+ * with FP64 prefix sums. */
+lg_status lg_set_lights(lg_ctx* ctx, const lg_light* lights, int n_lights,
+                        const float* env_rgb, int env_w, int env_h);
+
+lg_status lg_set_shader(lg_ctx* ctx, const lg_shader* shader);
+
+/* SceneSettings fields the hot path reads (src/SceneSettings.h:21-63), plus
+ * the seed of the counter-based random streams that replace RandGen. */
+typedef struct lg_settings {
+    double   cutoff;
+    double   step[2];              /* primary, shadow step in voxels             */
+    int32_t  iter;                 /* number of LightGraphs (splat kernel size)  */
+    int32_t  scatter_grid_res_factor;
+    int32_t  pts_per_kernel;
+    int32_t  _pad0;
+    uint64_t seed;
+} lg_settings;
+
+lg_status lg_set_settings(lg_ctx* ctx, const lg_settings* settings);
+
+/* PerspectiveCamera (src/Renderer.h:129-248) as main.cc:96-102 builds it. */
+typedef struct lg_camera {
+    double  rotate[3];             /* degrees, X then Y then Z (camRotate)       */
+    double  translate[3];          /* camTranslate                               */
+    double  y_rotate;              /* camYRotate (turntable, degrees)            */
+    double  focal;                 /* mm                                         */
+    double  aperture;              /* mm                                         */
+    double  znear;
+    double  zfar;
+    int32_t width;
+    int32_t height;
+    int32_t samples;               /* antialiasing samples per pixel            */
+    int32_t _pad0;
+} lg_camera;
+
+/* ------------------------------------------------------------------------- */
+/* Context                                                                   */
+/* ------------------------------------------------------------------------- */
+
+lg_status lg_create(int device, lg_ctx** out);
+lg_status lg_destroy(lg_ctx* ctx);
+const char* lg_last_error(const lg_ctx* ctx);
+/* The context's cudaStream_t, for callers that time with CUDA events. */
+void* lg_stream(lg_ctx* ctx);
+/* Library version string and the number of kernel launches issued so far. */
+const char* lg_version(void);
+uint64_t lg_kernel_launches(const lg_ctx* ctx);
+
+/* ------------------------------------------------------------------------- */
+/* Stage 1: LightGraph solve (LightGraph::operator(), src/LightGraph.h:158-196) */
+/* ------------------------------------------------------------------------- */
+
+/* Loads n_graphs point sets (the output of LightGraph::scatterPoints,
+ * src/LightGraph.h:206-274, injected by the caller) and connects each with the
+ * reference's greedy rule: pairs closer than sqrt(radius_sq[g]) in FP64, at
+ * most max_connect edges per point, decided in (i, j) order.
+ * Replaces LightGraph::buildGraph (src/LightGraph.h:287-318).
+ *   points  : sum(N_g) x 3 floats, graph g occupies rows offsets[g]..offsets[g+1]
+ *   radius_sq: per graph, the FP32 value searchRadiusConnectSquared
+ *   adj_out : optional, sum(N_g^2) bytes, graph g row-major at sum_{h<g} N_h^2
+ *   n_edges_out: optional, per graph edge count (connectCount) */
+lg_status lg_build_graphs(lg_ctx* ctx, int n_graphs, const float* points,
+                          const int64_t* offsets, const float* radius_sq,
+                          int max_connect, uint8_t* adj_out, int64_t* n_edges_out);
+
+/* Ray-marches every edge of the loaded graphs into a scalar optical depth
+ * S_ij = sum over samples of max(rho, densityMin) * step (voxel units), so the
+ * reference's RGB edge transmittance is T_c = exp(extinction_c * S_ij); no edge,
+ * a bbox miss or a dropout gives +inf (T = 0).
+ * Replaces LightGraph::raymarchConnection (src/LightGraph.h:347-418).
+ *   S_out: optional, sum(N_g^2) floats (graph-major, row-major). */
+lg_status lg_march_edges(lg_ctx* ctx, float* S_out);
+
+/* All-pairs most-transmissive paths: min-plus Floyd-Warshall over S on the
+ * device (equal to the reference's per-channel max-times FW on T because every
+ * channel is exp(-a_c * S)), then the diagonal is set to 0 (T = 1).
+ * Replaces LightGraph::floydAlgo (src/LightGraph.h:512-542).
+ *   dist_out: optional, sum(N_g^2) floats. */
+lg_status lg_solve_paths(lg_ctx* ctx, float* dist_out);
+
+/* Direct lighting plus emission per vertex.
+ * Replaces LightGraph::computeLighting (src/LightGraph.h:427-505).
+ *   light_out: optional, sum(N_g) x 3 floats. */
+lg_status lg_vertex_light(lg_ctx* ctx, float* light_out);
+
+/* Column-normalised diffusion of vertex radiance through the path matrix.
+ * Replaces LightGraph::diffuseLight (src/LightGraph.h:554-587).
+ *   diffuse_out: optional, sum(N_g) x 3 floats (mDiffusePointGather). */
+lg_status lg_diffuse(lg_ctx* ctx, float* diffuse_out);
+
+/* Runs lg_march_edges, lg_solve_paths, lg_vertex_light and lg_diffuse. */
+lg_status lg_solve_graphs(lg_ctx* ctx, float* diffuse_out);
+
+/* ------------------------------------------------------------------------- */
+/* Stage 2: ScatterGrid (src/ScatterGrid.h:61-144, src/LightGraph.h:706-755)  */
+/* ------------------------------------------------------------------------- */
+
+/* Builds the coarse scatter grid (voxel = density voxel * res_factor, topology
+ * = coarse voxels covering an active density voxel, dilated by one) and splats
+ * every solved vertex into it with the truncated Gaussian of ScatterGrid.
+ *   point_voxel_size: voxel size of the point index (computeVoxelSize at
+ *   src/LightGraph.h:714); <= 0 selects lg_point_voxel_size() of the points. */
+lg_status lg_splat(lg_ctx* ctx, double point_voxel_size);
+
+/* The estimate used when lg_splat gets point_voxel_size <= 0: the edge of a
+ * cube holding points_per_voxel points on average over the points' bbox. */
+double lg_point_voxel_size(int64_t n_points, const float* points, int points_per_voxel);
+
+/* Copies out the scatter grid: dims/origin of the coarse dense box and, if
+ * values is non-null, dims[0]*dims[1]*dims[2]*3 floats (0 = inactive). */
+lg_status lg_get_scatter_grid(lg_ctx* ctx, int32_t dims[3], int32_t origin[3],
+                              float* values);
+
+/* Vertex light / diffuse radiance of all loaded points (sum(N_g) x 3). */
+lg_status lg_get_vertex_data(lg_ctx* ctx, float* light_out, float* diffuse_out);
+
+/* ------------------------------------------------------------------------- */
+/* Stage 3: render (VolumeRender::render / operator(), src/Renderer.h:496-693) */
+/* ------------------------------------------------------------------------- */
+
+/* Renders the four films of the reference (Film::RGBA, width x height x 4
+ * floats each): beauty RGBA, and the direct, scatter and emission AOVs with
+ * alpha 0. Any output pointer may be null. */
+lg_status lg_render(lg_ctx* ctx, const lg_camera* camera, float* rgba,
+                    float* direct, float* scatter, float* emission);
+
+/* One whole frame: lg_build_graphs + lg_solve_graphs + lg_splat + lg_render. */
+lg_status lg_render_frame(lg_ctx* ctx, int n_graphs, const float* points,
+                          const int64_t* offsets, const float* radius_sq,
+                          int max_connect, double point_voxel_size,
+                          const lg_camera* camera, float* rgba, float* direct,
+                          float* scatter, float* emission);
+
+/* Device-resident variant of lg_render_frame for timing: points already on the
+ * device (loaded by a previous lg_build_graphs), outputs stay in device memory.
+ * Enqueues the whole frame on the context stream and returns without waiting. */
+lg_status lg_frame_device(lg_ctx* ctx, int max_connect, double point_voxel_size,
+                          const lg_camera* camera);
+
+/* Statistics of the last render on this context (after a sync): number of
+ * density samples taken by primary and shadow rays. */
+lg_status lg_render_stats(lg_ctx* ctx, uint64_t* primary_samples,
+                          uint64_t* shadow_samples);
+
+/* Stage timing of lg_frame_device, the equivalent of the reference's
+ * tbb::tick_count prints (src/main.cc:553,589,125, src/LightGraph.h:268-585):
+ * when on, CUDA events are recorded on the context stream around each stage.
+ * lg_stage_times waits for the last profiled frame and writes up to n stage
+ * durations in ms: build graph, edge march, Floyd-Warshall, vertex light,
+ * diffusion, splat, render. */
+lg_status lg_set_profiling(lg_ctx* ctx, int on);
+lg_status lg_stage_times(lg_ctx* ctx, double* ms, int n);
+
+/* ------------------------------------------------------------------------- */
+/* Kernel-level entry points (device pointers, caller's stream)              */
+/* ------------------------------------------------------------------------- */
+
+/* In-place min-plus Floyd-Warshall of one n x n FP32 matrix with leading
+ * dimension ld (floats) in device memory, enqueued on `stream`
+ * (a cudaStream_t; NULL = legacy default stream). No allocation.
+ * Replaces LightGraph::floydAlgo (src/LightGraph.h:516-528) without the final
+ * diagonal reset. */
+lg_status lg_fw_device(float* dist, int n, int ld, void* stream);
+
+/* Host-memory convenience wrapper of lg_fw_device (copies in and out). */
+lg_status lg_fw_host(lg_ctx* ctx, float* dist, int n);
+
+/* ------------------------------------------------------------------------- */
+/* Host helpers: the reference's scene description (no device work)          */
+/* ------------------------------------------------------------------------- */
+
+/* Shader() defaults (src/Shader.h:123-138). */
+void lg_shader_default(lg_shader* shader);
+/* setAbsorption/setScattering/setVolumeColor (src/Shader.h:165-211): stores
+ * scattering and recomputes albedo = color*scattering/(scattering+absorption)
+ * and extinction = -(scattering+absorption). */
+void lg_shader_set_coefficients(lg_shader* shader, const double absorption[3],
+                                const double scattering[3], const double volume_color[3]);
+/* SceneSettings() defaults (src/SceneSettings.h:40-61) with seed 0. */
+void lg_settings_default(lg_settings* settings);
+/* PerspectiveCamera/SceneSettings camera defaults (50 mm, 36 mm aperture,
+ * znear 1e-3, zfar FLT_MAX, 960x540, 1 sample). */
+void lg_camera_default(lg_camera* camera);
+/* parseLight (src/main.cc:234-274): "dir:yRot:r,g,b:intensity:rx,ry,rz" and
+ * "env:yRot:r,g,b:intensity:samples:file" (the map itself is passed to
+ * lg_set_lights), plus "point:yRot:r,g,b:intensity:x,y,z" for the reference's
+ * PointLight, which has no command-line syntax there. */
+lg_status lg_parse_light(const char* spec, lg_light* out);
+/* parseColorRamp (src/main.cc:280-319): "p0,p1,../r,g,b:r,g,b:../in/out". */
+lg_status lg_parse_color_ramp(const char* spec, lg_shader* shader);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* LIGHTGRAPH_C_H_ */

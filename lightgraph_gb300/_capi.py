@@ -1,0 +1,150 @@
+"""ctypes binding of include/lightgraph_c.h and include/lightgraph_scene.h.
+
+The shared library is built in-tree (lightgraph_gb300/_build) by
+``lightgraph_gb300.build``; importing this module without it raises, so the
+GPU path can never silently fall back to anything else.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+from . import build as _build
+
+LG_OK = 0
+LG_ERR_INVALID = 1
+LG_ERR_CUDA = 2
+LG_ERR_NOMEM = 3
+LG_ERR_STATE = 4
+LG_ERR_TIMEOUT = 5
+LG_ERR_NODEVICE = 6
+LG_ERR_BUSY = 7
+
+LG_GRID_DENSITY = 0
+LG_GRID_TEMPERATURE = 1
+LG_DTYPE_F32, LG_DTYPE_F16, LG_DTYPE_BF16 = 0, 1, 2
+LG_LIGHT_DISTANT, LG_LIGHT_POINT, LG_LIGHT_ENV = 0, 1, 2
+LG_MAX_RAMP_KEYS = 16
+LG_MAX_LIGHTS = 8
+
+LGS_VOLUME_SPHERE_FBM = 0
+LGS_VOLUME_CUMULUS = 1
+LGS_VOLUME_TEMPERATURE = 2
+
+_ERRORS = {1: "invalid argument", 2: "CUDA error", 3: "out of device memory", 4: "call order",
+           5: "device wait timed out", 6: "no CUDA device", 7: "queue full"}
+
+
+class GridDesc(C.Structure):
+    _fields_ = [("dims", C.c_int32 * 3), ("origin", C.c_int32 * 3), ("voxel_size", C.c_double),
+                ("world_origin", C.c_double * 3), ("leaf_mask", C.c_void_p)]
+
+
+class ShaderC(C.Structure):
+    _fields_ = [("density_scale", C.c_double), ("density_max", C.c_double),
+                ("shadow_density_scale", C.c_double), ("scatter_density_scale", C.c_double),
+                ("scatter_density_min", C.c_double), ("scattering", C.c_double * 3),
+                ("albedo", C.c_double * 3), ("extinction", C.c_double * 3),
+                ("emission_scale", C.c_double), ("scatter_scale", C.c_double),
+                ("scatter_density_mask_power", C.c_double), ("ramp_n", C.c_int32), ("_pad0", C.c_int32),
+                ("ramp_pos", C.c_double * LG_MAX_RAMP_KEYS), ("ramp_color", (C.c_double * 3) * LG_MAX_RAMP_KEYS),
+                ("ramp_in", C.c_double), ("ramp_out", C.c_double)]
+
+
+class LightC(C.Structure):
+    _fields_ = [("type", C.c_int32), ("samples", C.c_int32), ("color", C.c_double * 3),
+                ("intensity", C.c_double), ("dir", C.c_double * 3), ("pos", C.c_double * 3),
+                ("rot", C.c_double * 9)]
+
+
+class SettingsC(C.Structure):
+    _fields_ = [("cutoff", C.c_double), ("step", C.c_double * 2), ("iter", C.c_int32),
+                ("scatter_grid_res_factor", C.c_int32), ("pts_per_kernel", C.c_int32), ("_pad0", C.c_int32),
+                ("seed", C.c_uint64)]
+
+
+class CameraC(C.Structure):
+    _fields_ = [("rotate", C.c_double * 3), ("translate", C.c_double * 3), ("y_rotate", C.c_double),
+                ("focal", C.c_double), ("aperture", C.c_double), ("znear", C.c_double), ("zfar", C.c_double),
+                ("width", C.c_int32), ("height", C.c_int32), ("samples", C.c_int32), ("_pad0", C.c_int32)]
+
+
+P = C.c_void_p
+I32, I64, U64, D, F = C.c_int32, C.c_int64, C.c_uint64, C.c_double, C.c_float
+
+# name -> (restype, argtypes). Every symbol of include/lightgraph_c.h and
+# include/lightgraph_scene.h is listed; tests check the library exports them.
+SIGNATURES = {
+    "lg_create": (I32, [C.c_int, C.POINTER(P)]),
+    "lg_destroy": (I32, [P]),
+    "lg_last_error": (C.c_char_p, [P]),
+    "lg_stream": (P, [P]),
+    "lg_version": (C.c_char_p, []),
+    "lg_kernel_launches": (U64, [P]),
+    "lg_upload_grid": (I32, [P, C.c_int, C.POINTER(GridDesc), P, C.c_int]),
+    "lg_clear_temperature": (I32, [P]),
+    "lg_set_lights": (I32, [P, C.POINTER(LightC), C.c_int, P, C.c_int, C.c_int]),
+    "lg_set_shader": (I32, [P, C.POINTER(ShaderC)]),
+    "lg_set_settings": (I32, [P, C.POINTER(SettingsC)]),
+    "lg_build_graphs": (I32, [P, C.c_int, P, P, P, C.c_int, P, P]),
+    "lg_march_edges": (I32, [P, P]),
+    "lg_solve_paths": (I32, [P, P]),
+    "lg_vertex_light": (I32, [P, P]),
+    "lg_diffuse": (I32, [P, P]),
+    "lg_solve_graphs": (I32, [P, P]),
+    "lg_splat": (I32, [P, D]),
+    "lg_point_voxel_size": (D, [I64, P, C.c_int]),
+    "lg_get_scatter_grid": (I32, [P, P, P, P]),
+    "lg_get_vertex_data": (I32, [P, P, P]),
+    "lg_render": (I32, [P, C.POINTER(CameraC), P, P, P, P]),
+    "lg_render_frame": (I32, [P, C.c_int, P, P, P, C.c_int, D, C.POINTER(CameraC), P, P, P, P]),
+    "lg_frame_device": (I32, [P, C.c_int, D, C.POINTER(CameraC)]),
+    "lg_render_stats": (I32, [P, C.POINTER(U64), C.POINTER(U64)]),
+    "lg_set_profiling": (I32, [P, C.c_int]),
+    "lg_stage_times": (I32, [P, C.POINTER(D), C.c_int]),
+    "lg_fw_device": (I32, [P, C.c_int, C.c_int, P]),
+    "lg_fw_host": (I32, [P, P, C.c_int]),
+    "lg_shader_default": (None, [C.POINTER(ShaderC)]),
+    "lg_shader_set_coefficients": (None, [C.POINTER(ShaderC), C.POINTER(D), C.POINTER(D), C.POINTER(D)]),
+    "lg_settings_default": (None, [C.POINTER(SettingsC)]),
+    "lg_camera_default": (None, [C.POINTER(CameraC)]),
+    "lg_parse_light": (I32, [C.c_char_p, C.POINTER(LightC)]),
+    "lg_parse_color_ramp": (I32, [C.c_char_p, C.POINTER(ShaderC)]),
+    "lgs_volume": (I64, [C.c_int, C.c_int, C.c_int, U64, D, P, P]),
+    "lgs_points": (I64, [P, C.c_int, D, I64, U64, D, I64, P]),
+    "lgs_envmap": (None, [C.c_int, C.c_int, D, D, D, D, P]),
+}
+
+_lib = None
+
+
+def load() -> C.CDLL:
+    """Load the in-tree library; raise if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = _build.lib_path()
+    if not os.path.exists(path):
+        raise ImportError(
+            f"lightgraph_gb300 native library missing at {path}; run "
+            "`python -c 'import __graft_entry__ as g; g.build()'` (needs nvcc for sm_103a)")
+    lib = C.CDLL(path)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+class LightGraphError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"{_ERRORS.get(status, 'error')} ({status}): {msg}")
+        self.status = status
+
+
+def ptr(a) -> int | None:
+    """Data pointer of a numpy array (or None)."""
+    if a is None:
+        return None
+    return a.ctypes.data

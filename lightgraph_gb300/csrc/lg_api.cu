@@ -1,0 +1,993 @@
+// C ABI of the LightGraph path (include/lightgraph_c.h): context, grid upload,
+// scene state and the stage entry points that replace the reference's
+// LightGraph / ScatterGrid / VolumeRender member functions.
+#include <algorithm>
+#include <climits>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "lg_ctx.h"
+
+namespace lg {
+uint64_t g_launch_counter = 0;
+}
+
+using namespace lg;
+
+// ---------------------------------------------------------------------------
+// helpers
+// ---------------------------------------------------------------------------
+
+lg_status Ctx::fail(lg_status s, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    err = buf;
+    return s;
+}
+
+lg_status Ctx::cuda(cudaError_t e, const char* what) {
+    if (e == cudaSuccess) return LG_OK;
+    if (e == cudaErrorMemoryAllocation) {
+        cudaGetLastError();
+        return fail(LG_ERR_NOMEM, "%s: %s", what, cudaGetErrorString(e));
+    }
+    return fail(LG_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+#define CK(expr, what)                                         \
+    do {                                                       \
+        const lg_status _s = ctx->cuda((expr), (what));        \
+        if (_s != LG_OK) return _s;                            \
+    } while (0)
+
+#define GUARD(ctx)                                             \
+    if (!(ctx)) return LG_ERR_INVALID;                         \
+    std::lock_guard<std::mutex> _lock((ctx)->mu);              \
+    {                                                          \
+        const cudaError_t _e = cudaSetDevice((ctx)->device);   \
+        if (_e != cudaSuccess) return (ctx)->cuda(_e, "cudaSetDevice"); \
+    }
+
+static int round_up(int v, int m) { return (v + m - 1) / m * m; }
+
+static int floor_div(int a, int b) { return (a >= 0) ? a / b : -((-a + b - 1) / b); }
+
+// Optical depth where sum_c exp(-2 a_c tau) first drops below cutoff (the
+// reference's sTrans.lengthSqr() < cutoff, src/LightGraph.h:396).
+static float dropout_depth(const double a[3], double cutoff) {
+    auto f = [&](double t) {
+        double s = 0;
+        for (int c = 0; c < 3; ++c) s += std::exp(-2.0 * a[c] * t);
+        return s;
+    };
+    if (f(0.0) < cutoff) return -1.f;  // drops at the first contributing sample
+    int zero = 0;
+    for (int c = 0; c < 3; ++c) zero += (a[c] == 0.0);
+    if ((double)zero >= cutoff) return INFINITY;  // never drops
+    double lo = 0.0, hi = 1.0;
+    while (f(hi) >= cutoff) hi *= 2.0;
+    for (int it = 0; it < 200; ++it) {
+        const double mid = 0.5 * (lo + hi);
+        if (f(mid) < cutoff) hi = mid; else lo = mid;
+    }
+    return (float)lo;
+}
+
+// math::rotation<Mat4d>(axis, angle), 3x3 part (row-vector convention).
+static void rotation(int axis, double ang, double R[3][3]) {
+    const double c = std::cos(ang), s = std::sin(ang);
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) R[i][j] = (i == j) ? 1.0 : 0.0;
+    if (axis == 0) { R[1][1] = c; R[1][2] = s; R[2][1] = -s; R[2][2] = c; }
+    else if (axis == 1) { R[0][0] = c; R[0][2] = -s; R[2][0] = s; R[2][2] = c; }
+    else { R[0][0] = c; R[0][1] = s; R[1][0] = -s; R[1][1] = c; }
+}
+
+static void matmul3(const double A[3][3], const double B[3][3], double C[3][3]) {
+    double T[3][3];
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) T[i][j] = A[i][0] * B[0][j] + A[i][1] * B[1][j] + A[i][2] * B[2][j];
+    std::memcpy(C, T, sizeof T);
+}
+
+// AffineMap::accumPostRotation -> Mat4::postRotate, which rotates clockwise:
+// M <- M * rotation(axis, -angle).
+static void post_rotate(double M[3][3], int axis, double ang) {
+    double R[3][3];
+    rotation(axis, -ang, R);
+    matmul3(M, R, M);
+}
+
+// PerspectiveCamera as main.cc:96-102 builds it (src/Renderer.h:148-171,232-239).
+static DevCamera make_camera(const lg_camera& c) {
+    const double d2r = 3.14159265358979323846 / 180.0;
+    double M[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+    post_rotate(M, 0, c.rotate[0] * d2r);
+    post_rotate(M, 1, (c.rotate[1] + c.y_rotate) * d2r);
+    post_rotate(M, 2, c.rotate[2] * d2r);
+    double Ry[3][3];
+    rotation(1, c.y_rotate * d2r, Ry);  // yRotXform (src/main.cc:68-70)
+    double t[3];
+    for (int j = 0; j < 3; ++j)
+        t[j] = c.translate[0] * Ry[0][j] + c.translate[1] * Ry[1][j] + c.translate[2] * Ry[2][j];
+    DevCamera cam{};
+    for (int j = 0; j < 3; ++j) {
+        cam.eye[j] = (float)t[j];
+        cam.cdir[j] = (float)(-M[2][j]);
+        for (int i = 0; i < 3; ++i) cam.m[i * 3 + j] = (float)M[i][j];
+    }
+    const double sw = 0.5 * c.aperture / c.focal;
+    cam.sw = (float)sw;
+    cam.sh = (float)(sw * (double)c.height / (double)c.width);
+    cam.znear = (float)c.znear;
+    cam.zfar = (float)c.zfar;
+    cam.width = c.width;
+    cam.height = c.height;
+    cam.spp = c.samples;
+    return cam;
+}
+
+// ---------------------------------------------------------------------------
+// context
+// ---------------------------------------------------------------------------
+
+extern "C" lg_status lg_create(int device, lg_ctx** out) {
+    if (!out) return LG_ERR_INVALID;
+    *out = nullptr;
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) {
+        cudaGetLastError();
+        return LG_ERR_NODEVICE;
+    }
+    if (device < 0 || device >= n) return LG_ERR_INVALID;
+    if (cudaSetDevice(device) != cudaSuccess) return LG_ERR_CUDA;
+    Ctx* ctx = new Ctx();
+    ctx->device = device;
+    if (cudaStreamCreateWithFlags(&ctx->st, cudaStreamNonBlocking) != cudaSuccess) {
+        delete ctx;
+        return LG_ERR_CUDA;
+    }
+    // defaults: Shader() and SceneSettings() of the reference
+    lg_shader& s = ctx->shader;
+    std::memset(&s, 0, sizeof s);
+    s.density_scale = 1.0;
+    s.density_max = 100.0;
+    s.shadow_density_scale = 1.0;
+    s.scatter_density_scale = 0.35;
+    s.scatter_density_min = 0.025;
+    for (int c = 0; c < 3; ++c) {
+        s.scattering[c] = 1.5;
+        s.albedo[c] = 1.5 / 1.6;
+        s.extinction[c] = -1.6;
+    }
+    s.emission_scale = 0.0;
+    s.scatter_scale = 4.0;
+    s.scatter_density_mask_power = 0.25;
+    s.ramp_in = 0.0;
+    s.ramp_out = 1.0;
+    lg_settings& o = ctx->settings;
+    std::memset(&o, 0, sizeof o);
+    o.cutoff = 0.005;
+    o.step[0] = 1.0;
+    o.step[1] = 3.0;
+    o.iter = 1;
+    o.scatter_grid_res_factor = 4;
+    o.pts_per_kernel = 3;
+    o.seed = 0;
+    *out = reinterpret_cast<lg_ctx*>(ctx);
+    return LG_OK;
+}
+
+extern "C" lg_status lg_destroy(lg_ctx* handle) {
+    Ctx* ctx = reinterpret_cast<Ctx*>(handle);
+    if (!ctx) return LG_ERR_INVALID;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->st);
+    if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
+    for (int k = 0; k <= Ctx::kStages; ++k)
+        if (ctx->ev[k]) cudaEventDestroy(ctx->ev[k]);
+    cudaStreamDestroy(ctx->st);
+    delete ctx;
+    return LG_OK;
+}
+
+extern "C" const char* lg_last_error(const lg_ctx* handle) {
+    const Ctx* ctx = reinterpret_cast<const Ctx*>(handle);
+    return ctx ? ctx->err.c_str() : "null context";
+}
+
+extern "C" void* lg_stream(lg_ctx* handle) {
+    Ctx* ctx = reinterpret_cast<Ctx*>(handle);
+    return ctx ? (void*)ctx->st : nullptr;
+}
+
+extern "C" const char* lg_version(void) { return "lightgraph_gb300 1.0 (sm_103a)"; }
+
+extern "C" uint64_t lg_kernel_launches(const lg_ctx*) { return g_launch_counter; }
+
+// ---------------------------------------------------------------------------
+// grids
+// ---------------------------------------------------------------------------
+
+lg_status Ctx::upload_grid(int which, const lg_grid_desc* desc, const float* values, int dtype) {
+    Ctx* ctx = this;
+    if (!desc || !values) return fail(LG_ERR_INVALID, "null grid descriptor or values");
+    if (which != LG_GRID_DENSITY && which != LG_GRID_TEMPERATURE) return fail(LG_ERR_INVALID, "bad grid kind %d", which);
+    if (dtype < 0 || dtype > 2) return fail(LG_ERR_INVALID, "bad storage dtype %d", dtype);
+    for (int a = 0; a < 3; ++a) {
+        if (desc->dims[a] <= 0 || desc->dims[a] > (1 << 20)) return fail(LG_ERR_INVALID, "bad grid dims");
+        if (desc->origin[a] % 8 != 0) return fail(LG_ERR_INVALID, "grid origin must be a multiple of 8");
+    }
+    if (!(desc->voxel_size > 0.0)) return fail(LG_ERR_INVALID, "voxel size must be > 0");
+    GridStore& gs = which == LG_GRID_DENSITY ? dens : temp;
+    gs.valid = false;
+    DevGrid g;
+    g.dtype = dtype;
+    int nleaf[3];
+    for (int a = 0; a < 3; ++a) {
+        nleaf[a] = (desc->dims[a] + 7) / 8;
+        g.blo[a] = floor_div(desc->origin[a], 8) - 1;
+        g.nb[a] = nleaf[a] + 2;
+        g.wo[a] = (float)desc->world_origin[a];
+    }
+    g.h = (float)desc->voxel_size;
+    g.inv_h = (float)(1.0 / desc->voxel_size);
+    const int64_t nvox = (int64_t)desc->dims[0] * desc->dims[1] * desc->dims[2];
+    const int64_t nbt = (int64_t)g.nb[0] * g.nb[1] * g.nb[2];
+    const size_t esz = dtype == 0 ? 4 : 2;
+    CK(staging.reserve(sizeof(float) * nvox), "grid staging alloc");
+    CK(cudaMemcpyAsync(staging.p, values, sizeof(float) * nvox, cudaMemcpyHostToDevice, st), "grid upload");
+    CK(gs.bricks.reserve(esz * nbt * 512), "brick alloc");
+    CK(gs.bits.reserve(sizeof(uint32_t) * ((nbt + 31) / 32 + 1)), "leaf bitmap alloc");
+    CK(cudaMemsetAsync(gs.bits.p, 0, sizeof(uint32_t) * ((nbt + 31) / 32 + 1), st), "leaf bitmap clear");
+    const uint8_t* d_mask = nullptr;
+    if (desc->leaf_mask) {
+        const int64_t nl = (int64_t)nleaf[0] * nleaf[1] * nleaf[2];
+        CK(mask_staging.reserve(nl), "leaf mask alloc");
+        CK(cudaMemcpyAsync(mask_staging.p, desc->leaf_mask, nl, cudaMemcpyHostToDevice, st), "leaf mask upload");
+        d_mask = mask_staging.as<uint8_t>();
+    }
+    int bbox_init[6] = {INT_MAX, INT_MAX, INT_MAX, INT_MIN, INT_MIN, INT_MIN};
+    CK(small.reserve(64), "small alloc");
+    CK(cudaMemcpyAsync(small.p, bbox_init, sizeof bbox_init, cudaMemcpyHostToDevice, st), "bbox init");
+    g.data = gs.bricks.p;
+    g.leafbits = gs.bits.as<uint32_t>();
+    CK(launch_pack_bricks(staging.as<float>(), desc->dims, desc->origin, g, gs.bricks.p, st), "pack bricks");
+    CK(launch_leaf_bits(staging.as<float>(), desc->dims, desc->origin, d_mask, g, gs.bits.as<uint32_t>(),
+                        small.as<int>(), st), "leaf bitmap");
+    int bbox[6];
+    CK(cudaMemcpyAsync(bbox, small.p, sizeof bbox, cudaMemcpyDeviceToHost, st), "bbox download");
+    CK(cudaStreamSynchronize(st), "grid upload sync");
+    staging.release();
+    g.has_leaves = bbox[0] <= bbox[3];
+    for (int a = 0; a < 3; ++a) {
+        g.bbmin[a] = g.has_leaves ? (float)(bbox[a] * 8) : 0.f;
+        g.bbmax[a] = g.has_leaves ? (float)(bbox[3 + a] * 8 + 8) : 0.f;
+    }
+    gs.g = g;
+    gs.desc = *desc;
+    gs.desc.leaf_mask = nullptr;
+    gs.valid = true;
+    ++gs.version;
+    return LG_OK;
+}
+
+extern "C" lg_status lg_upload_grid(lg_ctx* handle, int which, const lg_grid_desc* desc,
+                                    const float* values, int storage_dtype) {
+    Ctx* ctx = reinterpret_cast<Ctx*>(handle);
+    GUARD(ctx);
+    return ctx->upload_grid(which, desc, values, storage_dtype);
+}
+
+extern "C" lg_status lg_clear_temperature(lg_ctx* handle) {
+    Ctx* ctx = reinterpret_cast<Ctx*>(handle);
+    GUARD(ctx);
+    ctx->temp.valid = false;
+    return LG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// scene state
+// ---------------------------------------------------------------------------
+
+extern "C" lg_status lg_set_shader(lg_ctx* handle, const lg_shader* s) {
+    Ctx* ctx = reinterpret_cast<Ctx*>(handle);
+    GUARD(ctx);
+    if (!s) return ctx->fail(LG_ERR_INVALID, "null shader");
+    if (s->ramp_n < 0 || s->ramp_n > LG_MAX_RAMP_KEYS) return ctx->fail(LG_ERR_INVALID, "ramp_n out of range");
+    for (int c = 0; c < 3; ++c)
+        if (!(s->extinction[c] <= 0.0))
+            return ctx->fail(LG_ERR_INVALID, "extinction must be <= 0 per channel (got %g)", s->extinction[c]);
+    ctx->shader = *s;
+    return LG_OK;
+}
+
+extern "C" lg_status lg_set_settings(lg_ctx* handle, const lg_settings* o) {
+    Ctx* ctx = reinterpret_cast<Ctx*>(handle);
+    GUARD(ctx);
+    if (!o) return ctx->fail(LG_ERR_INVALID, "null settings");
+    if (!(o->step[0] > 0.0) || !(o->step[1] > 0.0)) return ctx->fail(LG_ERR_INVALID, "steps must be > 0");
+    if (o->scatter_grid_res_factor < 1) return ctx->fail(LG_ERR_INVALID, "scatterGridResFactor must be >= 1");
+    if (o->iter < 1) return ctx->fail(LG_ERR_INVALID, "iter must be >= 1");
+    ctx->settings = *o;
+    return LG_OK;
+}
+
+lg_status Ctx::set_lights(const lg_light* ls, int n, const float* env_rgb, int env_w, int env_h) {
+    Ctx* ctx = this;
+    if (n < 0 || n > LG_MAX_LIGHTS) return fail(LG_ERR_INVALID, "at most %d lights", LG_MAX_LIGHTS);
+    if (n > 0 && !ls) return fail(LG_ERR_INVALID, "null lights");
+    bool need_env = false;
+    for (int k = 0; k < n; ++k) {
+        if (ls[k].type < 0 || ls[k].type > 2) return fail(LG_ERR_INVALID, "bad light type");
+        if (ls[k].samples < 1) return fail(LG_ERR_INVALID, "light samples must be >= 1");
+        need_env |= ls[k].type == LG_LIGHT_ENV;
+    }
+    if (need_env && (!env_rgb || env_w < 2 || env_h < 2))
+        return fail(LG_ERR_INVALID, "environment light needs an env map of at least 2x2");
+    lights.assign(ls, ls + n);
+    env_valid = false;
+    if (env_rgb && env_w > 1 && env_h > 1) {
+        const int64_t w = env_w, h = env_h;
+        CK(env_rgb_d.reserve(sizeof(float) * w * h * 3), "env alloc");
+        CK(env_cond_func.reserve(sizeof(float) * w * h), "env alloc");
+        CK(env_cond_cdf.reserve(sizeof(float) * (w + 1) * h), "env alloc");
+        CK(env_cond_int.reserve(sizeof(float) * h), "env alloc");
+        CK(env_marg_func.reserve(sizeof(float) * h), "env alloc");
+        CK(env_marg_cdf.reserve(sizeof(float) * (h + 1)), "env alloc");
+        CK(env_marg_int.reserve(sizeof(float) * 4), "env alloc");
+        CK(cudaMemcpyAsync(env_rgb_d.p, env_rgb, sizeof(float) * w * h * 3, cudaMemcpyHostToDevice, st), "env upload");
+        CK(launch_env_cdf(env_rgb_d.as<float>(), env_w, env_h, env_cond_func.as<float>(), env_cond_cdf.as<float>(),
+                          env_cond_int.as<float>(), env_marg_func.as<float>(), env_marg_cdf.as<float>(),
+                          env_marg_int.as<float>(), st), "env cdf");
+        float mi = 0.f;
+        CK(cudaMemcpyAsync(&mi, env_marg_int.p, sizeof(float), cudaMemcpyDeviceToHost, st), "env int");
+        CK(cudaStreamSynchronize(st), "env sync");
+        env_marg_int_h = mi;
+        env_w_ = env_w;
+        env_h_ = env_h;
+        env_valid = true;
+    }
+    return LG_OK;
+}
+
+extern "C" lg_status lg_set_lights(lg_ctx* handle, const lg_light* ls, int n, const float* env_rgb,
+                                   int env_w, int env_h) {
+    Ctx* ctx = reinterpret_cast<Ctx*>(handle);
+    GUARD(ctx);
+    return ctx->set_lights(ls, n, env_rgb, env_w, env_h);
+}
+
+DevScene Ctx::scene() const {
+    DevScene sc;
+    std::memset(&sc, 0, sizeof sc);
+    sc.dens = dens.g;
+    sc.temp = temp.g;
+    sc.has_temp = temp.valid ? 1 : 0;
+    const lg_shader& s = shader;
+    DevShader& d = sc.sh;
+    d.dS = (float)s.density_scale;
+    d.dMax = (float)s.density_max;
+    d.shadowDS = (float)s.shadow_density_scale;
+    d.scatterDS = (float)s.scatter_density_scale;
+    d.scatterDMin = (float)s.scatter_density_min;
+    double a[3];
+    for (int c = 0; c < 3; ++c) {
+        a[c] = -s.extinction[c];
+        d.a[c] = (float)a[c];
+        d.albedo[c] = (float)s.albedo[c];
+        d.inv_scatter[c] = (float)(1.0 / s.scattering[c]);
+    }
+    d.emission_scale = (float)s.emission_scale;
+    d.scatter_scale = (float)s.scatter_scale;
+    d.mask_power = (float)s.scatter_density_mask_power;
+    d.tau_drop = dropout_depth(a, settings.cutoff);
+    d.ramp_n = s.ramp_n;
+    for (int k = 0; k < s.ramp_n && k < kMaxRamp; ++k) {
+        d.ramp_pos[k] = (float)s.ramp_pos[k];
+        for (int c = 0; c < 3; ++c) d.ramp_col[k][c] = (float)s.ramp_color[k][c];
+    }
+    d.ramp_in = (float)s.ramp_in;
+    d.ramp_out = (float)s.ramp_out;
+    sc.n_lights = (int)lights.size();
+    for (size_t k = 0; k < lights.size(); ++k) {
+        const lg_light& L = lights[k];
+        DevLight& o = sc.lights[k];
+        o.type = L.type;
+        o.samples = L.samples;
+        for (int c = 0; c < 3; ++c) {
+            o.I[c] = (float)(L.color[c] * (double)(float)L.intensity);
+            o.dir[c] = (float)L.dir[c];
+            o.pos[c] = (float)L.pos[c];
+        }
+        for (int e = 0; e < 9; ++e) o.rot[e] = (float)L.rot[e];
+    }
+    if (env_valid) {
+        sc.env.rgb = env_rgb_d.as<float>();
+        sc.env.cond_cdf = env_cond_cdf.as<float>();
+        sc.env.cond_func = env_cond_func.as<float>();
+        sc.env.cond_int = env_cond_int.as<float>();
+        sc.env.marg_cdf = env_marg_cdf.as<float>();
+        sc.env.marg_func = env_marg_func.as<float>();
+        sc.env.marg_int = env_marg_int_h;
+        sc.env.w = env_w_;
+        sc.env.h = env_h_;
+    }
+    sc.cutoff = (float)settings.cutoff;
+    sc.step0 = (float)settings.step[0];
+    sc.step1 = (float)settings.step[1];
+    sc.seed = settings.seed;
+    return sc;
+}
+
+// ---------------------------------------------------------------------------
+// stage 1: graphs
+// ---------------------------------------------------------------------------
+
+lg_status Ctx::load_graphs(int n_graphs, const float* points, const int64_t* offsets,
+                           const float* radius_sq, int max_connect) {
+    Ctx* ctx = this;
+    if (n_graphs < 1) return fail(LG_ERR_INVALID, "n_graphs must be >= 1");
+    if (!offsets || !radius_sq) return fail(LG_ERR_INVALID, "null offsets or radius");
+    if (max_connect < 0 || max_connect > 255) return fail(LG_ERR_INVALID, "max_connect must be in [0, 255]");
+    if (offsets[0] != 0) return fail(LG_ERR_INVALID, "offsets[0] must be 0");
+    for (int g = 0; g < n_graphs; ++g) {
+        const int64_t n = offsets[g + 1] - offsets[g];
+        if (n < 0 || n > 65535) return fail(LG_ERR_INVALID, "graph %d has %lld points (0..65535)", g, (long long)n);
+    }
+    const int64_t P = offsets[n_graphs];
+    if (P > 0 && !points) return fail(LG_ERR_INVALID, "null points");
+    h_graphs.resize(n_graphs);
+    int64_t s_off = 0, e_off = 0;
+    max_n = 0;
+    max_edges = 0;
+    for (int g = 0; g < n_graphs; ++g) {
+        GraphInfo& gi = h_graphs[g];
+        gi.pt_off = offsets[g];
+        gi.n = (int32_t)(offsets[g + 1] - offsets[g]);
+        gi.ld = round_up(std::max(gi.n, 1), 128);
+        gi.s_off = s_off;
+        s_off += (int64_t)gi.ld * gi.ld;
+        gi.max_edges = (int32_t)(((int64_t)gi.n * max_connect) / 2);
+        gi.e_off = e_off;
+        e_off += gi.max_edges;
+        gi.r2 = radius_sq[g];
+        max_n = std::max(max_n, gi.n);
+        max_edges = std::max(max_edges, gi.max_edges);
+    }
+    this->n_graphs = n_graphs;
+    n_points = P;
+    s_floats = s_off;
+    edge_slots = e_off;
+    this->max_connect = max_connect;
+    h_pts.assign(points, points + 3 * P);
+    std::vector<int32_t> pg(P);
+    for (int g = 0; g < n_graphs; ++g)
+        for (int64_t i = offsets[g]; i < offsets[g + 1]; ++i) pg[i] = g;
+    CK(d_pts.reserve(sizeof(float) * 3 * std::max<int64_t>(P, 1)), "points alloc");
+    CK(d_graphs.reserve(sizeof(GraphInfo) * n_graphs), "graphs alloc");
+    CK(d_pt_graph.reserve(sizeof(int32_t) * std::max<int64_t>(P, 1)), "point graph alloc");
+    CK(d_cand.reserve(sizeof(uint16_t) * kCandCap * std::max<int64_t>(P, 1)), "candidate alloc");
+    CK(d_cand_cnt.reserve(sizeof(int32_t) * std::max<int64_t>(P, 1)), "candidate count alloc");
+    CK(d_edges.reserve(sizeof(int2) * std::max<int64_t>(e_off, 1)), "edge alloc");
+    CK(d_edge_cnt.reserve(sizeof(int32_t) * n_graphs), "edge count alloc");
+    if (P > 0) {
+        CK(cudaMemcpyAsync(d_pts.p, points, sizeof(float) * 3 * P, cudaMemcpyHostToDevice, st), "points upload");
+        CK(cudaMemcpyAsync(d_pt_graph.p, pg.data(), sizeof(int32_t) * P, cudaMemcpyHostToDevice, st), "graph ids upload");
+    }
+    CK(cudaMemcpyAsync(d_graphs.p, h_graphs.data(), sizeof(GraphInfo) * n_graphs, cudaMemcpyHostToDevice, st),
+       "graph info upload");
+    // the host copies above read pageable memory; finish them before the
+    // caller's buffers can change
+    CK(cudaStreamSynchronize(st), "graph upload sync");
+    point_voxel_size_cache = -1.0;
+    graphs_built = false;
+    return LG_OK;
+}
+
+lg_status Ctx::build_edges() {
+    Ctx* ctx = this;
+    CK(launch_candidates(d_pts.as<float>(), d_graphs.as<GraphInfo>(), d_pt_graph.as<int32_t>(), n_points,
+                         d_cand.as<uint16_t>(), d_cand_cnt.as<int32_t>(), st), "edge candidates");
+    CK(launch_greedy(d_pts.as<float>(), d_graphs.as<GraphInfo>(), n_graphs, max_n, d_cand.as<uint16_t>(),
+                     d_cand_cnt.as<int32_t>(), max_connect, d_edges.as<int2>(), d_edge_cnt.as<int32_t>(), st),
+       "greedy connect");
+    graphs_built = true;
+    return LG_OK;
+}
+
+extern "C" lg_status lg_build_graphs(lg_ctx* handle, int n_graphs, const float* points,
+                                     const int64_t* offsets, const float* radius_sq, int max_connect,
+                                     uint8_t* adj_out, int64_t* n_edges_out) {
+    Ctx* ctx = reinterpret_cast<Ctx*>(handle);
+    GUARD(ctx);
+    lg_status s = ctx->load_graphs(n_graphs, points, offsets, radius_sq, max_connect);
+    if (s != LG_OK) return s;
+    s = ctx->build_edges();
+    if (s != LG_OK) return s;
+    if (adj_out) {
+        int64_t total = 0;
+        std::vector<int64_t> aoff(n_graphs);
+        for (int g = 0; g < n_graphs; ++g) {
+            aoff[g] = total;
+            total += (int64_t)ctx->h_graphs[g].n * ctx->h_graphs[g].n;
+        }
+        CK(ctx->d_adj.reserve(std::max<int64_t>(total, 1)), "adjacency alloc");
+        CK(ctx->d_adj_off.reserve(sizeof(int64_t) * n_graphs), "adjacency offsets alloc");
+        CK(cudaMemcpyAsync(ctx->d_adj_off.p, aoff.data(), sizeof(int64_t) * n_graphs, cudaMemcpyHostToDevice,
+                           ctx->st), "adjacency offsets upload");
+        CK(cudaMemsetAsync(ctx->d_adj.p, 0, std::max<int64_t>(total, 1), ctx->st), "adjacency clear");
+        CK(launch_adjacency(ctx->d_graphs.as<GraphInfo>(), n_graphs, ctx->max_edges, ctx->d_edges.as<int2>(),
+                            ctx->d_edge_cnt.as<int32_t>(), ctx->d_adj.as<uint8_t>(), ctx->d_adj_off.as<int64_t>(),
+                            ctx->st), "adjacency");
+        if (total > 0)
+            CK(cudaMemcpyAsync(adj_out, ctx->d_adj.p, total, cudaMemcpyDeviceToHost, ctx->st), "adjacency download");
+    }
+    if (n_edges_out) {
+        std::vector<int32_t> ec(n_graphs);
+        CK(cudaMemcpyAsync(ec.data(), ctx->d_edge_cnt.p, sizeof(int32_t) * n_graphs, cudaMemcpyDeviceToHost,
+                           ctx->st), "edge count download");
+        CK(cudaStreamSynchronize(ctx->st), "sync");
+        for (int g = 0; g < n_graphs; ++g) n_edges_out[g] = ec[g];
+    }
+    CK(cudaStreamSynchronize(ctx->st), "sync");
+    return LG_OK;
+}
+
+lg_status Ctx::copy_matrix_out(float* out) {
+    Ctx* ctx = this;
+    int64_t o = 0;
+    for (const GraphInfo& g : h_graphs) {
+        if (g.n > 0)
+            CK(cudaMemcpy2DAsync(out + o, sizeof(float) * g.n, d_S.as<float>() + g.s_off, sizeof(float) * g.ld,
+                                 sizeof(float) * g.n, g.n, cudaMemcpyDeviceToHost, st), "matrix download");
+        o += (int64_t)g.n * g.n;
+    }
+    CK(cudaStreamSynchronize(st), "sync");
+    return LG_OK;
+}
+
+lg_status Ctx::march_edges() {
+    Ctx* ctx = this;
+    if (!dens.valid) return fail(LG_ERR_STATE, "no density grid uploaded");
+    if (!graphs_built) return fail(LG_ERR_STATE, "no graphs built");
+    CK(d_S.reserve(sizeof(float) * std::max<int64_t>(s_floats, 1)), "S alloc");
+    CK(launch_fill(d_S.as<float>(), s_floats, INFINITY, st), "S fill");
+    CK(launch_edge_march(scene(), d_pts.as<float>(), d_graphs.as<GraphInfo>(), n_graphs, max_edges,
+                         d_edges.as<int2>(), d_edge_cnt.as<int32_t>(), d_S.as<float>(), st), "edge march");
+    return LG_OK;
+}
+
+lg_status Ctx::solve_paths() {
+    Ctx* ctx = this;
+    for (const GraphInfo& g : h_graphs) {
+        if (g.n == 0) continue;
+        CK(fw_solve(d_S.as<float>() + g.s_off, g.ld, g.ld, st), "floyd-warshall");
+    }
+    CK(launch_set_diag(d_S.as<float>(), d_graphs.as<GraphInfo>(), n_graphs, max_n, st), "diagonal");
+    return LG_OK;
+}
+
+lg_status Ctx::vertex_light() {
+    Ctx* ctx = this;
+    if (!dens.valid) return fail(LG_ERR_STATE, "no density grid uploaded");
+    CK(d_L.reserve(sizeof(float) * 3 * std::max<int64_t>(n_points, 1)), "L alloc");
+    CK(launch_vertex_light(scene(), d_pts.as<float>(), d_graphs.as<GraphInfo>(), n_graphs, max_n, d_L.as<float>(),
+                           st), "vertex light");
+    return LG_OK;
+}
+
+lg_status Ctx::diffuse() {
+    Ctx* ctx = this;
+    const int64_t P = std::max<int64_t>(n_points, 1);
+    CK(d_D.reserve(sizeof(float) * 3 * P), "D alloc");
+    CK(d_part.reserve(sizeof(float) * 3 * kRowChunks * P), "diffuse scratch alloc");
+    CK(d_colw.reserve(sizeof(float) * 3 * P), "diffuse scratch alloc");
+    CK(launch_diffuse(scene().sh, d_S.as<float>(), d_graphs.as<GraphInfo>(), n_graphs, max_n, d_L.as<float>(),
+                      d_part.as<float>(), d_colw.as<float>(), d_D.as<float>(), st), "diffuse");
+    return LG_OK;
+}
+
+extern "C" lg_status lg_march_edges(lg_ctx* handle, float* S_out) {
+    Ctx* ctx = reinterpret_cast<Ctx*>(handle);
+    GUARD(ctx);
+    lg_status s = ctx->march_edges();
+    if (s != LG_OK) return s;
+    ctx->paths_solved = false;
+    if (S_out) return ctx->copy_matrix_out(S_out);
+    return LG_OK;
+}
+
+extern "C" lg_status lg_solve_paths(lg_ctx* handle, float* dist_out) {
+    Ctx* ctx = reinterpret_cast<Ctx*>(handle);
+    GUARD(ctx);
+    if (!ctx->graphs_built || ctx->d_S.bytes == 0) return ctx->fail(LG_ERR_STATE, "edges not marched");
+    lg_status s = ctx->solve_paths();
+    if (s != LG_OK) return s;
+    ctx->paths_solved = true;
+    if (dist_out) return ctx->copy_matrix_out(dist_out);
+    return LG_OK;
+}
+
+extern "C" lg_status lg_vertex_light(lg_ctx* handle, float* light_out) {
+    Ctx* ctx = reinterpret_cast<Ctx*>(handle);
+    GUARD(ctx);
+    if (!ctx->graphs_built) return ctx->fail(LG_ERR_STATE, "no graphs loaded");
+    lg_status s = ctx->vertex_light();
+    if (s != LG_OK) return s;
+    ctx->light_done = true;
+    if (light_out && ctx->n_points > 0) {
+        CK(cudaMemcpyAsync(light_out, ctx->d_L.p, sizeof(float) * 3 * ctx->n_points, cudaMemcpyDeviceToHost,
+                           ctx->st), "L download");
+        CK(cudaStreamSynchronize(ctx->st), "sync");
+    }
+    return LG_OK;
+}
+
+extern "C" lg_status lg_diffuse(lg_ctx* handle, float* diffuse_out) {
+    Ctx* ctx = reinterpret_cast<Ctx*>(handle);
+    GUARD(ctx);
+    if (!ctx->paths_solved || !ctx->light_done)
+        return ctx->fail(LG_ERR_STATE, "diffuse needs solved paths and vertex light");
+    lg_status s = ctx->diffuse();
+    if (s != LG_OK) return s;
+    ctx->diffuse_done = true;
+    if (diffuse_out && ctx->n_points > 0) {
+        CK(cudaMemcpyAsync(diffuse_out, ctx->d_D.p, sizeof(float) * 3 * ctx->n_points, cudaMemcpyDeviceToHost,
+                           ctx->st), "D download");
+        CK(cudaStreamSynchronize(ctx->st), "sync");
+    }
+    return LG_OK;
+}
+
+lg_status Ctx::solve_all() {
+    lg_status s = march_edges();
+    if (s != LG_OK) return s;
+    s = solve_paths();
+    if (s != LG_OK) return s;
+    paths_solved = true;
+    s = vertex_light();
+    if (s != LG_OK) return s;
+    light_done = true;
+    s = diffuse();
+    if (s != LG_OK) return s;
+    diffuse_done = true;
+    return LG_OK;
+}
+
+extern "C" lg_status lg_solve_graphs(lg_ctx* handle, float* diffuse_out) {
+    Ctx* ctx = reinterpret_cast<Ctx*>(handle);
+    GUARD(ctx);
+    if (!ctx->graphs_built) return ctx->fail(LG_ERR_STATE, "no graphs built");
+    lg_status s = ctx->solve_all();
+    if (s != LG_OK) return s;
+    if (diffuse_out && ctx->n_points > 0) {
+        CK(cudaMemcpyAsync(diffuse_out, ctx->d_D.p, sizeof(float) * 3 * ctx->n_points, cudaMemcpyDeviceToHost,
+                           ctx->st), "D download");
+    }
+    CK(cudaStreamSynchronize(ctx->st), "sync");
+    return LG_OK;
+}
+
+extern "C" lg_status lg_get_vertex_data(lg_ctx* handle, float* light_out, float* diffuse_out) {
+    Ctx* ctx = reinterpret_cast<Ctx*>(handle);
+    GUARD(ctx);
+    if (light_out) {
+        if (!ctx->light_done) return ctx->fail(LG_ERR_STATE, "vertex light not computed");
+        CK(cudaMemcpyAsync(light_out, ctx->d_L.p, sizeof(float) * 3 * ctx->n_points, cudaMemcpyDeviceToHost,
+                           ctx->st), "L download");
+    }
+    if (diffuse_out) {
+        if (!ctx->diffuse_done) return ctx->fail(LG_ERR_STATE, "diffusion not computed");
+        CK(cudaMemcpyAsync(diffuse_out, ctx->d_D.p, sizeof(float) * 3 * ctx->n_points, cudaMemcpyDeviceToHost,
+                           ctx->st), "D download");
+    }
+    CK(cudaStreamSynchronize(ctx->st), "sync");
+    return LG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// stage 2: scatter grid
+// ---------------------------------------------------------------------------
+
+extern "C" double lg_point_voxel_size(int64_t n, const float* pts, int points_per_voxel) {
+    // computeVoxelSize's starting estimate (src/LightGraph.h:713-714): the
+    // edge of a cube holding points_per_voxel points on average over the
+    // points' bounding box. 0.1 (OpenVDB's default) for fewer than 2 points.
+    if (n <= 1 || !pts || points_per_voxel <= 0) return 0.1;
+    double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+    for (int64_t i = 0; i < n; ++i)
+        for (int a = 0; a < 3; ++a) {
+            lo[a] = std::min(lo[a], (double)pts[3 * i + a]);
+            hi[a] = std::max(hi[a], (double)pts[3 * i + a]);
+        }
+    double ext[3];
+    double maxe = 0;
+    for (int a = 0; a < 3; ++a) {
+        ext[a] = hi[a] - lo[a];
+        maxe = std::max(maxe, ext[a]);
+    }
+    if (maxe <= 0) return 0.1;
+    // flat point sets: a degenerate axis gets the extent of the largest one
+    for (int a = 0; a < 3; ++a)
+        if (ext[a] <= 0) ext[a] = maxe;
+    const double target = std::max<double>(1.0, (double)(n / points_per_voxel));
+    const double vol = ext[0] * ext[1] * ext[2];
+    return std::cbrt(vol / target);
+}
+
+lg_status Ctx::splat(double point_voxel_size) {
+    Ctx* ctx = this;
+    if (!dens.valid) return fail(LG_ERR_STATE, "no density grid uploaded");
+    if (!diffuse_done) return fail(LG_ERR_STATE, "graphs not solved");
+    const int f = settings.scatter_grid_res_factor;
+    const lg_grid_desc& dd = dens.desc;
+    CoarseGrid cg;
+    for (int a = 0; a < 3; ++a) {
+        const int lo = floor_div(dd.origin[a], f) - 1;
+        const int hi = floor_div(dd.origin[a] + dd.dims[a] - 1, f) + 1;
+        cg.lo[a] = lo;
+        cg.dims[a] = hi - lo + 1;
+    }
+    cg.H = (float)(dd.voxel_size * f);
+    const int64_t ncoarse = (int64_t)cg.dims[0] * cg.dims[1] * cg.dims[2];
+    if (topo_version != dens.version || topo_factor != f) {
+        CK(d_act0.reserve(ncoarse), "coarse mask alloc");
+        CK(d_act.reserve(ncoarse), "coarse mask alloc");
+        CK(launch_coarse_topology(dens.g, f, cg, d_act0.as<uint8_t>(), d_act.as<uint8_t>(), st), "coarse topology");
+        topo_version = dens.version;
+        topo_factor = f;
+    }
+    double hp = point_voxel_size;
+    if (!(hp > 0)) {
+        if (point_voxel_size_cache < 0) point_voxel_size_cache = lg_point_voxel_size(n_points, h_pts.data(), 8);
+        hp = point_voxel_size_cache;
+    }
+    // ScatterGrid::operator() kernel size (src/ScatterGrid.h:69-75), with
+    // K = ptsPerKernel * iter (src/main.cc:586)
+    const double K = (double)settings.pts_per_kernel * (double)settings.iter;
+    const double radius = std::cbrt((3.0 * K * hp * hp * hp) / (32.0 * 3.14159265358979323846));
+    const double sigma2 = -(radius * radius) / (2.0 * std::log(0.1));
+    const float inv2s2 = (float)(1.0 / (2.0 * sigma2));
+    // point bins
+    PointBins pb{};
+    double lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+    if (n_points > 0) {
+        for (int a = 0; a < 3; ++a) { lo[a] = 1e300; hi[a] = -1e300; }
+        for (int64_t i = 0; i < n_points; ++i)
+            for (int a = 0; a < 3; ++a) {
+                lo[a] = std::min(lo[a], (double)h_pts[3 * i + a]);
+                hi[a] = std::max(hi[a], (double)h_pts[3 * i + a]);
+            }
+    }
+    double cell = std::max(radius, 1e-12);
+    double ext = 0;
+    for (int a = 0; a < 3; ++a) ext = std::max(ext, hi[a] - lo[a]);
+    if (ext / cell > 255.0) cell = ext / 255.0;  // at most 256^3 cells
+    pb.cell = (float)cell;
+    pb.n_cells = 1;
+    for (int a = 0; a < 3; ++a) {
+        pb.lo[a] = (float)lo[a];
+        pb.dims[a] = (int)std::floor((hi[a] - lo[a]) / cell) + 1;
+        pb.n_cells *= pb.dims[a];
+    }
+    const int64_t P = std::max<int64_t>(n_points, 1);
+    CK(d_cell_count.reserve(sizeof(int32_t) * pb.n_cells), "bins alloc");
+    CK(d_cell_start.reserve(sizeof(int32_t) * pb.n_cells), "bins alloc");
+    CK(d_cursor.reserve(sizeof(int32_t) * pb.n_cells), "bins alloc");
+    CK(d_scan_tmp.reserve(sizeof(int32_t) * ((pb.n_cells + 1023) / 1024 + 1)), "bins alloc");
+    CK(d_sorted.reserve(sizeof(int32_t) * P), "bins alloc");
+    CK(launch_bin_points(d_pts.as<float>(), n_points, pb, d_cell_count.as<int32_t>(), d_cell_start.as<int32_t>(),
+                         d_cursor.as<int32_t>(), d_sorted.as<int32_t>(), d_scan_tmp.as<int32_t>(), st), "bin points");
+    CK(d_sg.reserve(sizeof(float4) * ncoarse), "scatter grid alloc");
+    CK(launch_splat(cg, d_act.as<uint8_t>(), d_pts.as<float>(), d_D.as<float>(), pb, d_cell_start.as<int32_t>(),
+                    d_cell_count.as<int32_t>(), d_sorted.as<int32_t>(), (float)radius, inv2s2, d_sg.as<float4>(), st),
+       "splat");
+    coarse = cg;
+    splat_done = true;
+    splat_radius = radius;
+    return LG_OK;
+}
+
+extern "C" lg_status lg_splat(lg_ctx* handle, double point_voxel_size) {
+    Ctx* ctx = reinterpret_cast<Ctx*>(handle);
+    GUARD(ctx);
+    lg_status s = ctx->splat(point_voxel_size);
+    if (s != LG_OK) return s;
+    CK(cudaStreamSynchronize(ctx->st), "sync");
+    return LG_OK;
+}
+
+extern "C" lg_status lg_get_scatter_grid(lg_ctx* handle, int32_t dims[3], int32_t origin[3], float* values) {
+    Ctx* ctx = reinterpret_cast<Ctx*>(handle);
+    GUARD(ctx);
+    if (!ctx->splat_done) return ctx->fail(LG_ERR_STATE, "no scatter grid");
+    for (int a = 0; a < 3; ++a) {
+        if (dims) dims[a] = ctx->coarse.dims[a];
+        if (origin) origin[a] = ctx->coarse.lo[a];
+    }
+    if (values) {
+        const int64_t n = (int64_t)ctx->coarse.dims[0] * ctx->coarse.dims[1] * ctx->coarse.dims[2];
+        std::vector<float4> tmp(n);
+        CK(cudaMemcpyAsync(tmp.data(), ctx->d_sg.p, sizeof(float4) * n, cudaMemcpyDeviceToHost, ctx->st),
+           "scatter grid download");
+        CK(cudaStreamSynchronize(ctx->st), "sync");
+        for (int64_t i = 0; i < n; ++i) {
+            values[3 * i] = tmp[i].x;
+            values[3 * i + 1] = tmp[i].y;
+            values[3 * i + 2] = tmp[i].z;
+        }
+    }
+    return LG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// stage 3: render
+// ---------------------------------------------------------------------------
+
+lg_status Ctx::render(const lg_camera* c) {
+    Ctx* ctx = this;
+    if (!c) return fail(LG_ERR_INVALID, "null camera");
+    if (c->width <= 0 || c->height <= 0 || c->samples < 0) return fail(LG_ERR_INVALID, "bad image size or samples");
+    if (!(c->focal > 0) || !(c->aperture > 0)) return fail(LG_ERR_INVALID, "bad focal length or aperture");
+    if (!(c->znear > 0) || !(c->zfar > c->znear)) return fail(LG_ERR_INVALID, "need 0 < znear < zfar");
+    if (!dens.valid) return fail(LG_ERR_STATE, "no density grid uploaded");
+    const int64_t np = (int64_t)c->width * c->height;
+    for (DevBuf* b : {&d_rgba, &d_direct, &d_scatter, &d_emission}) CK(b->reserve(sizeof(float4) * np), "film alloc");
+    CK(d_counters.reserve(2 * sizeof(unsigned long long)), "counter alloc");
+    CK(cudaMemsetAsync(d_counters.p, 0, 2 * sizeof(unsigned long long), st), "counter clear");
+    DevScatterGrid sg{};
+    if (splat_done) {
+        sg.v = d_sg.as<float4>();
+        for (int a = 0; a < 3; ++a) {
+            sg.lo[a] = coarse.lo[a];
+            sg.dims[a] = coarse.dims[a];
+        }
+        sg.inv_H = 1.f / coarse.H;
+    } else {
+        // no multiple scattering estimate yet: an empty grid reads 0
+        sg.v = nullptr;
+        sg.inv_H = 1.f;
+    }
+    film_w = c->width;
+    film_h = c->height;
+    CK(launch_render(scene(), make_camera(*c), sg, d_rgba.as<float4>(), d_direct.as<float4>(),
+                     d_scatter.as<float4>(), d_emission.as<float4>(), d_counters.as<unsigned long long>(), st),
+       "render");
+    return LG_OK;
+}
+
+lg_status Ctx::download_films(float* rgba, float* direct, float* scatter, float* emission) {
+    Ctx* ctx = this;
+    const int64_t np = (int64_t)film_w * film_h;
+    const void* src[4] = {d_rgba.p, d_direct.p, d_scatter.p, d_emission.p};
+    float* dst[4] = {rgba, direct, scatter, emission};
+    for (int k = 0; k < 4; ++k)
+        if (dst[k]) CK(cudaMemcpyAsync(dst[k], src[k], sizeof(float4) * np, cudaMemcpyDeviceToHost, st), "film download");
+    CK(cudaStreamSynchronize(st), "sync");
+    return LG_OK;
+}
+
+extern "C" lg_status lg_render(lg_ctx* handle, const lg_camera* camera, float* rgba, float* direct,
+                               float* scatter, float* emission) {
+    Ctx* ctx = reinterpret_cast<Ctx*>(handle);
+    GUARD(ctx);
+    lg_status s = ctx->render(camera);
+    if (s != LG_OK) return s;
+    return ctx->download_films(rgba, direct, scatter, emission);
+}
+
+extern "C" lg_status lg_render_stats(lg_ctx* handle, uint64_t* primary, uint64_t* shadow) {
+    Ctx* ctx = reinterpret_cast<Ctx*>(handle);
+    GUARD(ctx);
+    unsigned long long c[2] = {0, 0};
+    if (ctx->d_counters.bytes >= sizeof c) {
+        CK(cudaMemcpyAsync(c, ctx->d_counters.p, sizeof c, cudaMemcpyDeviceToHost, ctx->st), "counter download");
+        CK(cudaStreamSynchronize(ctx->st), "sync");
+    }
+    if (primary) *primary = c[0];
+    if (shadow) *shadow = c[1];
+    return LG_OK;
+}
+
+extern "C" lg_status lg_render_frame(lg_ctx* handle, int n_graphs, const float* points,
+                                     const int64_t* offsets, const float* radius_sq, int max_connect,
+                                     double point_voxel_size, const lg_camera* camera, float* rgba,
+                                     float* direct, float* scatter, float* emission) {
+    Ctx* ctx = reinterpret_cast<Ctx*>(handle);
+    GUARD(ctx);
+    lg_status s = ctx->load_graphs(n_graphs, points, offsets, radius_sq, max_connect);
+    if (s == LG_OK) s = ctx->build_edges();
+    if (s == LG_OK) s = ctx->solve_all();
+    if (s == LG_OK) s = ctx->splat(point_voxel_size);
+    if (s == LG_OK) s = ctx->render(camera);
+    if (s == LG_OK) s = ctx->download_films(rgba, direct, scatter, emission);
+    return s;
+}
+
+extern "C" lg_status lg_frame_device(lg_ctx* handle, int max_connect, double point_voxel_size,
+                                     const lg_camera* camera) {
+    Ctx* ctx = reinterpret_cast<Ctx*>(handle);
+    GUARD(ctx);
+    if (ctx->n_graphs == 0) return ctx->fail(LG_ERR_STATE, "no graphs loaded");
+    if (max_connect < 0 || max_connect > 255) return ctx->fail(LG_ERR_INVALID, "bad max_connect");
+    if (max_connect != ctx->max_connect) return ctx->fail(LG_ERR_INVALID, "max_connect differs from the loaded graphs");
+    ctx->mark(0);
+    lg_status s = ctx->build_edges();
+    ctx->mark(1);
+    if (s == LG_OK) s = ctx->march_edges();
+    ctx->mark(2);
+    if (s == LG_OK) { s = ctx->solve_paths(); ctx->paths_solved = s == LG_OK; }
+    ctx->mark(3);
+    if (s == LG_OK) { s = ctx->vertex_light(); ctx->light_done = s == LG_OK; }
+    ctx->mark(4);
+    if (s == LG_OK) { s = ctx->diffuse(); ctx->diffuse_done = s == LG_OK; }
+    ctx->mark(5);
+    if (s == LG_OK) s = ctx->splat(point_voxel_size);
+    ctx->mark(6);
+    if (s == LG_OK) s = ctx->render(camera);
+    ctx->mark(7);
+    ctx->ev_recorded = ctx->profiling && s == LG_OK;
+    return s;
+}
+
+extern "C" lg_status lg_set_profiling(lg_ctx* handle, int on) {
+    Ctx* ctx = reinterpret_cast<Ctx*>(handle);
+    GUARD(ctx);
+    if (on && !ctx->ev[0]) {
+        for (int k = 0; k <= Ctx::kStages; ++k) CK(cudaEventCreate(&ctx->ev[k]), "event create");
+    }
+    ctx->profiling = on != 0;
+    ctx->ev_recorded = false;
+    return LG_OK;
+}
+
+extern "C" lg_status lg_stage_times(lg_ctx* handle, double* ms, int n) {
+    Ctx* ctx = reinterpret_cast<Ctx*>(handle);
+    GUARD(ctx);
+    if (!ctx->ev_recorded) return ctx->fail(LG_ERR_STATE, "no profiled frame");
+    if (!ms || n < 1) return ctx->fail(LG_ERR_INVALID, "bad output");
+    CK(cudaEventSynchronize(ctx->ev[Ctx::kStages]), "event sync");
+    for (int k = 0; k < n && k < Ctx::kStages; ++k) {
+        float t = 0.f;
+        CK(cudaEventElapsedTime(&t, ctx->ev[k], ctx->ev[k + 1]), "event time");
+        ms[k] = t;
+    }
+    return LG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// kernel-level entry points
+// ---------------------------------------------------------------------------
+
+extern "C" lg_status lg_fw_device(float* dist, int n, int ld, void* stream) {
+    if (n < 0 || ld < n || (n > 0 && !dist)) return LG_ERR_INVALID;
+    if (ld % 4 != 0 || (reinterpret_cast<uintptr_t>(dist) & 15) != 0) return LG_ERR_INVALID;
+    const cudaError_t e = fw_solve(dist, n, ld, (cudaStream_t)stream);
+    return e == cudaSuccess ? LG_OK : LG_ERR_CUDA;
+}
+
+extern "C" lg_status lg_fw_host(lg_ctx* handle, float* dist, int n) {
+    Ctx* ctx = reinterpret_cast<Ctx*>(handle);
+    GUARD(ctx);
+    if (n < 0 || (n > 0 && !dist)) return ctx->fail(LG_ERR_INVALID, "bad matrix");
+    if (n == 0) return LG_OK;
+    const int ld = round_up(n, 4);
+    CK(ctx->d_fw.reserve(sizeof(float) * (size_t)n * ld), "fw alloc");
+    CK(cudaMemcpy2DAsync(ctx->d_fw.p, sizeof(float) * ld, dist, sizeof(float) * n, sizeof(float) * n, n,
+                         cudaMemcpyHostToDevice, ctx->st), "fw upload");
+    CK(fw_solve(ctx->d_fw.as<float>(), n, ld, ctx->st), "floyd-warshall");
+    CK(cudaMemcpy2DAsync(dist, sizeof(float) * n, ctx->d_fw.p, sizeof(float) * ld, sizeof(float) * n, n,
+                         cudaMemcpyDeviceToHost, ctx->st), "fw download");
+    CK(cudaStreamSynchronize(ctx->st), "sync");
+    return LG_OK;
+}
+

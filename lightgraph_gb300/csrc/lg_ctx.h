@@ -1,0 +1,125 @@
+// Context object behind the opaque lg_ctx handle: one device, one stream,
+// the resident grids and the device buffers of each stage (grow-only).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "lg_kernels.h"
+#include "lightgraph_c.h"
+
+namespace lg {
+
+// Grow-only device allocation.
+struct DevBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    DevBuf() = default;
+    DevBuf(const DevBuf&) = delete;
+    DevBuf& operator=(const DevBuf&) = delete;
+    ~DevBuf() { release(); }
+    cudaError_t reserve(size_t b) {
+        if (b <= bytes) return cudaSuccess;
+        release();
+        const cudaError_t e = cudaMalloc(&p, b);
+        if (e != cudaSuccess) {
+            p = nullptr;
+            return e;
+        }
+        bytes = b;
+        return cudaSuccess;
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+    }
+    template <class T>
+    T* as() const {
+        return reinterpret_cast<T*>(p);
+    }
+};
+
+struct GridStore {
+    DevBuf bricks, bits;
+    DevGrid g;
+    lg_grid_desc desc{};
+    bool valid = false;
+    int version = 0;
+};
+
+struct Ctx {
+    int device = 0;
+    cudaStream_t st = nullptr;
+    std::mutex mu;
+    std::string err;
+    cudaGraphExec_t graph_exec = nullptr;
+
+    // grids
+    GridStore dens, temp;
+    DevBuf staging, mask_staging, small;
+
+    // scene
+    lg_shader shader{};
+    lg_settings settings{};
+    std::vector<lg_light> lights;
+    DevBuf env_rgb_d, env_cond_func, env_cond_cdf, env_cond_int, env_marg_func, env_marg_cdf, env_marg_int;
+    float env_marg_int_h = 0.f;
+    int env_w_ = 0, env_h_ = 0;
+    bool env_valid = false;
+
+    // graphs
+    int n_graphs = 0;
+    int64_t n_points = 0;
+    int max_n = 0, max_edges = 0, max_connect = 12;
+    int64_t s_floats = 0, edge_slots = 0;
+    std::vector<GraphInfo> h_graphs;
+    std::vector<float> h_pts;
+    double point_voxel_size_cache = -1.0;
+    bool graphs_built = false, paths_solved = false, light_done = false, diffuse_done = false;
+    DevBuf d_pts, d_graphs, d_pt_graph, d_cand, d_cand_cnt, d_edges, d_edge_cnt, d_adj, d_adj_off;
+    DevBuf d_S, d_L, d_D, d_part, d_colw, d_fw;
+
+    // scatter grid
+    CoarseGrid coarse{};
+    int topo_version = -1, topo_factor = -1;
+    bool splat_done = false;
+    double splat_radius = 0.0;
+    DevBuf d_act0, d_act, d_sg, d_cell_count, d_cell_start, d_cursor, d_sorted, d_scan_tmp;
+
+    // films
+    int film_w = 0, film_h = 0;
+    DevBuf d_rgba, d_direct, d_scatter, d_emission, d_counters;
+
+    // stage timing: events recorded on the stream around each stage of a frame
+    static constexpr int kStages = 7;  // build, march, fw, light, diffuse, splat, render
+    bool profiling = false;
+    cudaEvent_t ev[kStages + 1] = {};
+    bool ev_recorded = false;
+    void mark(int k) {
+        if (profiling && ev[k]) cudaEventRecord(ev[k], st);
+    }
+
+    lg_status fail(lg_status s, const char* fmt, ...);
+    lg_status cuda(cudaError_t e, const char* what);
+
+    lg_status upload_grid(int which, const lg_grid_desc* desc, const float* values, int dtype);
+    lg_status set_lights(const lg_light* ls, int n, const float* env_rgb, int env_w, int env_h);
+    DevScene scene() const;
+    lg_status load_graphs(int n_graphs, const float* points, const int64_t* offsets, const float* radius_sq,
+                          int max_connect);
+    lg_status build_edges();
+    lg_status march_edges();
+    lg_status solve_paths();
+    lg_status vertex_light();
+    lg_status diffuse();
+    lg_status solve_all();
+    lg_status splat(double point_voxel_size);
+    lg_status render(const lg_camera* c);
+    lg_status download_films(float* rgba, float* direct, float* scatter, float* emission);
+    lg_status copy_matrix_out(float* out);
+};
+
+}  // namespace lg

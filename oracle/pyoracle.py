@@ -1,0 +1,206 @@
+"""ctypes binding of the CPU oracle (oracle/lg_oracle.h).
+
+TEST INFRASTRUCTURE: imported only by tests/, __graft_entry__.smoke() and the
+CPU-baseline leg of bench.py, as the checker / the timed CPU baseline. The
+product package (lightgraph_gb300) never imports it.
+
+PARITY UNPINNED: the reference has no tests or fixtures and cannot be built
+here; see lg_oracle.h.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import sys
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_ROOT = os.path.dirname(_HERE)
+if _ROOT not in sys.path:
+    sys.path.insert(0, _ROOT)
+
+from lightgraph_gb300 import build as _build  # noqa: E402  (build recipe only)
+from lightgraph_gb300._capi import CameraC, GridDesc, LightC, SettingsC, ShaderC  # noqa: E402  (struct layouts)
+
+
+class OGrid(C.Structure):
+    _fields_ = [("desc", GridDesc), ("values", C.c_void_p)]
+
+
+class OEnv(C.Structure):
+    _fields_ = [("rgb", C.c_void_p), ("w", C.c_int32), ("h", C.c_int32)]
+
+
+P = C.c_void_p
+_lib = None
+
+
+def load() -> C.CDLL:
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = _build.oracle_path()
+    if not os.path.exists(path):
+        _build.build_oracle()
+    lib = C.CDLL(path)
+    lib.lgo_build_graph.restype = C.c_int64
+    lib.lgo_build_graph.argtypes = [C.c_int, P, C.c_float, C.c_int, P]
+    lib.lgo_march_edges.restype = None
+    lib.lgo_march_edges.argtypes = [C.POINTER(OGrid), C.POINTER(ShaderC), C.POINTER(SettingsC), C.c_int, P, P, P, P]
+    lib.lgo_fw_maxtimes.argtypes = [C.c_int, P]
+    lib.lgo_fw_minplus_f32.argtypes = [C.c_int, P]
+    lib.lgo_fw_minplus_f64.argtypes = [C.c_int, P]
+    lib.lgo_vertex_light.argtypes = [C.POINTER(OGrid), C.POINTER(OGrid), C.POINTER(ShaderC), C.POINTER(SettingsC),
+                                     C.POINTER(LightC), C.c_int, C.POINTER(OEnv), C.c_int, P, C.c_int, P]
+    lib.lgo_diffuse.argtypes = [C.c_int, P, P, P]
+    lib.lgo_splat.restype = C.c_double
+    lib.lgo_splat.argtypes = [C.POINTER(OGrid), C.c_int, C.c_int64, P, P, C.c_double, C.c_double, P, P, P]
+    lib.lgo_render.argtypes = [C.POINTER(OGrid), C.POINTER(OGrid), C.POINTER(ShaderC), C.POINTER(SettingsC),
+                               C.POINTER(LightC), C.c_int, C.POINTER(OEnv), C.POINTER(CameraC), P, P, C.c_double, P,
+                               C.c_int, C.c_int, P, P, P, P, P]
+    lib.lgo_env_cdf.argtypes = [C.POINTER(OEnv), P, P, P, P, P, P]
+    lib.lgo_threads.restype = C.c_int
+    _lib = lib
+    return lib
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data
+
+
+class Oracle:
+    """Holds one scene (grids, shader, settings, lights) and runs the
+    reference's stages on the CPU in FP64."""
+
+    def __init__(self, density, shader, opts, lights=(), temperature=None, env_map=None):
+        self.lib = load()
+        self._keep = []
+        self.dens = self._grid(density)
+        self.temp = self._grid(temperature) if temperature is not None else None
+        self.shader = shader.to_c()
+        self.settings = opts.to_c()
+        self.opts = opts
+        self.lights = (LightC * max(1, len(lights)))(*[l.c for l in lights])
+        self.n_lights = len(lights)
+        if env_map is not None:
+            env = np.ascontiguousarray(env_map, np.float32)
+            self._keep.append(env)
+            self.env = OEnv(env.ctypes.data, env.shape[1], env.shape[0])
+        else:
+            self.env = None
+
+    def _grid(self, g):
+        vals = np.ascontiguousarray(g.values, np.float32)
+        self._keep.append(vals)
+        if g.leaf_mask is not None:
+            self._keep.append(g.leaf_mask)
+        return OGrid(g.desc(), vals.ctypes.data)
+
+    def threads(self) -> int:
+        return self.lib.lgo_threads()
+
+    def build_graph(self, pts, radius_sq, max_connect=12):
+        pts = np.ascontiguousarray(pts, np.float32)
+        n = len(pts)
+        adj = np.zeros((n, n), np.uint8)
+        ne = self.lib.lgo_build_graph(n, _p(pts), C.c_float(radius_sq), max_connect, _p(adj))
+        return adj, ne
+
+    def march_edges(self, pts, adj, want_T=True):
+        pts = np.ascontiguousarray(pts, np.float32)
+        n = len(pts)
+        T = np.zeros((n, n, 3)) if want_T else None
+        S = np.zeros((n, n))
+        self.lib.lgo_march_edges(C.byref(self.dens), C.byref(self.shader), C.byref(self.settings), n, _p(pts),
+                                 _p(np.ascontiguousarray(adj, np.uint8)), _p(T), _p(S))
+        return T, S
+
+    def fw_maxtimes(self, T):
+        T = np.ascontiguousarray(T, np.float64).copy()
+        self.lib.lgo_fw_maxtimes(T.shape[0], _p(T))
+        return T
+
+    def vertex_light(self, pts, graph_id=0):
+        pts = np.ascontiguousarray(pts, np.float32)
+        L = np.zeros((len(pts), 3))
+        self.lib.lgo_vertex_light(C.byref(self.dens), C.byref(self.temp) if self.temp else None,
+                                  C.byref(self.shader), C.byref(self.settings), self.lights, self.n_lights,
+                                  C.byref(self.env) if self.env else None, len(pts), _p(pts), graph_id, _p(L))
+        return L
+
+    def diffuse(self, T_solved, L):
+        n = T_solved.shape[0]
+        D = np.zeros((n, 3))
+        self.lib.lgo_diffuse(n, _p(np.ascontiguousarray(T_solved, np.float64)),
+                             _p(np.ascontiguousarray(L, np.float64)), _p(D))
+        return D
+
+    def splat(self, pts, D, point_voxel_size, factor=None, kernel_points=None):
+        pts = np.ascontiguousarray(pts, np.float32)
+        D = np.ascontiguousarray(D, np.float64)
+        f = factor or self.opts.scatterGridResFactor
+        K = kernel_points if kernel_points is not None else self.opts.ptsPerKernel * self.opts.iter
+        lo = (C.c_int32 * 3)()
+        dims = (C.c_int32 * 3)()
+        d = self.dens.desc
+        box = []
+        for a in range(3):
+            l = (d.origin[a] // f) - 1
+            h = (d.origin[a] + d.dims[a] - 1) // f + 1
+            box.append(h - l + 1)
+        out = np.zeros((box[2], box[1], box[0], 3))
+        r = self.lib.lgo_splat(C.byref(self.dens), f, len(pts), _p(pts), _p(D), point_voxel_size, K, lo, dims,
+                               _p(out))
+        return tuple(lo), tuple(dims), out, r
+
+    def render(self, sg=None, rows=None, counters=False):
+        """sg = (lo, dims, values (z,y,x,3)) of the scatter grid, or None."""
+        cam = self.opts.camera_c()
+        W, H = self.opts.width, self.opts.height
+        r0, r1 = (0, H) if rows is None else rows
+        films = [np.zeros((H, W, 4), np.float32) for _ in range(4)]
+        cnt = np.zeros(2, np.uint64)
+        if sg is not None:
+            lo, dims, vals = sg
+            vals32 = np.ascontiguousarray(vals, np.float32)
+            lo_c, dims_c = (C.c_int32 * 3)(*lo), (C.c_int32 * 3)(*dims)
+            sg_h = self.dens.desc.voxel_size * self.opts.scatterGridResFactor
+        else:
+            vals32, lo_c, dims_c, sg_h = None, None, None, 1.0
+        self.lib.lgo_render(C.byref(self.dens), C.byref(self.temp) if self.temp else None, C.byref(self.shader),
+                            C.byref(self.settings), self.lights, self.n_lights,
+                            C.byref(self.env) if self.env else None, C.byref(cam), lo_c, dims_c, sg_h, _p(vals32),
+                            r0, r1, *[_p(f) for f in films], _p(cnt))
+        return (films, cnt) if counters else films
+
+    def env_cdf(self):
+        w, h = self.env.w, self.env.h
+        cf = np.zeros((h, w), np.float32)
+        cc = np.zeros((h, w + 1), np.float32)
+        ci = np.zeros(h, np.float32)
+        mf = np.zeros(h, np.float32)
+        mc = np.zeros(h + 1, np.float32)
+        mi = np.zeros(1, np.float32)
+        self.lib.lgo_env_cdf(C.byref(self.env), *[_p(x) for x in (cf, cc, ci, mf, mc, mi)])
+        return cf, cc, ci, mf, mc, mi[0]
+
+
+def fw_minplus_f32(S):
+    S = np.ascontiguousarray(S, np.float32).copy()
+    load().lgo_fw_minplus_f32(S.shape[0], _p(S))
+    return S
+
+
+def fw_minplus_f64(S):
+    S = np.ascontiguousarray(S, np.float64).copy()
+    load().lgo_fw_minplus_f64(S.shape[0], _p(S))
+    return S
+
+
+def build_graph(pts, radius_sq, max_connect=12):
+    pts = np.ascontiguousarray(pts, np.float32)
+    n = len(pts)
+    adj = np.zeros((n, n), np.uint8)
+    ne = load().lgo_build_graph(n, _p(pts), C.c_float(radius_sq), max_connect, _p(adj))
+    return adj, ne

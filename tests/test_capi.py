@@ -1,0 +1,105 @@
+"""The C-ABI library: loads without a GPU, exports every declared symbol, and
+its host helpers mirror the reference's scene description."""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+import pytest
+
+from lightgraph_gb300 import _capi
+from lightgraph_gb300.lightgraph import ColorRamp, Light, Shader
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions():
+    names = set()
+    for h in ("lightgraph_c.h", "lightgraph_scene.h"):
+        src = open(os.path.join(ROOT, "include", h)).read()
+        src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+        for m in re.finditer(r"\b((?:lg|lgs)_[a-z0-9_]+)\s*\(", src):
+            names.add(m.group(1))
+    return names
+
+
+def test_exports_every_declared_symbol():
+    lib = _capi.load()
+    names = declared_functions()
+    assert len(names) > 30
+    missing = [n for n in sorted(names) if not hasattr(lib, n)]
+    assert not missing, missing
+    # and the ctypes table covers them all
+    assert names <= set(_capi.SIGNATURES), sorted(names - set(_capi.SIGNATURES))
+
+
+def test_version_and_no_device_is_reported():
+    lib = _capi.load()
+    assert b"sm_103a" in lib.lg_version()
+    h = C.c_void_p()
+    st = lib.lg_create(0, C.byref(h))
+    if st == _capi.LG_OK:  # running on a GPU host
+        lib.lg_destroy(h)
+    else:
+        assert st == _capi.LG_ERR_NODEVICE
+
+
+def test_shader_defaults_and_coefficients():
+    s = Shader()
+    c = s.to_c()
+    assert c.density_scale == 1.0 and c.density_max == 100.0 and c.scatter_density_scale == 0.35
+    assert c.scatter_density_min == 0.025 and c.scatter_scale == 4.0 and c.scatter_density_mask_power == 0.25
+    # albedo = color * s / (s + a), extinction = -(s + a)  (src/Shader.h:132-133)
+    assert np.allclose(list(c.albedo), [1.5 / 1.6] * 3)
+    assert np.allclose(list(c.extinction), [-1.6] * 3)
+    s.setScattering((1.0, 1.25, 1.5))
+    s.setAbsorption(0.5)
+    s.setVolumeColor((0.5, 1.0, 2.0))
+    c = s.to_c()
+    assert np.allclose(list(c.albedo), [0.5 * 1 / 1.5, 1.25 / 1.75, 2 * 1.5 / 2.0])
+    assert np.allclose(list(c.extinction), [-1.5, -1.75, -2.0])
+
+
+def test_parse_lights():
+    d = Light.parse("dir:0:1,0.5,0.25:0.7:0,0,0")
+    assert d.type == _capi.LG_LIGHT_DISTANT
+    assert np.allclose(list(d.c.dir), [0, 0, -1])
+    assert np.allclose(list(d.c.color), [1, 0.5, 0.25])
+    assert d.c.intensity == pytest.approx(np.float32(0.7))
+    # directions stay unit length and the yRot turntable rotates about +y
+    d2 = Light.parse("dir:90:1:1:0,0,0")
+    assert np.allclose(np.linalg.norm(list(d2.c.dir)), 1.0)
+    assert abs(d2.c.dir[1]) < 1e-12
+    p = Light.parse("point:0:1,1,1:3:0.5,0.25,-1")
+    assert p.type == _capi.LG_LIGHT_POINT and np.allclose(list(p.c.pos), [0.5, 0.25, -1])
+    e = Light.parse("env:0:1,1,1:1.0:3:/some/map.exr")
+    assert e.type == _capi.LG_LIGHT_ENV and e.c.samples == 3
+    with pytest.raises(ValueError):
+        Light.parse("spot:0:1:1:0,0,0")
+
+
+def test_parse_color_ramp():
+    r = ColorRamp.parse("0.0,0.33,0.66,1.0/0,0,0:1.0,0.076,0.0:1.0,0.322,0.0:1.0,0.45,0.15/0.35/1.5")
+    assert r.positions == [0.0, 0.33, 0.66, 1.0]
+    assert r.colors[1] == [1.0, 0.076, 0.0]
+    assert (r.in_, r.out) == (0.35, 1.5)
+
+
+def test_point_voxel_size_estimate():
+    lib = _capi.load()
+    rng = np.random.default_rng(0)
+    pts = rng.random((8000, 3)).astype(np.float32)
+    h = lib.lg_point_voxel_size(len(pts), pts.ctypes.data, 8)
+    # ~8 points per h^3 over a unit-ish box
+    assert h == pytest.approx(np.cbrt(np.prod(pts.max(0) - pts.min(0)) / 1000), rel=1e-6)
+    assert lib.lg_point_voxel_size(1, pts.ctypes.data, 8) == 0.1
+
+
+def test_scene_generator_is_deterministic():
+    from lightgraph_gb300 import scenes
+    a = scenes.volume(_capi.LGS_VOLUME_SPHERE_FBM, 32, 4, 0)
+    b = scenes.volume(_capi.LGS_VOLUME_SPHERE_FBM, 32, 4, 0)
+    assert np.array_equal(a, b) and a.max() <= 1.0 and a.min() >= 0.0 and (a > 0).any()
+    p = scenes.points(a, 0.04, 100, seed=5)
+    q = scenes.points(a, 0.04, 100, seed=5)
+    assert np.array_equal(p, q) and len(p) == 100

@@ -1,0 +1,208 @@
+"""GPU path vs the CPU oracle, stage by stage and end to end.
+
+Tolerances (stated per test):
+  adjacency            bit-exact
+  Floyd-Warshall       <= 1e-6 relative vs the oracle's FP32 min-plus on the same input
+  edge optical depth   <= 1e-4 relative vs FP64 (FP32 accumulation on the GPU)
+  vertex light / D     <= 1e-4 relative vs FP64
+  scatter grid         <= 1e-4 relative vs FP64 on the same radiances
+  films (AOVs)         relative RMSE <= 1e-3 vs the FP64 oracle
+"""
+import numpy as np
+import pytest
+
+from lightgraph_gb300 import scenes
+from oracle import pyoracle as po
+
+pytestmark = pytest.mark.gpu
+
+
+def rel_rmse(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    den = np.sqrt(np.mean(b * b))
+    if den == 0:
+        return float(np.sqrt(np.mean(a * a)))
+    return float(np.sqrt(np.mean((a - b) ** 2)) / den)
+
+
+def rand_graph_matrix(n, p, seed, symmetric=True):
+    rng = np.random.default_rng(seed)
+    S = np.full((n, n), np.inf, np.float32)
+    mask = rng.random((n, n)) < p
+    w = rng.random((n, n)).astype(np.float32) * 3.0
+    S[mask] = w[mask]
+    if symmetric:
+        S = np.minimum(S, S.T)
+    return S
+
+
+@pytest.mark.parametrize("n", [1, 2, 5, 63, 64, 65, 127, 128, 129, 200, 333, 512])
+def test_fw_matches_oracle_f32(gpu_ctx, n):
+    S = rand_graph_matrix(n, min(1.0, 6.0 / max(n, 1)), seed=n)
+    got = gpu_ctx.fw_host(S)
+    ref = po.fw_minplus_f32(S)
+    fin = np.isfinite(ref)
+    assert np.array_equal(np.isfinite(got), fin)
+    rel = np.abs(got[fin] - ref[fin]) / np.maximum(np.abs(ref[fin]), 1e-30)
+    assert rel.max(initial=0) <= 1e-6
+    ref64 = po.fw_minplus_f64(S.astype(np.float64))
+    rel64 = np.abs(got[fin] - ref64[fin]) / np.maximum(np.abs(ref64[fin]), 1e-30)
+    assert rel64.max(initial=0) <= 1e-5
+
+
+def test_fw_general_nonsymmetric(gpu_ctx):
+    S = rand_graph_matrix(300, 0.03, seed=7, symmetric=False)
+    got = gpu_ctx.fw_host(S)
+    ref = po.fw_minplus_f32(S)
+    fin = np.isfinite(ref)
+    assert np.array_equal(np.isfinite(got), fin)
+    assert np.allclose(got[fin], ref[fin], rtol=1e-6, atol=0)
+
+
+@pytest.fixture(scope="module")
+def small_scene():
+    return scenes.small(n_points=512, width=64, height=64, spp=2)
+
+
+@pytest.fixture(scope="module")
+def small_oracle(small_scene):
+    sc = small_scene
+    return po.Oracle(sc.density, sc.shader, sc.opts, sc.lights)
+
+
+@pytest.mark.parametrize("max_connect", [0, 1, 3, 12])
+@pytest.mark.parametrize("radius", [0.05, 0.15, 0.4])
+def test_adjacency_bitexact(gpu_ctx, small_scene, max_connect, radius):
+    sc = small_scene
+    pts = sc.points[0]
+    r2 = np.float32(radius) * np.float32(radius)
+    adj, ne = gpu_ctx.build_graphs([pts], [r2], max_connect, want_adjacency=True)
+    ref, ne_ref = po.build_graph(pts, r2, max_connect)
+    assert np.array_equal(adj[0], ref)
+    assert ne[0] == ne_ref
+
+
+def test_adjacency_ties_and_many_graphs(gpu_ctx):
+    rng = np.random.default_rng(3)
+    graphs, r2s = [], []
+    for g, n in enumerate([0, 1, 7, 100, 300, 257]):
+        p = (rng.random((n, 3)).astype(np.float32) - 0.5) * 0.5
+        if n > 10:
+            p[5] = p[3]          # coincident points
+            p[8] = p[3] + np.float32(0.1)  # exactly on a lattice offset
+        graphs.append(p)
+        r2s.append(np.float32(0.1) * np.float32(0.1))
+    adj, ne = gpu_ctx.build_graphs(graphs, r2s, 12, want_adjacency=True)
+    for g, p in enumerate(graphs):
+        ref, ne_ref = po.build_graph(p, r2s[g], 12)
+        assert np.array_equal(adj[g], ref), g
+        assert ne[g] == ne_ref
+
+
+def test_adjacency_dense_cluster_overflow(gpu_ctx):
+    # more than the stored candidate capacity per row: the greedy pass must
+    # continue the scan on the fly
+    rng = np.random.default_rng(11)
+    p = (rng.random((400, 3)).astype(np.float32) - 0.5) * 0.02
+    r2 = np.float32(1.0)
+    for mc in (12, 200):
+        adj, ne = gpu_ctx.build_graphs([p], [r2], mc, want_adjacency=True)
+        ref, ne_ref = po.build_graph(p, r2, mc)
+        assert np.array_equal(adj[0], ref)
+
+
+@pytest.fixture(scope="module")
+def small_solved(gpu_ctx, small_scene, small_oracle):
+    sc, o = small_scene, small_oracle
+    scenes.load_into(gpu_ctx, sc)
+    adj, _ = gpu_ctx.build_graphs(sc.points, sc.radius_sq, sc.max_connect, want_adjacency=True)
+    S_gpu = gpu_ctx.march_edges(want=True)[0]
+    dist_gpu = gpu_ctx.solve_paths(want=True)[0]
+    L_gpu = gpu_ctx.vertex_light(want=True)
+    D_gpu = gpu_ctx.diffuse(want=True)
+    T, S_ref = o.march_edges(sc.points[0], adj[0])
+    return dict(adj=adj[0], S_gpu=S_gpu, dist_gpu=dist_gpu, L_gpu=L_gpu, D_gpu=D_gpu, T=T, S_ref=S_ref)
+
+
+def test_edge_march(small_solved):
+    r = small_solved
+    fin = np.isfinite(r["S_ref"])
+    assert fin.sum() > 100
+    assert np.array_equal(np.isfinite(r["S_gpu"]), fin)
+    assert np.allclose(r["S_gpu"][fin], r["S_ref"][fin], rtol=1e-4, atol=1e-6)
+    # the reference's RGB edge transmittance is exp(extinction_c * S)
+    T = r["T"]
+    nz = T[..., 0] > 0
+    assert np.array_equal(nz, fin)
+    assert np.allclose(T[fin][:, 0], np.exp(-np.float64(0.1) * r["S_ref"][fin]), rtol=1e-12)
+
+
+def test_apsp_pipeline(small_solved):
+    r = small_solved
+    ref = po.fw_minplus_f64(r["S_ref"])
+    np.fill_diagonal(ref, 0.0)
+    fin = np.isfinite(ref)
+    assert np.array_equal(np.isfinite(r["dist_gpu"]), fin)
+    rel = np.abs(r["dist_gpu"][fin] - ref[fin]) / np.maximum(ref[fin], 1e-12)
+    assert rel.max() <= 1e-4
+    # the FW kernel itself on the GPU's own S: FP32 oracle within 1e-6
+    ref32 = po.fw_minplus_f32(r["S_gpu"])
+    np.fill_diagonal(ref32, 0.0)
+    assert np.allclose(r["dist_gpu"][fin], ref32[fin], rtol=1e-6, atol=0)
+
+
+def test_vertex_light(small_solved, small_scene, small_oracle):
+    L_ref = small_oracle.vertex_light(small_scene.points[0])
+    assert np.allclose(small_solved["L_gpu"], L_ref, rtol=1e-4, atol=1e-6)
+
+
+def test_diffuse(small_solved, small_scene, small_oracle):
+    o = small_oracle
+    Tsol = o.fw_maxtimes(small_solved["T"])
+    L_ref = o.vertex_light(small_scene.points[0])
+    D_ref = o.diffuse(Tsol, L_ref)
+    assert np.allclose(small_solved["D_gpu"], D_ref, rtol=1e-4, atol=1e-6)
+
+
+def test_splat_and_render(gpu_ctx, small_scene, small_oracle, small_solved):
+    sc, o = small_scene, small_oracle
+    gpu_ctx.splat()
+    lo, dims, sg = gpu_ctx.scatter_grid()
+    hp = gpu_ctx.lib.lg_point_voxel_size(len(sc.points[0]), sc.points[0].ctypes.data, 8)
+    lo_r, dims_r, sg_ref, _ = o.splat(sc.points[0], small_solved["D_gpu"].astype(np.float64), hp)
+    assert tuple(lo) == tuple(lo_r) and tuple(dims) == tuple(dims_r)
+    assert np.allclose(sg, sg_ref, rtol=1e-4, atol=1e-6)
+    films = gpu_ctx.render(sc.opts)
+    ref = o.render((lo, dims, sg))
+    for k, name in enumerate(["rgba", "direct", "scatter", "emission"]):
+        got = getattr(films, name)
+        e = rel_rmse(got, ref[k])
+        assert e <= 1e-3, (name, e)
+
+
+def test_full_frame_vs_fp64_oracle(gpu_ctx, small_scene, small_oracle):
+    sc, o = small_scene, small_oracle
+    scenes.load_into(gpu_ctx, sc)
+    films = gpu_ctx.render_frame(sc.points, sc.radius_sq, sc.opts, sc.max_connect)
+    # FP64 reference-faithful chain on the CPU
+    adj, _ = o.build_graph(sc.points[0], sc.radius_sq[0], sc.max_connect)
+    T, _ = o.march_edges(sc.points[0], adj)
+    Tsol = o.fw_maxtimes(T)
+    L = o.vertex_light(sc.points[0])
+    D = o.diffuse(Tsol, L)
+    hp = gpu_ctx.lib.lg_point_voxel_size(len(sc.points[0]), sc.points[0].ctypes.data, 8)
+    lo, dims, sg, _ = o.splat(sc.points[0], D, hp)
+    ref = o.render((lo, dims, sg))
+    for k, name in enumerate(["rgba", "direct", "scatter", "emission"]):
+        e = rel_rmse(getattr(films, name), ref[k])
+        assert e <= 1e-3, (name, e)
+
+
+def test_deterministic(gpu_ctx, small_scene):
+    sc = small_scene
+    scenes.load_into(gpu_ctx, sc)
+    a = gpu_ctx.render_frame(sc.points, sc.radius_sq, sc.opts, sc.max_connect)
+    b = gpu_ctx.render_frame(sc.points, sc.radius_sq, sc.opts, sc.max_connect)
+    for name in ["rgba", "direct", "scatter", "emission"]:
+        assert np.array_equal(getattr(a, name), getattr(b, name))

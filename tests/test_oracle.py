@@ -1,0 +1,163 @@
+"""Known-answer tests that pin the CPU oracle (the reference has no tests or
+fixtures of its own, so these and tests/golden are the pins)."""
+import numpy as np
+import pytest
+
+from lightgraph_gb300 import scenes
+from lightgraph_gb300.lightgraph import ColorRamp, Grid, Light, SceneSettings, Shader
+from oracle import pyoracle as po
+
+
+def slab_scene(density=0.5, res=64):
+    vals = np.full((res, res, res), density, np.float32)
+    g = Grid(vals, (-res // 2,) * 3, 1.0)
+    sh = Shader()
+    sh.setScattering(0.09)
+    sh.setAbsorption(0.01)
+    opts = SceneSettings(width=8, height=8, iter=1)
+    return g, sh, opts
+
+
+def test_homogeneous_edge_transmittance():
+    """Constant density: samples at t = k*step inside the span, each adding
+    max(rho*dS*shadowDS*scatterDS, densityMin)*step."""
+    g, sh, opts = slab_scene(0.5)
+    o = po.Oracle(g, sh, opts)
+    # two points along x, 30 voxels apart, well inside the grid
+    p = np.array([[-15.3, 0.2, 0.1], [14.7, 0.2, 0.1]], np.float32)
+    adj = np.array([[0, 1], [1, 0]], np.uint8)
+    T, S = o.march_edges(p, adj)
+    dist = float(np.linalg.norm(p[1].astype(np.float64) - p[0].astype(np.float64)))
+    t0 = 1e-9  # Delta start time, inside the first leaf span
+    ks = np.arange(np.ceil(t0 / 3.0), np.floor(np.float32(dist) / 3.0) + 1)
+    x = max(0.5 * 1.0 * 1.0 * 0.35, 0.025)
+    assert S[0, 1] == pytest.approx(len(ks) * x * 3.0, rel=1e-12)
+    assert np.allclose(T[0, 1], np.exp(-0.1 * len(ks) * x * 3.0), rtol=1e-12)
+
+
+def test_edge_dropout_and_miss():
+    g, sh, opts = slab_scene(1.0)
+    sh.setScatterDensityScale(10.0)
+    o = po.Oracle(g, sh, opts)
+    p = np.array([[-25.0, 0, 0], [25.0, 0, 0], [0, 0, 1000.0]], np.float32)
+    adj = np.ones((3, 3), np.uint8)
+    np.fill_diagonal(adj, 0)
+    T, S = o.march_edges(p, adj)
+    assert np.isinf(S[0, 1]) and (T[0, 1] == 0).all()  # opaque: dropout
+    assert S[0, 1] == S[1, 0]
+
+
+def random_graph(n, p, seed):
+    rng = np.random.default_rng(seed)
+    S = np.full((n, n), np.inf)
+    m = rng.random((n, n)) < p
+    S[m] = rng.random((n, n))[m] * 2
+    return np.minimum(S, S.T)
+
+
+@pytest.mark.parametrize("n", [1, 7, 40, 150])
+def test_fw_against_dijkstra(n):
+    scipy = pytest.importorskip("scipy.sparse.csgraph")
+    S = random_graph(n, 0.08, n)
+    got = po.fw_minplus_f64(S)
+    W = np.where(np.isfinite(S), S, 0.0)
+    ref = scipy.dijkstra(W, directed=True)
+    # FW keeps the (i, i) entries as shortest cycles; Dijkstra reports 0
+    off = ~np.eye(n, dtype=bool)
+    assert np.allclose(got[off], ref[off], rtol=1e-12)
+    got32 = po.fw_minplus_f32(S.astype(np.float32))
+    fin = np.isfinite(ref) & off
+    assert np.allclose(got32[fin], ref[fin], rtol=1e-5)
+
+
+def test_maxtimes_equals_minplus():
+    """The reference's RGB max-times FW equals per-channel exp(-a_c * minplus(S))."""
+    n = 60
+    S = random_graph(n, 0.1, 3)
+    a = np.array([0.1, 0.15, 0.3])
+    T = np.where(np.isfinite(S)[..., None], np.exp(-a * np.where(np.isfinite(S), S, 0)[..., None]), 0.0)
+    o = po.load()
+    Tm = np.ascontiguousarray(T.copy())
+    o.lgo_fw_maxtimes(n, Tm.ctypes.data)
+    Sm = po.fw_minplus_f64(S)
+    expect = np.where(np.isfinite(Sm)[..., None], np.exp(-a * np.where(np.isfinite(Sm), Sm, 0)[..., None]), 0.0)
+    idx = np.arange(n)
+    expect[idx, idx] = 1.0
+    assert np.allclose(Tm, expect, rtol=1e-12, atol=1e-300)
+
+
+def test_greedy_graph_cap_order():
+    # five points on a line, all within the radius: the cap is spent in (i, j) order
+    p = np.array([[0, 0, 0], [0.1, 0, 0], [0.2, 0, 0], [0.3, 0, 0], [0.4, 0, 0]], np.float32)
+    adj, ne = po.build_graph(p, np.float32(1.0), max_connect=2)
+    # i=0 takes 1 and 2 (full); i=1 skips 0 (full), takes 2 (1 and 2 now full);
+    # i=2 is full; i=3 skips 0..2 (full) and takes 4.
+    expect = np.zeros((5, 5), np.uint8)
+    for i, j in [(0, 1), (0, 2), (1, 2), (3, 4)]:
+        expect[i, j] = expect[j, i] = 1
+    assert np.array_equal(adj, expect)
+    assert ne == 4
+    # strict radius: a pair exactly at the radius is not connected
+    q = np.array([[0, 0, 0], [0.5, 0, 0]], np.float32)
+    adj2, _ = po.build_graph(q, np.float32(0.25), 12)
+    assert adj2.sum() == 0
+
+
+def test_color_ramp_knots_via_vertex_emission():
+    res = 32
+    vals = np.full((res, res, res), 0.5, np.float32)
+    g = Grid(vals, (-16,) * 3, 1.0)
+    sh = Shader()
+    sh.setEmissionScale(2.0)
+    sh.setEmissionColorRamp(ColorRamp([0.0, 0.5, 1.0], [[0, 0, 0], [1, 0.5, 0.25], [1, 1, 1]], 100.0, 300.0))
+    opts = SceneSettings(iter=1)
+    for temp, expect in [(100.0, [0, 0, 0]), (200.0, [1, 0.5, 0.25]), (300.0, [1, 1, 1]), (150.0, [0.5, 0.25, 0.125]),
+                         (50.0, [0, 0, 0]), (1000.0, [1, 1, 1])]:
+        tg = Grid(np.full((res, res, res), temp, np.float32), (-16,) * 3, 1.0)
+        o = po.Oracle(g, sh, opts, [], temperature=tg)
+        L = o.vertex_light(np.zeros((1, 3), np.float32))
+        assert np.allclose(L[0], 2.0 * np.array(expect)), temp
+
+
+def test_env_cdf_step_function():
+    """Distribution1D over a step function (src/Sampling.h:81-93): the CDF is
+    the normalised running sum of func/n."""
+    h, w = 4, 8
+    env = np.zeros((h, w, 3), np.float32)
+    env[:, 4:, :] = 1.0  # right half bright
+    g, sh, opts = slab_scene(0.1, 16)
+    o = po.Oracle(g, sh, opts, [Light.parse("env:0:1:1:2:x")], env_map=env)
+    cf, cc, ci, mf, mc, mi = o.env_cdf()
+    sin_t = np.sin(np.pi * (np.arange(h, dtype=np.float32) / np.float32(h - 1))).astype(np.float32)
+    for r in range(h):
+        if sin_t[r] == 0:
+            assert np.allclose(cc[r], np.arange(w + 1) / w)
+        else:
+            assert np.allclose(cc[r], np.clip((np.arange(w + 1) - 4) / 4, 0, 1), atol=1e-7)
+    assert mc[0] == 0 and mc[-1] == pytest.approx(1.0)
+
+
+def test_render_empty_grid_is_transparent():
+    res = 16
+    g = Grid(np.zeros((res, res, res), np.float32), (-8,) * 3, 0.1)
+    sh = Shader()
+    opts = SceneSettings(width=6, height=4, samples=2, camTranslate=(0, 0, 5), iter=1)
+    o = po.Oracle(g, sh, opts, [Light.parse("dir:0:1:1:0,0,0")])
+    rgba, direct, scatter, emission = o.render()
+    assert np.all(rgba[..., :3] == 0) and np.all(rgba[..., 3] == 0)
+    assert np.all(direct == 0) and np.all(scatter == 0) and np.all(emission == 0)
+
+
+def test_small_scene_oracle_runs_and_conserves_energy():
+    sc = scenes.small(n_points=200, width=16, height=16)
+    o = po.Oracle(sc.density, sc.shader, sc.opts, sc.lights)
+    adj, ne = o.build_graph(sc.points[0], sc.radius_sq[0])
+    assert ne > 100 and adj.sum(1).max() <= 12
+    T, S = o.march_edges(sc.points[0], adj)
+    Ts = o.fw_maxtimes(T)
+    L = o.vertex_light(sc.points[0])
+    D = o.diffuse(Ts, L)
+    # column-normalised diffusion with all column sums >= 1 conserves total radiance
+    colsum = Ts.sum(axis=0)
+    if (colsum >= 1).all():
+        assert np.allclose(D.sum(0), L.sum(0), rtol=1e-9)
