@@ -36,7 +36,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 STAGES = ["build_graph", "edge_march", "floyd_warshall", "vertex_light", "diffuse", "splat", "render"]
-NOMINAL_FP32_TFLOPS = 152 * 128 * 2 * 2.070  # GB300: SMs x FP32 lanes x 2 (FMA) x max clock (GHz)
+NOMINAL_FP32_TFLOPS = 152 * 128 * 2 * 2.070 / 1000  # GB300: SMs x FP32 lanes x 2 (FMA) x 2.07 GHz
 
 
 def parse():
@@ -47,6 +47,8 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--small", action="store_true", help="the 128^3 / 1024-point / 256^2 case instead")
+    ap.add_argument("--image", type=int, default=0, help="override the square image size (profiling runs)")
+    ap.add_argument("--spp", type=int, default=0, help="override the samples per pixel (profiling runs)")
     return ap.parse_args()
 
 
@@ -57,11 +59,14 @@ def dist_env():
     return rank, world, local
 
 
-def make_scene(small: bool):
+def make_scene(small: bool, image: int = 0, spp: int = 0):
     from lightgraph_gb300 import scenes
-    if small:
-        return scenes.small()
-    return scenes.production()
+    sc = scenes.small() if small else scenes.production()
+    if image > 0:
+        sc.opts.width = sc.opts.height = image
+    if spp > 0:
+        sc.opts.samples = spp
+    return sc
 
 
 def workload_config(sc, small):
@@ -215,7 +220,7 @@ def run_reference(args):
     rank, world, local = dist_env()
     if rank != 0:
         return 0
-    sc = make_scene(args.small)
+    sc = make_scene(args.small, args.image, args.spp)
     fw_rounds, stride = (32, 256) if not args.small else (64, 32)
     vals = []
     for _ in range(args.warmup):
@@ -251,7 +256,7 @@ def run_ours(args):
     if world > 1:
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     torch.cuda.set_device(local)
-    sc = make_scene(args.small)
+    sc = make_scene(args.small, args.image, args.spp)
     ctx = Context(local)
     scenes.load_into(ctx, sc)
     ctx.build_graphs(sc.points, sc.radius_sq, sc.max_connect)
@@ -346,7 +351,8 @@ def run_ours(args):
         "gpu_launches": int(launches),
         "clocks": clk,
         "stages_ms": {k: round(float(v), 4) for k, v in zip(STAGES, stage_ms)},
-        "roofline": {"kernel": "k_render", "bound": "hbm", "achieved": achieved,
+        "roofline": {"kernel": "render waves (k_primary x2, k_shadow, k_resolve)", "bound": "hbm",
+                     "achieved": achieved,
                      "peak": peaks.get("hbm_gbs"), "unit": "GB/s",
                      "frac": achieved / peaks.get("hbm_gbs"), "peak_kind": peak_kind,
                      "traffic": profile_traffic("k_render_production.txt"),

@@ -273,6 +273,11 @@ lg_status lg_render_frame(lg_ctx* ctx, int n_graphs, const float* points,
 lg_status lg_frame_device(lg_ctx* ctx, int max_connect, double point_voxel_size,
                           const lg_camera* camera);
 
+/* Copies the films of the last render (lg_render, lg_frame_device) to host
+ * memory, waiting for it; width x height x 4 floats each, any may be null. */
+lg_status lg_get_films(lg_ctx* ctx, float* rgba, float* direct, float* scatter,
+                       float* emission);
+
 /* Statistics of the last render on this context (after a sync): number of
  * density samples taken by primary and shadow rays. */
 lg_status lg_render_stats(lg_ctx* ctx, uint64_t* primary_samples,
@@ -287,6 +292,23 @@ lg_status lg_render_stats(lg_ctx* ctx, uint64_t* primary_samples,
 lg_status lg_set_profiling(lg_ctx* ctx, int on);
 lg_status lg_stage_times(lg_ctx* ctx, double* ms, int n);
 
+/* Frame replay: when on, lg_frame_device runs the frame once, captures the
+ * same launch sequence in a CUDA graph and replays it on later calls with the
+ * same camera while no scene state or buffer changed. */
+lg_status lg_set_graph_mode(lg_ctx* ctx, int on);
+/* Kernels in one captured frame (0 before the first capture). */
+uint64_t lg_frame_launches(const lg_ctx* ctx);
+
+/* Schedule of the path solve over all loaded graphs. -1 (default): chosen by
+ * the autotuner, which times every candidate once per (graph count, largest
+ * graph) on a scratch copy and keeps the fastest; 0: two launches per round
+ * per graph; 1 or 2: one persistent launch for every graph with 1 or 2 CTAs
+ * per SM (a work queue with per-graph dependency counters). */
+lg_status lg_set_fw_schedule(lg_ctx* ctx, int schedule);
+/* The schedule in use and the autotuner's timings (ms) of schedules 0, 1, 2.
+ * Returns LG_ERR_TIMEOUT if a persistent solve reported a stalled queue. */
+lg_status lg_fw_schedule(lg_ctx* ctx, int* schedule, double* tuned_ms, int n);
+
 /* ------------------------------------------------------------------------- */
 /* Kernel-level entry points (device pointers, caller's stream)              */
 /* ------------------------------------------------------------------------- */
@@ -300,6 +322,65 @@ lg_status lg_fw_device(float* dist, int n, int ld, void* stream);
 
 /* Host-memory convenience wrapper of lg_fw_device (copies in and out). */
 lg_status lg_fw_host(lg_ctx* ctx, float* dist, int n);
+
+/* ------------------------------------------------------------------------- */
+/* Serving (no counterpart in the reference, which renders one frame per run) */
+/* ------------------------------------------------------------------------- */
+
+typedef struct lg_server lg_server;
+
+typedef struct lg_server_opts {
+    int32_t device;
+    int32_t max_inflight;          /* requests on the device at once (slots)    */
+    int32_t queue_capacity;        /* waiting requests before LG_ERR_BUSY        */
+    int32_t _pad0;
+    uint64_t hbm_budget_bytes;     /* device bytes admitted at once (0: 64 GiB)  */
+} lg_server_opts;
+
+/* A render request against a resident volume: one frame of the three stages
+ * with its own graphs, lights, shader, settings (settings.seed keys its random
+ * streams) and camera. Arrays are copied at submit time. Environment lights
+ * are not accepted (no per-request map). */
+typedef struct lg_request {
+    int32_t volume;                /* id from lg_server_add_volume                */
+    int32_t n_graphs;
+    const float* points;
+    const int64_t* offsets;
+    const float* radius_sq;
+    int32_t max_connect;
+    int32_t n_lights;
+    const lg_light* lights;
+    lg_shader shader;
+    lg_settings settings;
+    lg_camera camera;
+    double point_voxel_size;
+} lg_request;
+
+/* Creates a server with max_inflight slots (one context, stream and worker
+ * thread each). Admission is FIFO: the head request is admitted when a slot is
+ * free and its lg_request_bytes fit in hbm_budget_bytes next to the requests
+ * in flight; admitted requests run concurrently. */
+lg_status lg_server_create(const lg_server_opts* opts, lg_server** out);
+lg_status lg_server_destroy(lg_server* srv);
+const char* lg_server_last_error(const lg_server* srv);
+/* Uploads a volume (density and optional temperature) that stays resident for
+ * the server's lifetime; *volume_id names it in requests. */
+lg_status lg_server_add_volume(lg_server* srv, const lg_grid_desc* density,
+                               const float* density_values,
+                               const lg_grid_desc* temperature,
+                               const float* temperature_values,
+                               int storage_dtype, int32_t* volume_id);
+/* Enqueues a request and returns at once; *ticket identifies it.
+ * LG_ERR_BUSY: queue full; LG_ERR_NOMEM: larger than the whole budget. */
+lg_status lg_server_submit(lg_server* srv, const lg_request* req, int64_t* ticket);
+/* Waits for a request (timeout_ms < 0: no limit; LG_ERR_TIMEOUT otherwise)
+ * and copies its beauty film (width x height x 4 floats) into rgba if
+ * non-null. queue_us: submit -> admit, latency_us: submit -> done (host
+ * microseconds). A ticket can be waited for once. */
+lg_status lg_server_wait(lg_server* srv, int64_t ticket, int timeout_ms,
+                         float* rgba, double* queue_us, double* latency_us);
+/* Device bytes a request is charged against the HBM budget. */
+uint64_t lg_request_bytes(const lg_request* req);
 
 /* ------------------------------------------------------------------------- */
 /* Host helpers: the reference's scene description (no device work)          */

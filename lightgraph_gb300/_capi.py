@@ -69,6 +69,18 @@ class CameraC(C.Structure):
                 ("width", C.c_int32), ("height", C.c_int32), ("samples", C.c_int32), ("_pad0", C.c_int32)]
 
 
+class ServerOptsC(C.Structure):
+    _fields_ = [("device", C.c_int32), ("max_inflight", C.c_int32), ("queue_capacity", C.c_int32),
+                ("_pad0", C.c_int32), ("hbm_budget_bytes", C.c_uint64)]
+
+
+class RequestC(C.Structure):
+    _fields_ = [("volume", C.c_int32), ("n_graphs", C.c_int32), ("points", C.c_void_p), ("offsets", C.c_void_p),
+                ("radius_sq", C.c_void_p), ("max_connect", C.c_int32), ("n_lights", C.c_int32),
+                ("lights", C.c_void_p), ("shader", ShaderC), ("settings", SettingsC), ("camera", CameraC),
+                ("point_voxel_size", C.c_double)]
+
+
 P = C.c_void_p
 I32, I64, U64, D, F = C.c_int32, C.c_int64, C.c_uint64, C.c_double, C.c_float
 
@@ -100,10 +112,23 @@ SIGNATURES = {
     "lg_render_frame": (I32, [P, C.c_int, P, P, P, C.c_int, D, C.POINTER(CameraC), P, P, P, P]),
     "lg_frame_device": (I32, [P, C.c_int, D, C.POINTER(CameraC)]),
     "lg_render_stats": (I32, [P, C.POINTER(U64), C.POINTER(U64)]),
+    "lg_get_films": (I32, [P, P, P, P, P]),
     "lg_set_profiling": (I32, [P, C.c_int]),
     "lg_stage_times": (I32, [P, C.POINTER(D), C.c_int]),
+    "lg_set_graph_mode": (I32, [P, C.c_int]),
+    "lg_frame_launches": (U64, [P]),
+    "lg_set_fw_schedule": (I32, [P, C.c_int]),
+    "lg_fw_schedule": (I32, [P, C.POINTER(C.c_int), C.POINTER(D), C.c_int]),
     "lg_fw_device": (I32, [P, C.c_int, C.c_int, P]),
     "lg_fw_host": (I32, [P, P, C.c_int]),
+    "lg_server_create": (I32, [C.POINTER(ServerOptsC), C.POINTER(P)]),
+    "lg_server_destroy": (I32, [P]),
+    "lg_server_last_error": (C.c_char_p, [P]),
+    "lg_server_add_volume": (I32, [P, C.POINTER(GridDesc), P, C.POINTER(GridDesc), P, C.c_int,
+                                   C.POINTER(C.c_int32)]),
+    "lg_server_submit": (I32, [P, C.POINTER(RequestC), C.POINTER(I64)]),
+    "lg_server_wait": (I32, [P, I64, C.c_int, P, C.POINTER(D), C.POINTER(D)]),
+    "lg_request_bytes": (U64, [C.POINTER(RequestC)]),
     "lg_shader_default": (None, [C.POINTER(ShaderC)]),
     "lg_shader_set_coefficients": (None, [C.POINTER(ShaderC), C.POINTER(D), C.POINTER(D), C.POINTER(D)]),
     "lg_settings_default": (None, [C.POINTER(SettingsC)]),

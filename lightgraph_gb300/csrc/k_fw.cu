@@ -8,11 +8,11 @@
 //   S_ij = min(S_ij, S_ik + S_kj).
 // This file solves that recurrence in FP32 with the 3-phase blocked schedule,
 // k-blocks of 64:
-//   k_fw_panels : the diagonal tile is closed in shared memory, then each
-//                 CTA closes one tile of the k-block row or column panel
-//                 (every CTA recomputes the diagonal tile, which saves a
-//                 launch and a grid-wide dependency per round);
-//   k_fw_update : every other element, S_ij = min(S_ij, min_k A_ik + B_kj),
+//   panel tiles : the diagonal tile is closed in shared memory, then one tile
+//                 of the k-block row or column panel (every panel CTA
+//                 recomputes the diagonal tile, which saves a launch and a
+//                 dependency per round);
+//   update tiles: every other element, S_ij = min(S_ij, min_k A_ik + B_kj),
 //                 a min-plus product on the CUDA cores. Each thread owns an
 //                 8x8 register tile and consumes k in pairs:
 //                   s = add.rn.f32x2({A_ik, A_ik+1}, {B_kj, B_k+1,j})
@@ -21,6 +21,18 @@
 // It is not a dense contraction, so tensor cores do not apply.
 // All values must be >= 0 (or +inf); then row and column k do not change in
 // round k, which makes each round's updates independent of their order.
+//
+// Two drivers share the tile code:
+//   fw_solve         : one matrix, two launches per round (k_fw_panels,
+//                      k_fw_update);
+//   fw_solve_batched : many matrices of different sizes in ONE persistent
+//                      launch (k_fw_persistent). CTAs claim work items from a
+//                      queue ordered round by round; an item waits (bounded)
+//                      on per-graph completion counters for the items it
+//                      depends on, which always come earlier in the queue, so
+//                      the schedule cannot deadlock whatever the residency.
+#include <algorithm>
+
 #include "lg_kernels.h"
 
 namespace lg {
@@ -35,31 +47,55 @@ __device__ __forceinline__ float min3f(float a, float b, float c) {
     return r;
 }
 
-__device__ __forceinline__ float ld_or_inf(const float* d, int n, int ld, int i, int j) {
-    return (i < n && j < n) ? d[(int64_t)i * ld + j] : kInf;
+// Loads of the matrix. The persistent kernel reads data other CTAs wrote
+// during the same launch, so it reads through L2 (ld.global.cg), never a
+// possibly stale L1 line.
+template <bool kL2>
+__device__ __forceinline__ float ldm(const float* p) {
+    if (kL2) return __ldcg(p);
+    return *p;
+}
+template <bool kL2>
+__device__ __forceinline__ float2 ldm2(const float* p) {
+    if (kL2) return __ldcg(reinterpret_cast<const float2*>(p));
+    return *reinterpret_cast<const float2*>(p);
+}
+template <bool kL2>
+__device__ __forceinline__ float4 ldm4(const float* p) {
+    if (kL2) return __ldcg(reinterpret_cast<const float4*>(p));
+    return *reinterpret_cast<const float4*>(p);
 }
 
-// Phases 1 and 2 of round kb. blockIdx.x: 0 = diagonal tile, 1..nt-1 = row
-// panel tiles, nt..2nt-2 = column panel tiles (the diagonal's index skipped).
-__global__ void __launch_bounds__(256) k_fw_panels(float* __restrict__ d, int n, int ld, int kb) {
-    __shared__ float Dg[kKB][kKB + 1];
-    __shared__ float T[kKB][kKB + 1];
+template <bool kL2>
+__device__ __forceinline__ float ld_or_inf(const float* d, int n, int ld, int i, int j) {
+    return (i < n && j < n) ? ldm<kL2>(d + (int64_t)i * ld + j) : kInf;
+}
+
+struct PanelSmem {
+    float Dg[kKB][kKB + 1];
+    float T[kKB][kKB + 1];
+};
+
+// Panel tile b of round kb: 0 = diagonal, 1..nt-1 = row panel, nt..2nt-2 =
+// column panel (the diagonal's index skipped). 256 threads.
+template <bool kL2>
+__device__ __forceinline__ void fw_panel_tile(float* __restrict__ d, int n, int ld, int kb, int b, PanelSmem& sm) {
     const int nt = (n + kKB - 1) / kKB;
     const int tid = threadIdx.x, ty = tid >> 4, tx = tid & 15;
     const int K0 = kb * kKB;
     int kind = 0, other = kb;  // 0 diag, 1 row tile (K0, other), 2 col tile (other, K0)
-    if (blockIdx.x > 0) {
-        int b = blockIdx.x - 1;
+    if (b > 0) {
+        int q = b - 1;
         kind = 1;
-        if (b >= nt - 1) { kind = 2; b -= nt - 1; }
-        other = b < kb ? b : b + 1;
+        if (q >= nt - 1) { kind = 2; q -= nt - 1; }
+        other = q < kb ? q : q + 1;
     }
     const int O0 = other * kKB;
     for (int e = tid; e < kKB * kKB; e += 256) {
         const int r = e >> 6, c = e & 63;
-        Dg[r][c] = ld_or_inf(d, n, ld, K0 + r, K0 + c);
-        if (kind == 1) T[r][c] = ld_or_inf(d, n, ld, K0 + r, O0 + c);
-        if (kind == 2) T[r][c] = ld_or_inf(d, n, ld, O0 + r, K0 + c);
+        sm.Dg[r][c] = ld_or_inf<kL2>(d, n, ld, K0 + r, K0 + c);
+        if (kind == 1) sm.T[r][c] = ld_or_inf<kL2>(d, n, ld, K0 + r, O0 + c);
+        if (kind == 2) sm.T[r][c] = ld_or_inf<kL2>(d, n, ld, O0 + r, K0 + c);
     }
     __syncthreads();
     // phase 1: close the diagonal tile
@@ -67,12 +103,12 @@ __global__ void __launch_bounds__(256) k_fw_panels(float* __restrict__ d, int n,
 #pragma unroll
         for (int r = 0; r < 4; ++r) {
             const int i = ty + 16 * r;
-            const float dik = Dg[i][k];
+            const float dik = sm.Dg[i][k];
 #pragma unroll
             for (int c = 0; c < 4; ++c) {
                 const int j = tx + 16 * c;
-                const float v = dik + Dg[k][j];
-                if (v < Dg[i][j]) Dg[i][j] = v;
+                const float v = dik + sm.Dg[k][j];
+                if (v < sm.Dg[i][j]) sm.Dg[i][j] = v;
             }
         }
         __syncthreads();
@@ -80,7 +116,7 @@ __global__ void __launch_bounds__(256) k_fw_panels(float* __restrict__ d, int n,
     if (kind == 0) {
         for (int e = tid; e < kKB * kKB; e += 256) {
             const int r = e >> 6, c = e & 63;
-            if (K0 + r < n && K0 + c < n) d[(int64_t)(K0 + r) * ld + K0 + c] = Dg[r][c];
+            if (K0 + r < n && K0 + c < n) d[(int64_t)(K0 + r) * ld + K0 + c] = sm.Dg[r][c];
         }
         return;
     }
@@ -92,8 +128,8 @@ __global__ void __launch_bounds__(256) k_fw_panels(float* __restrict__ d, int n,
 #pragma unroll
             for (int c = 0; c < 4; ++c) {
                 const int j = tx + 16 * c;
-                const float v = (kind == 1) ? Dg[i][k] + T[k][j] : T[i][k] + Dg[k][j];
-                if (v < T[i][j]) T[i][j] = v;
+                const float v = (kind == 1) ? sm.Dg[i][k] + sm.T[k][j] : sm.T[i][k] + sm.Dg[k][j];
+                if (v < sm.T[i][j]) sm.T[i][j] = v;
             }
         }
         __syncthreads();
@@ -102,18 +138,17 @@ __global__ void __launch_bounds__(256) k_fw_panels(float* __restrict__ d, int n,
         const int r = e >> 6, c = e & 63;
         const int gi = kind == 1 ? K0 + r : O0 + r;
         const int gj = kind == 1 ? O0 + c : K0 + c;
-        if (gi < n && gj < n) d[(int64_t)gi * ld + gj] = T[r][c];
+        if (gi < n && gj < n) d[(int64_t)gi * ld + gj] = sm.T[r][c];
     }
 }
 
-// Phase 3 of round kb on a 128x128 tile. 256 threads = 8 warps (4 x 2), each
-// warp 32 x 64, each thread 8 x 8 (rows/cols interleaved so the shared-memory
-// fragment loads are conflict-free 128-bit reads).
-__global__ void __launch_bounds__(256, 2) k_fw_update(float* __restrict__ d, int n, int ld, int kb) {
-    extern __shared__ float4 fw_smem[];
-    float2* As = reinterpret_cast<float2*>(fw_smem);         // [32][kTile + kApad]
-    float2* Bs = As + 32 * (kTile + kApad);                   // [32][kTile]
-    const int I0 = blockIdx.y * kTile, J0 = blockIdx.x * kTile, K0 = kb * kKB;
+// Update tile (ti, tj) of round kb, 128x128. 256 threads = 8 warps (4 x 2),
+// each warp 32 x 64, each thread 8 x 8 (rows/cols interleaved so the
+// shared-memory fragment loads are conflict-free 128-bit reads).
+template <bool kL2>
+__device__ __forceinline__ void fw_update_tile(float* __restrict__ d, int n, int ld, int kb, int ti, int tj,
+                                               float2* __restrict__ As, float2* __restrict__ Bs) {
+    const int I0 = ti * kTile, J0 = tj * kTile, K0 = kb * kKB;
     const int tid = threadIdx.x;
     const bool full = (I0 + kTile <= n) && (J0 + kTile <= n) && (K0 + kKB <= n);
 
@@ -127,12 +162,12 @@ __global__ void __launch_bounds__(256, 2) k_fw_update(float* __restrict__ d, int
             const int gk = K0 + 2 * kp;
             float4 v;
             if (full) {
-                v = *reinterpret_cast<const float4*>(d + (int64_t)gi * ld + gk);
+                v = ldm4<kL2>(d + (int64_t)gi * ld + gk);
             } else {
-                v.x = ld_or_inf(d, n, ld, gi, gk);
-                v.y = ld_or_inf(d, n, ld, gi, gk + 1);
-                v.z = ld_or_inf(d, n, ld, gi, gk + 2);
-                v.w = ld_or_inf(d, n, ld, gi, gk + 3);
+                v.x = ld_or_inf<kL2>(d, n, ld, gi, gk);
+                v.y = ld_or_inf<kL2>(d, n, ld, gi, gk + 1);
+                v.z = ld_or_inf<kL2>(d, n, ld, gi, gk + 2);
+                v.w = ld_or_inf<kL2>(d, n, ld, gi, gk + 3);
             }
             As[kp * (kTile + kApad) + i] = make_float2(v.x, v.y);
             As[(kp + 1) * (kTile + kApad) + i] = make_float2(v.z, v.w);
@@ -147,13 +182,13 @@ __global__ void __launch_bounds__(256, 2) k_fw_update(float* __restrict__ d, int
             const int gk = K0 + 2 * kp, gj = J0 + 4 * j4;
             float4 r0, r1;
             if (full) {
-                r0 = *reinterpret_cast<const float4*>(d + (int64_t)gk * ld + gj);
-                r1 = *reinterpret_cast<const float4*>(d + (int64_t)(gk + 1) * ld + gj);
+                r0 = ldm4<kL2>(d + (int64_t)gk * ld + gj);
+                r1 = ldm4<kL2>(d + (int64_t)(gk + 1) * ld + gj);
             } else {
-                r0.x = ld_or_inf(d, n, ld, gk, gj); r0.y = ld_or_inf(d, n, ld, gk, gj + 1);
-                r0.z = ld_or_inf(d, n, ld, gk, gj + 2); r0.w = ld_or_inf(d, n, ld, gk, gj + 3);
-                r1.x = ld_or_inf(d, n, ld, gk + 1, gj); r1.y = ld_or_inf(d, n, ld, gk + 1, gj + 1);
-                r1.z = ld_or_inf(d, n, ld, gk + 1, gj + 2); r1.w = ld_or_inf(d, n, ld, gk + 1, gj + 3);
+                r0.x = ld_or_inf<kL2>(d, n, ld, gk, gj); r0.y = ld_or_inf<kL2>(d, n, ld, gk, gj + 1);
+                r0.z = ld_or_inf<kL2>(d, n, ld, gk, gj + 2); r0.w = ld_or_inf<kL2>(d, n, ld, gk, gj + 3);
+                r1.x = ld_or_inf<kL2>(d, n, ld, gk + 1, gj); r1.y = ld_or_inf<kL2>(d, n, ld, gk + 1, gj + 1);
+                r1.z = ld_or_inf<kL2>(d, n, ld, gk + 1, gj + 2); r1.w = ld_or_inf<kL2>(d, n, ld, gk + 1, gj + 3);
             }
             float4* dst = reinterpret_cast<float4*>(Bs + kp * kTile + 4 * j4);
             dst[0] = make_float4(r0.x, r1.x, r0.y, r1.y);
@@ -177,10 +212,10 @@ __global__ void __launch_bounds__(256, 2) k_fw_update(float* __restrict__ d, int
                 const int gj = J0 + cbase + 16 * p;
                 float2 v;
                 if (full) {
-                    v = *reinterpret_cast<const float2*>(d + (int64_t)gi * ld + gj);
+                    v = ldm2<kL2>(d + (int64_t)gi * ld + gj);
                 } else {
-                    v.x = ld_or_inf(d, n, ld, gi, gj);
-                    v.y = ld_or_inf(d, n, ld, gi, gj + 1);
+                    v.x = ld_or_inf<kL2>(d, n, ld, gi, gj);
+                    v.y = ld_or_inf<kL2>(d, n, ld, gi, gj + 1);
                 }
                 acc[2 * q + s][2 * p] = v.x;
                 acc[2 * q + s][2 * p + 1] = v.y;
@@ -238,6 +273,19 @@ __global__ void __launch_bounds__(256, 2) k_fw_update(float* __restrict__ d, int
 }
 
 constexpr size_t kUpdateSmem = sizeof(float2) * 32 * (kTile + kApad) + sizeof(float2) * 32 * kTile;
+static_assert(sizeof(PanelSmem) <= kUpdateSmem, "panel tiles reuse the update stage");
+
+__global__ void __launch_bounds__(256) k_fw_panels(float* __restrict__ d, int n, int ld, int kb) {
+    __shared__ PanelSmem sm;
+    fw_panel_tile<false>(d, n, ld, kb, blockIdx.x, sm);
+}
+
+__global__ void __launch_bounds__(256, 2) k_fw_update(float* __restrict__ d, int n, int ld, int kb) {
+    extern __shared__ float4 fw_smem[];
+    float2* As = reinterpret_cast<float2*>(fw_smem);
+    float2* Bs = As + 32 * (kTile + kApad);
+    fw_update_tile<false>(d, n, ld, kb, blockIdx.y, blockIdx.x, As, Bs);
+}
 
 cudaError_t fw_solve(float* d, int n, int ld, cudaStream_t st) {
     if (n <= 0) return cudaSuccess;
@@ -261,10 +309,130 @@ cudaError_t fw_solve(float* d, int n, int ld, cudaStream_t st) {
     return cudaGetLastError();
 }
 
-cudaError_t fw_solve_batched(float* base, const int64_t* offs, const int32_t* ns, const int32_t* lds,
-                             int n_graphs, int max_n, cudaStream_t st) {
-    (void)base; (void)offs; (void)ns; (void)lds; (void)n_graphs; (void)max_n; (void)st;
-    return cudaErrorNotSupported;
+// ---------------------------------------------------------------------------
+// persistent batched solve
+// ---------------------------------------------------------------------------
+
+// Each CTA claims items until the queue is empty. An item is
+// {graph, round, kind (0 panel, 1 update), tile}. Dependencies:
+//   panel  (g, r) : all update items of (g, r - 1) done
+//   update (g, r) : all panel items of (g, r) done
+// both earlier in the queue. Waits spin at most kSpinLimit polls (with
+// nanosleep) and then raise err[0] = 1; every CTA checks err[0] before each
+// item, so a stalled queue ends the launch instead of hanging the GPU.
+constexpr uint32_t kSpinLimit = 1u << 24;  // x ~200 ns sleeps: several seconds
+
+__device__ __forceinline__ uint32_t ld_acquire(const uint32_t* p) {
+    uint32_t v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__global__ void __launch_bounds__(256, 2) k_fw_persistent(float* __restrict__ base, const FwGraph* __restrict__ gs,
+                                                          const int4* __restrict__ items, int n_items,
+                                                          uint32_t* __restrict__ sync) {
+    // sync layout: [0] queue head, [1] error flag, [2 + 2g] panels done of
+    // graph g, [3 + 2g] updates done of graph g
+    extern __shared__ float4 fw_smem[];
+    float2* As = reinterpret_cast<float2*>(fw_smem);
+    float2* Bs = As + 32 * (kTile + kApad);
+    PanelSmem& psm = *reinterpret_cast<PanelSmem*>(fw_smem);
+    __shared__ int s_item;
+    __shared__ int s_abort;
+    uint32_t* head = sync;
+    uint32_t* err = sync + 1;
+    for (;;) {
+        if (threadIdx.x == 0) {
+            s_item = (int)atomicAdd(head, 1u);
+            s_abort = ld_acquire(err) != 0;
+        }
+        __syncthreads();
+        const int it = s_item;
+        if (it >= n_items || s_abort) break;
+        const int4 w = items[it];
+        const FwGraph g = gs[w.x];
+        if (threadIdx.x == 0) {
+            const uint32_t* ctr;
+            uint32_t target;
+            if (w.z == 0) {  // panel: wait for the previous round's updates
+                ctr = sync + 3 + 2 * w.x;
+                target = (uint32_t)w.y * (uint32_t)(g.nu * g.nu);
+            } else {         // update: wait for this round's panels
+                ctr = sync + 2 + 2 * w.x;
+                target = (uint32_t)(w.y + 1) * (uint32_t)(2 * g.nt - 1);
+            }
+            uint32_t spins = 0;
+            while (ld_acquire(ctr) < target) {
+                if (++spins > kSpinLimit || ld_acquire(err) != 0) {
+                    atomicExch(err, 1u);
+                    s_abort = 1;
+                    break;
+                }
+                __nanosleep(200);
+            }
+        }
+        __syncthreads();
+        if (s_abort) break;
+        float* d = base + g.off;
+        if (w.z == 0) {
+            fw_panel_tile<true>(d, g.n, g.ld, w.y, w.w, psm);
+        } else {
+            fw_update_tile<true>(d, g.n, g.ld, w.y, w.w / g.nu, w.w % g.nu, As, Bs);
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            __threadfence();
+            atomicAdd(sync + 2 + 2 * w.x + w.z, 1u);
+        }
+    }
+}
+
+size_t fw_batched_items(const FwGraph* graphs, int n_graphs, int4* items) {
+    int max_nt = 0;
+    for (int g = 0; g < n_graphs; ++g) max_nt = std::max(max_nt, graphs[g].nt);
+    size_t k = 0;
+    for (int r = 0; r < max_nt; ++r) {
+        for (int g = 0; g < n_graphs; ++g) {
+            if (r >= graphs[g].nt) continue;
+            for (int b = 0; b < 2 * graphs[g].nt - 1; ++b) {
+                if (items) items[k] = make_int4(g, r, 0, b);
+                ++k;
+            }
+        }
+        for (int g = 0; g < n_graphs; ++g) {
+            if (r >= graphs[g].nt || graphs[g].nt < 2) continue;
+            for (int t = 0; t < graphs[g].nu * graphs[g].nu; ++t) {
+                if (items) items[k] = make_int4(g, r, 1, t);
+                ++k;
+            }
+        }
+    }
+    return k;
+}
+
+cudaError_t fw_solve_batched(float* base, const FwGraph* graphs, const int4* items, int n_items, uint32_t* sync,
+                             int n_graphs, int ctas, cudaStream_t st) {
+    static bool attr_set = false;
+    if (!attr_set) {
+        cudaError_t e = cudaFuncSetAttribute(k_fw_persistent, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)kUpdateSmem);
+        if (e != cudaSuccess) return e;
+        attr_set = true;
+    }
+    cudaError_t e = cudaMemsetAsync(sync, 0, sizeof(uint32_t) * (2 + 2 * (size_t)n_graphs), st);
+    if (e != cudaSuccess) return e;
+    if (n_items == 0) return cudaSuccess;
+    k_fw_persistent<<<ctas, 256, kUpdateSmem, st>>>(base, graphs, items, n_items, sync);
+    ++g_launch_counter;
+    return cudaGetLastError();
+}
+
+int fw_persistent_ctas_per_sm() {
+    int blocks = 0;
+    cudaFuncSetAttribute(k_fw_persistent, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kUpdateSmem);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, k_fw_persistent, 256, kUpdateSmem) != cudaSuccess)
+        return 1;
+    return std::max(blocks, 1);
 }
 
 __global__ void k_set_diag(float* __restrict__ S, const GraphInfo* __restrict__ graphs) {

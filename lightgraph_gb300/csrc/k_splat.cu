@@ -158,6 +158,26 @@ __global__ void k_scan_add(int32_t* __restrict__ out, int64_t n, const int32_t* 
     cursor[i] = v;
 }
 
+__global__ void k_scan_add_total(int32_t* __restrict__ out, const int32_t* __restrict__ in, int64_t n,
+                                 const int32_t* __restrict__ sums, int32_t* __restrict__ total) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int32_t v = out[i] + sums[i / 1024];
+    out[i] = v;
+    if (i == n - 1 && total) *total = v + in[i];
+}
+
+cudaError_t launch_exclusive_scan(const int32_t* in, int64_t n, int32_t* out, int32_t* block_sums, int32_t* total,
+                                  cudaStream_t st) {
+    if (n <= 0) return total ? cudaMemsetAsync(total, 0, sizeof(int32_t), st) : cudaSuccess;
+    const int64_t nb = (n + 1023) / 1024;
+    k_scan_block<<<(unsigned)nb, 1024, 0, st>>>(in, n, out, block_sums);
+    k_scan_sums<<<1, 1024, 0, st>>>(block_sums, nb);
+    k_scan_add_total<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(out, in, n, block_sums, total);
+    g_launch_counter += 3;
+    return cudaGetLastError();
+}
+
 __global__ void k_bin_scatter(const float* __restrict__ pts, int64_t n, PointBins pb,
                               int32_t* __restrict__ cursor, int32_t* __restrict__ sorted) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;

@@ -15,6 +15,7 @@
 
 namespace lg {
 uint64_t g_launch_counter = 0;
+uint64_t g_alloc_epoch = 0;
 }
 
 using namespace lg;
@@ -276,6 +277,7 @@ lg_status Ctx::upload_grid(int which, const lg_grid_desc* desc, const float* val
     gs.desc = *desc;
     gs.desc.leaf_mask = nullptr;
     gs.valid = true;
+    graph_valid = false;
     ++gs.version;
     return LG_OK;
 }
@@ -291,6 +293,7 @@ extern "C" lg_status lg_clear_temperature(lg_ctx* handle) {
     Ctx* ctx = reinterpret_cast<Ctx*>(handle);
     GUARD(ctx);
     ctx->temp.valid = false;
+    ctx->graph_valid = false;
     return LG_OK;
 }
 
@@ -307,6 +310,7 @@ extern "C" lg_status lg_set_shader(lg_ctx* handle, const lg_shader* s) {
         if (!(s->extinction[c] <= 0.0))
             return ctx->fail(LG_ERR_INVALID, "extinction must be <= 0 per channel (got %g)", s->extinction[c]);
     ctx->shader = *s;
+    ctx->graph_valid = false;
     return LG_OK;
 }
 
@@ -318,6 +322,7 @@ extern "C" lg_status lg_set_settings(lg_ctx* handle, const lg_settings* o) {
     if (o->scatter_grid_res_factor < 1) return ctx->fail(LG_ERR_INVALID, "scatterGridResFactor must be >= 1");
     if (o->iter < 1) return ctx->fail(LG_ERR_INVALID, "iter must be >= 1");
     ctx->settings = *o;
+    ctx->graph_valid = false;
     return LG_OK;
 }
 
@@ -334,6 +339,7 @@ lg_status Ctx::set_lights(const lg_light* ls, int n, const float* env_rgb, int e
     if (need_env && (!env_rgb || env_w < 2 || env_h < 2))
         return fail(LG_ERR_INVALID, "environment light needs an env map of at least 2x2");
     lights.assign(ls, ls + n);
+    graph_valid = false;
     env_valid = false;
     if (env_rgb && env_w > 1 && env_h > 1) {
         const int64_t w = env_w, h = env_h;
@@ -369,9 +375,9 @@ extern "C" lg_status lg_set_lights(lg_ctx* handle, const lg_light* ls, int n, co
 DevScene Ctx::scene() const {
     DevScene sc;
     std::memset(&sc, 0, sizeof sc);
-    sc.dens = dens.g;
-    sc.temp = temp.g;
-    sc.has_temp = temp.valid ? 1 : 0;
+    sc.dens = D().g;
+    sc.temp = T().g;
+    sc.has_temp = T().valid ? 1 : 0;
     const lg_shader& s = shader;
     DevShader& d = sc.sh;
     d.dS = (float)s.density_scale;
@@ -489,6 +495,11 @@ lg_status Ctx::load_graphs(int n_graphs, const float* points, const int64_t* off
     // caller's buffers can change
     CK(cudaStreamSynchronize(st), "graph upload sync");
     point_voxel_size_cache = -1.0;
+    graph_valid = false;
+    fw_queue_valid = false;
+    fw_choice = -1;
+    for (auto& kv : fw_tuned)
+        if (kv.first == std::make_pair(n_graphs, max_n)) fw_choice = kv.second;
     graphs_built = false;
     return LG_OK;
 }
@@ -557,7 +568,7 @@ lg_status Ctx::copy_matrix_out(float* out) {
 
 lg_status Ctx::march_edges() {
     Ctx* ctx = this;
-    if (!dens.valid) return fail(LG_ERR_STATE, "no density grid uploaded");
+    if (!D().valid) return fail(LG_ERR_STATE, "no density grid uploaded");
     if (!graphs_built) return fail(LG_ERR_STATE, "no graphs built");
     CK(d_S.reserve(sizeof(float) * std::max<int64_t>(s_floats, 1)), "S alloc");
     CK(launch_fill(d_S.as<float>(), s_floats, INFINITY, st), "S fill");
@@ -566,19 +577,114 @@ lg_status Ctx::march_edges() {
     return LG_OK;
 }
 
+// Schedules of the path solve: 0 = two launches per round per graph
+// (fw_solve), k >= 1 = one persistent launch for all graphs with k CTAs per SM.
+static lg_status run_fw_schedule(Ctx* ctx, float* base, int choice) {
+    if (choice == 0) {
+        for (const GraphInfo& g : ctx->h_graphs) {
+            if (g.n == 0) continue;
+            CK(fw_solve(base + g.s_off, g.ld, g.ld, ctx->st), "floyd-warshall");
+        }
+        return LG_OK;
+    }
+    int sms = 0;
+    CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device), "device query");
+    CK(fw_solve_batched(base, ctx->d_fwg.as<FwGraph>(), ctx->d_fw_items.as<int4>(), ctx->fw_items_n,
+                        ctx->d_fw_sync.as<uint32_t>(), ctx->n_graphs, choice * sms, ctx->st),
+       "batched floyd-warshall");
+    return LG_OK;
+}
+
+lg_status Ctx::solve_paths_batched(int choice) {
+    Ctx* ctx = this;
+    if (!fw_queue_valid) {
+        std::vector<FwGraph> fg(n_graphs);
+        for (int g = 0; g < n_graphs; ++g) {
+            const GraphInfo& gi = h_graphs[g];
+            fg[g].off = gi.s_off;
+            fg[g].n = gi.ld;  // the padded matrix: every tile is full
+            fg[g].ld = gi.ld;
+            fg[g].nt = gi.n == 0 ? 0 : gi.ld / 64;
+            fg[g].nu = gi.n == 0 ? 0 : gi.ld / 128;
+        }
+        const size_t n_items = fw_batched_items(fg.data(), n_graphs, nullptr);
+        std::vector<int4> items(std::max<size_t>(n_items, 1));
+        fw_batched_items(fg.data(), n_graphs, items.data());
+        CK(d_fwg.reserve(sizeof(FwGraph) * n_graphs), "fw queue alloc");
+        CK(d_fw_items.reserve(sizeof(int4) * items.size()), "fw queue alloc");
+        CK(d_fw_sync.reserve(sizeof(uint32_t) * (2 + 2 * (size_t)n_graphs)), "fw queue alloc");
+        CK(cudaMemcpyAsync(d_fwg.p, fg.data(), sizeof(FwGraph) * n_graphs, cudaMemcpyHostToDevice, st), "fw queue upload");
+        CK(cudaMemcpyAsync(d_fw_items.p, items.data(), sizeof(int4) * items.size(), cudaMemcpyHostToDevice, st),
+           "fw queue upload");
+        CK(cudaStreamSynchronize(st), "fw queue sync");
+        fw_items_n = (int)n_items;
+        fw_queue_valid = true;
+    }
+    (void)choice;
+    return LG_OK;
+}
+
+// Autotuner: times every candidate schedule once on a scratch copy of the
+// batch and keeps the fastest for this (graph count, largest graph) key.
+lg_status Ctx::tune_fw() {
+    Ctx* ctx = this;
+    const std::pair<int, int> key(n_graphs, max_n);
+    for (auto& kv : fw_tuned)
+        if (kv.first == key) { fw_choice = kv.second; return LG_OK; }
+    lg_status s = solve_paths_batched(1);
+    if (s != LG_OK) return s;
+    const int per_sm = fw_persistent_ctas_per_sm();
+    std::vector<int> cands = {0, 1};
+    if (per_sm >= 2) cands.push_back(2);
+    CK(d_fw_tune.reserve(sizeof(float) * std::max<int64_t>(s_floats, 1)), "fw tune alloc");
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0), "event");
+    CK(cudaEventCreate(&e1), "event");
+    int best = 0;
+    float best_ms = 1e30f;
+    for (size_t c = 0; c < cands.size(); ++c) {
+        CK(cudaMemcpyAsync(d_fw_tune.p, d_S.p, sizeof(float) * s_floats, cudaMemcpyDeviceToDevice, st), "fw tune copy");
+        CK(cudaEventRecord(e0, st), "event");
+        s = run_fw_schedule(this, d_fw_tune.as<float>(), cands[c]);
+        if (s != LG_OK) break;
+        CK(cudaEventRecord(e1, st), "event");
+        CK(cudaEventSynchronize(e1), "event sync");
+        float ms = 0.f;
+        CK(cudaEventElapsedTime(&ms, e0, e1), "event time");
+        if (c < 4) fw_tune_ms[c] = ms;
+        if (ms < best_ms) { best_ms = ms; best = cands[c]; }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (s != LG_OK) return s;
+    // a persistent launch reports a stalled queue through its error flag
+    uint32_t flags[2] = {0, 0};
+    CK(cudaMemcpy(flags, d_fw_sync.p, sizeof flags, cudaMemcpyDeviceToHost), "fw flag read");
+    if (flags[1] != 0) return fail(LG_ERR_TIMEOUT, "batched floyd-warshall: a dependency wait timed out");
+    fw_tuned.push_back({key, best});
+    fw_choice = best;
+    return LG_OK;
+}
+
 lg_status Ctx::solve_paths() {
     Ctx* ctx = this;
-    for (const GraphInfo& g : h_graphs) {
-        if (g.n == 0) continue;
-        CK(fw_solve(d_S.as<float>() + g.s_off, g.ld, g.ld, st), "floyd-warshall");
+    if (fw_choice < 0) {
+        lg_status s = tune_fw();
+        if (s != LG_OK) return s;
     }
+    if (fw_choice > 0) {
+        lg_status s = solve_paths_batched(fw_choice);
+        if (s != LG_OK) return s;
+    }
+    lg_status s = run_fw_schedule(this, d_S.as<float>(), fw_choice);
+    if (s != LG_OK) return s;
     CK(launch_set_diag(d_S.as<float>(), d_graphs.as<GraphInfo>(), n_graphs, max_n, st), "diagonal");
     return LG_OK;
 }
 
 lg_status Ctx::vertex_light() {
     Ctx* ctx = this;
-    if (!dens.valid) return fail(LG_ERR_STATE, "no density grid uploaded");
+    if (!D().valid) return fail(LG_ERR_STATE, "no density grid uploaded");
     CK(d_L.reserve(sizeof(float) * 3 * std::max<int64_t>(n_points, 1)), "L alloc");
     CK(launch_vertex_light(scene(), d_pts.as<float>(), d_graphs.as<GraphInfo>(), n_graphs, max_n, d_L.as<float>(),
                            st), "vertex light");
@@ -726,10 +832,10 @@ extern "C" double lg_point_voxel_size(int64_t n, const float* pts, int points_pe
 
 lg_status Ctx::splat(double point_voxel_size) {
     Ctx* ctx = this;
-    if (!dens.valid) return fail(LG_ERR_STATE, "no density grid uploaded");
+    if (!D().valid) return fail(LG_ERR_STATE, "no density grid uploaded");
     if (!diffuse_done) return fail(LG_ERR_STATE, "graphs not solved");
     const int f = settings.scatter_grid_res_factor;
-    const lg_grid_desc& dd = dens.desc;
+    const lg_grid_desc& dd = D().desc;
     CoarseGrid cg;
     for (int a = 0; a < 3; ++a) {
         const int lo = floor_div(dd.origin[a], f) - 1;
@@ -739,11 +845,12 @@ lg_status Ctx::splat(double point_voxel_size) {
     }
     cg.H = (float)(dd.voxel_size * f);
     const int64_t ncoarse = (int64_t)cg.dims[0] * cg.dims[1] * cg.dims[2];
-    if (topo_version != dens.version || topo_factor != f) {
+    if (topo_store != &D() || topo_version != D().version || topo_factor != f) {
         CK(d_act0.reserve(ncoarse), "coarse mask alloc");
         CK(d_act.reserve(ncoarse), "coarse mask alloc");
-        CK(launch_coarse_topology(dens.g, f, cg, d_act0.as<uint8_t>(), d_act.as<uint8_t>(), st), "coarse topology");
-        topo_version = dens.version;
+        CK(launch_coarse_topology(D().g, f, cg, d_act0.as<uint8_t>(), d_act.as<uint8_t>(), st), "coarse topology");
+        topo_store = &D();
+        topo_version = D().version;
         topo_factor = f;
     }
     double hp = point_voxel_size;
@@ -771,7 +878,7 @@ lg_status Ctx::splat(double point_voxel_size) {
     double cell = std::max(radius, 1e-12);
     double ext = 0;
     for (int a = 0; a < 3; ++a) ext = std::max(ext, hi[a] - lo[a]);
-    if (ext / cell > 255.0) cell = ext / 255.0;  // at most 256^3 cells
+    if (ext / cell > 159.0) cell = ext / 159.0;  // at most 160^3 cells (16 MB of bins)
     pb.cell = (float)cell;
     pb.n_cells = 1;
     for (int a = 0; a < 3; ++a) {
@@ -839,7 +946,7 @@ lg_status Ctx::render(const lg_camera* c) {
     if (c->width <= 0 || c->height <= 0 || c->samples < 0) return fail(LG_ERR_INVALID, "bad image size or samples");
     if (!(c->focal > 0) || !(c->aperture > 0)) return fail(LG_ERR_INVALID, "bad focal length or aperture");
     if (!(c->znear > 0) || !(c->zfar > c->znear)) return fail(LG_ERR_INVALID, "need 0 < znear < zfar");
-    if (!dens.valid) return fail(LG_ERR_STATE, "no density grid uploaded");
+    if (!D().valid) return fail(LG_ERR_STATE, "no density grid uploaded");
     const int64_t np = (int64_t)c->width * c->height;
     for (DevBuf* b : {&d_rgba, &d_direct, &d_scatter, &d_emission}) CK(b->reserve(sizeof(float4) * np), "film alloc");
     CK(d_counters.reserve(2 * sizeof(unsigned long long)), "counter alloc");
@@ -859,8 +966,36 @@ lg_status Ctx::render(const lg_camera* c) {
     }
     film_w = c->width;
     film_h = c->height;
-    CK(launch_render(scene(), make_camera(*c), sg, d_rgba.as<float4>(), d_direct.as<float4>(),
-                     d_scatter.as<float4>(), d_emission.as<float4>(), d_counters.as<unsigned long long>(), st),
+    const DevScene sc = scene();
+    const DevCamera cam = make_camera(*c);
+    const int64_t n_ps = np * c->samples;
+    const int64_t nps1 = std::max<int64_t>(n_ps, 1);
+    if (n_ps > INT32_MAX) return fail(LG_ERR_INVALID, "too many pixel samples");
+    CK(d_ps_count.reserve(sizeof(int32_t) * nps1), "render alloc");
+    CK(d_ps_offset.reserve(sizeof(int32_t) * nps1), "render alloc");
+    CK(d_ps_scan.reserve(sizeof(int32_t) * (nps1 / 1024 + 2)), "render alloc");
+    CK(d_ps_total.reserve(sizeof(int32_t) * 2), "render alloc");
+    CK(d_ps_data.reserve(pixel_sample_bytes() * nps1), "render alloc");
+    CK(launch_render_count(sc, cam, sg, d_ps_count.as<int32_t>(), st), "render count");
+    CK(launch_exclusive_scan(d_ps_count.as<int32_t>(), n_ps, d_ps_offset.as<int32_t>(), d_ps_scan.as<int32_t>(),
+                             d_ps_total.as<int32_t>(), st), "render scan");
+    if (!capturing) {
+        // size the shadow-task buffer from this frame's count (a captured
+        // replay reuses the capacity of the run it was captured after)
+        int32_t total = 0;
+        CK(cudaMemcpyAsync(&total, d_ps_total.p, sizeof total, cudaMemcpyDeviceToHost, st), "render total");
+        CK(cudaStreamSynchronize(st), "render total sync");
+        if (total < 0) return fail(LG_ERR_INVALID, "more than 2^31 shading samples in one frame");
+        CK(d_tasks.reserve(sizeof(ShadowTask) * std::max<int64_t>(total, 1)), "shadow task alloc");
+        CK(d_task_direct.reserve(sizeof(float4) * std::max<int64_t>(total, 1)), "shadow task alloc");
+    }
+    int sms = 0;
+    CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device), "device query");
+    const int64_t cap = (int64_t)(d_tasks.bytes / sizeof(ShadowTask));
+    CK(launch_render_shade(sc, cam, sg, d_ps_count.as<int32_t>(), d_ps_offset.as<int32_t>(), d_ps_total.as<int32_t>(),
+                           d_tasks.as<ShadowTask>(), cap, d_ps_data.p, d_task_direct.as<float4>(), d_rgba.as<float4>(),
+                           d_direct.as<float4>(), d_scatter.as<float4>(), d_emission.as<float4>(),
+                           d_counters.as<unsigned long long>(), sms, st),
        "render");
     return LG_OK;
 }
@@ -882,6 +1017,13 @@ extern "C" lg_status lg_render(lg_ctx* handle, const lg_camera* camera, float* r
     GUARD(ctx);
     lg_status s = ctx->render(camera);
     if (s != LG_OK) return s;
+    return ctx->download_films(rgba, direct, scatter, emission);
+}
+
+extern "C" lg_status lg_get_films(lg_ctx* handle, float* rgba, float* direct, float* scatter, float* emission) {
+    Ctx* ctx = reinterpret_cast<Ctx*>(handle);
+    GUARD(ctx);
+    if (ctx->film_w == 0) return ctx->fail(LG_ERR_STATE, "nothing rendered yet");
     return ctx->download_films(rgba, direct, scatter, emission);
 }
 
@@ -920,23 +1062,104 @@ extern "C" lg_status lg_frame_device(lg_ctx* handle, int max_connect, double poi
     if (ctx->n_graphs == 0) return ctx->fail(LG_ERR_STATE, "no graphs loaded");
     if (max_connect < 0 || max_connect > 255) return ctx->fail(LG_ERR_INVALID, "bad max_connect");
     if (max_connect != ctx->max_connect) return ctx->fail(LG_ERR_INVALID, "max_connect differs from the loaded graphs");
-    ctx->mark(0);
-    lg_status s = ctx->build_edges();
-    ctx->mark(1);
-    if (s == LG_OK) s = ctx->march_edges();
-    ctx->mark(2);
-    if (s == LG_OK) { s = ctx->solve_paths(); ctx->paths_solved = s == LG_OK; }
-    ctx->mark(3);
-    if (s == LG_OK) { s = ctx->vertex_light(); ctx->light_done = s == LG_OK; }
-    ctx->mark(4);
-    if (s == LG_OK) { s = ctx->diffuse(); ctx->diffuse_done = s == LG_OK; }
-    ctx->mark(5);
-    if (s == LG_OK) s = ctx->splat(point_voxel_size);
-    ctx->mark(6);
-    if (s == LG_OK) s = ctx->render(camera);
-    ctx->mark(7);
-    ctx->ev_recorded = ctx->profiling && s == LG_OK;
+    if (!camera) return ctx->fail(LG_ERR_INVALID, "null camera");
+    if (!ctx->graph_mode) return ctx->frame_enqueue(point_voxel_size, camera);
+    if (ctx->graph_valid && ctx->graph_epoch == g_alloc_epoch && ctx->graph_pvs == point_voxel_size &&
+        std::memcmp(&ctx->graph_cam, camera, sizeof(lg_camera)) == 0) {
+        CK(cudaGraphLaunch(ctx->graph_exec, ctx->st), "frame graph launch");
+        ++g_launch_counter;
+        ctx->ev_recorded = ctx->profiling;
+        return LG_OK;
+    }
+    // run the frame once (this also tunes and allocates), then capture the
+    // same launch sequence for replay
+    lg_status s = ctx->frame_enqueue(point_voxel_size, camera);
+    if (s != LG_OK) return s;
+    CK(cudaStreamSynchronize(ctx->st), "sync");
+    if (ctx->graph_exec) { cudaGraphExecDestroy(ctx->graph_exec); ctx->graph_exec = nullptr; }
+    if (ctx->graph) { cudaGraphDestroy(ctx->graph); ctx->graph = nullptr; }
+    const uint64_t launches = g_launch_counter;
+    CK(cudaStreamBeginCapture(ctx->st, cudaStreamCaptureModeThreadLocal), "begin capture");
+    ctx->capturing = true;
+    s = ctx->frame_enqueue(point_voxel_size, camera);
+    ctx->capturing = false;
+    cudaGraph_t graph = nullptr;
+    const cudaError_t ce = cudaStreamEndCapture(ctx->st, &graph);
+    const uint64_t captured = g_launch_counter - launches;
+    g_launch_counter = launches;  // captured, not launched
+    if (s != LG_OK) { if (graph) cudaGraphDestroy(graph); return s; }
+    CK(ce, "end capture");
+    ctx->graph = graph;
+    CK(cudaGraphInstantiate(&ctx->graph_exec, graph, 0), "graph instantiate");
+    ctx->graph_valid = true;
+    ctx->graph_epoch = g_alloc_epoch;
+    ctx->graph_cam = *camera;
+    ctx->graph_pvs = point_voxel_size;
+    ctx->frame_launches = captured;
+    return LG_OK;
+}
+
+lg_status Ctx::frame_enqueue(double point_voxel_size, const lg_camera* camera) {
+    frame_launch_base = g_launch_counter;
+    mark(0);
+    lg_status s = build_edges();
+    mark(1);
+    if (s == LG_OK) s = march_edges();
+    mark(2);
+    if (s == LG_OK) { s = solve_paths(); paths_solved = s == LG_OK; }
+    mark(3);
+    if (s == LG_OK) { s = vertex_light(); light_done = s == LG_OK; }
+    mark(4);
+    if (s == LG_OK) { s = diffuse(); diffuse_done = s == LG_OK; }
+    mark(5);
+    if (s == LG_OK) s = splat(point_voxel_size);
+    mark(6);
+    if (s == LG_OK) s = render(camera);
+    mark(7);
+    ev_recorded = profiling && s == LG_OK;
     return s;
+}
+
+extern "C" lg_status lg_set_graph_mode(lg_ctx* handle, int on) {
+    Ctx* ctx = reinterpret_cast<Ctx*>(handle);
+    GUARD(ctx);
+    ctx->graph_mode = on != 0;
+    ctx->graph_valid = false;
+    return LG_OK;
+}
+
+extern "C" lg_status lg_set_fw_schedule(lg_ctx* handle, int schedule) {
+    Ctx* ctx = reinterpret_cast<Ctx*>(handle);
+    GUARD(ctx);
+    if (schedule < -1 || schedule > 2) return ctx->fail(LG_ERR_INVALID, "schedule must be -1, 0, 1 or 2");
+    if (schedule == -1) {
+        ctx->fw_choice = -1;
+        for (auto& kv : ctx->fw_tuned)
+            if (kv.first == std::make_pair(ctx->n_graphs, ctx->max_n)) ctx->fw_choice = kv.second;
+    } else {
+        ctx->fw_choice = schedule;
+    }
+    ctx->graph_valid = false;
+    return LG_OK;
+}
+
+extern "C" lg_status lg_fw_schedule(lg_ctx* handle, int* schedule, double* tuned_ms, int n) {
+    Ctx* ctx = reinterpret_cast<Ctx*>(handle);
+    GUARD(ctx);
+    if (schedule) *schedule = ctx->fw_choice;
+    for (int k = 0; tuned_ms && k < n && k < 4; ++k) tuned_ms[k] = ctx->fw_tune_ms[k];
+    if (ctx->fw_choice > 0 && ctx->d_fw_sync.bytes >= 8) {
+        uint32_t flags[2] = {0, 0};
+        CK(cudaMemcpyAsync(flags, ctx->d_fw_sync.p, sizeof flags, cudaMemcpyDeviceToHost, ctx->st), "flag read");
+        CK(cudaStreamSynchronize(ctx->st), "sync");
+        if (flags[1] != 0) return ctx->fail(LG_ERR_TIMEOUT, "batched floyd-warshall: a dependency wait timed out");
+    }
+    return LG_OK;
+}
+
+extern "C" uint64_t lg_frame_launches(const lg_ctx* handle) {
+    const Ctx* ctx = reinterpret_cast<const Ctx*>(handle);
+    return ctx ? ctx->frame_launches : 0;
 }
 
 extern "C" lg_status lg_set_profiling(lg_ctx* handle, int on) {
@@ -946,6 +1169,7 @@ extern "C" lg_status lg_set_profiling(lg_ctx* handle, int on) {
         for (int k = 0; k <= Ctx::kStages; ++k) CK(cudaEventCreate(&ctx->ev[k]), "event create");
     }
     ctx->profiling = on != 0;
+    ctx->graph_valid = false;
     ctx->ev_recorded = false;
     return LG_OK;
 }

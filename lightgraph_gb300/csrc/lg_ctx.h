@@ -12,6 +12,10 @@
 
 namespace lg {
 
+// Bumped whenever any DevBuf is reallocated: a captured frame graph is only
+// replayed while its buffers are the ones it was captured with.
+extern uint64_t g_alloc_epoch;
+
 // Grow-only device allocation.
 struct DevBuf {
     void* p = nullptr;
@@ -23,6 +27,7 @@ struct DevBuf {
     cudaError_t reserve(size_t b) {
         if (b <= bytes) return cudaSuccess;
         release();
+        ++g_alloc_epoch;
         const cudaError_t e = cudaMalloc(&p, b);
         if (e != cudaSuccess) {
             p = nullptr;
@@ -57,8 +62,14 @@ struct Ctx {
     std::string err;
     cudaGraphExec_t graph_exec = nullptr;
 
-    // grids
+    // grids: owned (uploaded through this context) or bound to a resident
+    // volume shared by several contexts (the serving slots)
     GridStore dens, temp;
+    const GridStore* dens_ext = nullptr;
+    const GridStore* temp_ext = nullptr;
+    bool temp_ext_set = false;
+    const GridStore& D() const { return dens_ext ? *dens_ext : dens; }
+    const GridStore& T() const { return temp_ext_set ? *temp_ext : temp; }
     DevBuf staging, mask_staging, small;
 
     // scene
@@ -82,16 +93,42 @@ struct Ctx {
     DevBuf d_pts, d_graphs, d_pt_graph, d_cand, d_cand_cnt, d_edges, d_edge_cnt, d_adj, d_adj_off;
     DevBuf d_S, d_L, d_D, d_part, d_colw, d_fw;
 
+    // batched Floyd-Warshall: work queue, counters and the autotuned schedule
+    DevBuf d_fwg, d_fw_items, d_fw_sync, d_fw_tune;
+    int fw_items_n = 0;
+    bool fw_queue_valid = false;
+    // schedule per (graph count, largest n): 0 = per-graph launches,
+    // k > 0 = persistent with k CTAs per SM
+    std::vector<std::pair<std::pair<int, int>, int>> fw_tuned;
+    int fw_choice = -1;
+    double fw_tune_ms[4] = {0, 0, 0, 0};
+
+    // frame replay through a captured CUDA graph
+    bool graph_mode = false;
+    bool graph_valid = false;
+    cudaGraph_t graph = nullptr;
+    lg_camera graph_cam{};
+    double graph_pvs = 0.0;
+    uint64_t graph_epoch = 0;
+    uint64_t frame_launch_base = 0, frame_launches = 0;  // kernels in one frame
+    void invalidate_graph() { graph_valid = false; }
+    lg_status frame_enqueue(double point_voxel_size, const lg_camera* camera);
+    lg_status solve_paths_batched(int choice);
+    lg_status tune_fw();
+
     // scatter grid
     CoarseGrid coarse{};
     int topo_version = -1, topo_factor = -1;
+    const GridStore* topo_store = nullptr;
     bool splat_done = false;
     double splat_radius = 0.0;
     DevBuf d_act0, d_act, d_sg, d_cell_count, d_cell_start, d_cursor, d_sorted, d_scan_tmp;
 
-    // films
+    // films and the render waves' buffers
     int film_w = 0, film_h = 0;
     DevBuf d_rgba, d_direct, d_scatter, d_emission, d_counters;
+    DevBuf d_ps_count, d_ps_offset, d_ps_scan, d_ps_total, d_ps_data, d_tasks, d_task_direct;
+    bool capturing = false;  // inside a CUDA graph capture: no host syncs
 
     // stage timing: events recorded on the stream around each stage of a frame
     static constexpr int kStages = 7;  // build, march, fw, light, diffuse, splat, render

@@ -149,14 +149,37 @@ __device__ __forceinline__ bool clip_to_bbox(const DevGrid& g, IRay& r) {
     return true;
 }
 
+// Per-axis state is kept in scalars (no runtime-indexed arrays), so the
+// walker lives in registers.
 struct LeafDDA {
     float t, tmax;
-    float next[3], delta[3];
-    int cell[3], step[3];
-    bool open;     // a span has started
-    float start;   // its start time
+    float nx, ny, nz;   // next crossing time per axis
+    float dx, dy, dz;   // crossing interval per axis
+    int cx, cy, cz;     // current leaf cell
+    int sx, sy, sz;     // cell step per axis
+    bool open;          // a span has started
+    float start;        // its start time
     bool done;
 };
+
+__device__ __forceinline__ void dda_axis(float e, float d, float inv, float t0, int& c, int& step, float& next,
+                                         float& delta) {
+    const float p = e + t0 * d;
+    c = ((int)floorf(p)) >> 3;
+    if (d == 0.f) {
+        step = 0;
+        next = kInf;
+        delta = kInf;
+    } else if (inv > 0.f) {
+        step = 1;
+        next = t0 + ((float)(c * 8 + 8) - p) * inv;
+        delta = 8.f * inv;
+    } else {
+        step = -1;
+        next = t0 + ((float)(c * 8) - p) * inv;
+        delta = -8.f * inv;
+    }
+}
 
 __device__ __forceinline__ void dda_init(LeafDDA& s, const IRay& r) {
     s.t = r.t0;
@@ -164,44 +187,30 @@ __device__ __forceinline__ void dda_init(LeafDDA& s, const IRay& r) {
     s.open = false;
     s.start = 0.f;
     s.done = false;
-#pragma unroll
-    for (int i = 0; i < 3; ++i) {
-        const float p = r.e[i] + r.t0 * r.d[i];
-        const int c = ((int)floorf(p)) >> 3;
-        s.cell[i] = c;
-        if (r.d[i] == 0.f) {
-            s.step[i] = 0;
-            s.next[i] = kInf;
-            s.delta[i] = kInf;
-        } else if (r.inv[i] > 0.f) {
-            s.step[i] = 1;
-            s.next[i] = r.t0 + ((float)(c * 8 + 8) - p) * r.inv[i];
-            s.delta[i] = 8.f * r.inv[i];
-        } else {
-            s.step[i] = -1;
-            s.next[i] = r.t0 + ((float)(c * 8) - p) * r.inv[i];
-            s.delta[i] = -8.f * r.inv[i];
-        }
-    }
+    dda_axis(r.e[0], r.d[0], r.inv[0], r.t0, s.cx, s.sx, s.nx, s.dx);
+    dda_axis(r.e[1], r.d[1], r.inv[1], r.t0, s.cy, s.sy, s.ny, s.dy);
+    dda_axis(r.e[2], r.d[2], r.inv[2], r.t0, s.cz, s.sz, s.nz, s.dz);
 }
 
 // Next span [ta, tb] of consecutive leaf cells with tb - ta > kDelta.
 __device__ __forceinline__ bool next_span(const DevGrid& g, LeafDDA& s, float& ta, float& tb) {
     while (!s.done) {
-        const bool leaf = is_leaf(g, s.cell[0], s.cell[1], s.cell[2]);
+        const bool leaf = is_leaf(g, s.cx, s.cy, s.cz);
         if (leaf) {
             if (!s.open) { s.open = true; s.start = s.t; }
         } else if (s.open) {
             s.open = false;
             if (s.t - s.start > kDelta) { ta = s.start; tb = s.t; return true; }
         }
-        // step to the next cell (math::MinIndex tie order)
-        int a;
-        if (s.next[0] < s.next[1]) a = (s.next[0] < s.next[2]) ? 0 : 2;
-        else a = (s.next[1] < s.next[2]) ? 1 : 2;
-        s.t = s.next[a];
-        s.next[a] += s.delta[a];
-        s.cell[a] += s.step[a];
+        // step to the next cell (math::MinIndex tie order: x if strictly
+        // smallest, else y if below z, else z)
+        const bool ax = (s.nx < s.ny) && (s.nx < s.nz);
+        const bool ay = !(s.nx < s.ny) && (s.ny < s.nz);
+        const bool az = !ax && !ay;
+        s.t = ax ? s.nx : (ay ? s.ny : s.nz);
+        if (ax) { s.nx += s.dx; s.cx += s.sx; }
+        if (ay) { s.ny += s.dy; s.cy += s.sy; }
+        if (az) { s.nz += s.dz; s.cz += s.sz; }
         if (!(s.t <= s.tmax)) {
             s.done = true;
             if (s.open && s.tmax - s.start > kDelta) { ta = s.start; tb = s.tmax; return true; }

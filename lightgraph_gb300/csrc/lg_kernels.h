@@ -40,9 +40,20 @@ cudaError_t launch_vertex_light(const DevScene& sc, const float* pts, const Grap
 
 // Floyd-Warshall on one matrix (general, any n, ld % 4 == 0).
 cudaError_t fw_solve(float* d, int n, int ld, cudaStream_t st);
-// Batched: every graph's matrix in one set of launches.
-cudaError_t fw_solve_batched(float* base, const int64_t* offs, const int32_t* ns,
-                             const int32_t* lds, int n_graphs, int max_n, cudaStream_t st);
+
+// Batched: many matrices in one persistent launch.
+struct FwGraph {
+    int64_t off;  // first float of the matrix
+    int32_t n, ld;
+    int32_t nt;   // k-blocks of 64
+    int32_t nu;   // update tiles of 128 per side
+};
+// Writes the work queue (if items != null) and returns its length.
+size_t fw_batched_items(const FwGraph* graphs, int n_graphs, int4* items);
+// sync: 2 + 2 * n_graphs uint32 (cleared here). ctas: persistent CTAs.
+cudaError_t fw_solve_batched(float* base, const FwGraph* graphs, const int4* items, int n_items, uint32_t* sync,
+                             int n_graphs, int ctas, cudaStream_t st);
+int fw_persistent_ctas_per_sm();
 cudaError_t launch_set_diag(float* S, const GraphInfo* graphs, int n_graphs, int max_n,
                             cudaStream_t st);
 
@@ -88,9 +99,28 @@ struct DevScatterGrid {
     int lo[3], dims[3];
     float inv_H;
 };
-cudaError_t launch_render(const DevScene& sc, const DevCamera& cam, const DevScatterGrid& sg,
-                          float4* rgba, float4* direct, float4* scatter, float4* emission,
-                          unsigned long long* counters, cudaStream_t st);
+// One shading sample of a primary ray: where its shadow rays start and the
+// weight pTrans * (1 - dT) of their contribution.
+struct ShadowTask {
+    float p[3];    // index-space position
+    float w[3];    // pTrans * (1 - dT) per channel
+    uint32_t n;    // primary loop iteration (keys the shadow random streams)
+    uint32_t ps;   // pixel * spp + sample
+};
+static_assert(sizeof(ShadowTask) == 32, "ShadowTask is two 16-byte words");
+size_t pixel_sample_bytes();
+// Wave 1: counts[ps] = shading samples of each pixel-sample.
+cudaError_t launch_render_count(const DevScene& sc, const DevCamera& cam, const DevScatterGrid& sg, int32_t* counts,
+                                cudaStream_t st);
+// Waves 2-4 given the exclusive scan of the counts (offsets, device total).
+cudaError_t launch_render_shade(const DevScene& sc, const DevCamera& cam, const DevScatterGrid& sg,
+                                const int32_t* counts, const int32_t* offsets, const int32_t* total,
+                                ShadowTask* tasks, int64_t task_cap, void* pixel_samples, float4* direct,
+                                float4* rgba, float4* dfilm, float4* sfilm, float4* efilm,
+                                unsigned long long* counters, int sms, cudaStream_t st);
+// Exclusive scan of n int32 (block_sums: n/1024 + 1 ints); *total = sum.
+cudaError_t launch_exclusive_scan(const int32_t* in, int64_t n, int32_t* out, int32_t* block_sums, int32_t* total,
+                                  cudaStream_t st);
 
 // Environment map CDFs (FP64 prefix sums)
 cudaError_t launch_env_cdf(const float* rgb, int w, int h, float* cond_func, float* cond_cdf,

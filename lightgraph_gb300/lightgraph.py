@@ -381,6 +381,26 @@ class Context:
         cam = opts.camera_c()
         self._ck(self.lib.lg_frame_device(self.h, max_connect, point_voxel_size, C.byref(cam)))
 
+    def set_fw_schedule(self, schedule: int) -> None:
+        """-1 autotuned, 0 per-graph launches, 1/2 persistent (CTAs per SM)."""
+        self._ck(self.lib.lg_set_fw_schedule(self.h, schedule))
+
+    def fw_schedule(self):
+        s = C.c_int()
+        ms = (C.c_double * 3)()
+        self._ck(self.lib.lg_fw_schedule(self.h, C.byref(s), ms, 3))
+        return s.value, list(ms)
+
+    def set_graph_mode(self, on: bool) -> None:
+        self._ck(self.lib.lg_set_graph_mode(self.h, 1 if on else 0))
+
+    def films(self, opts: SceneSettings) -> Films:
+        """The films of the last render or frame_device (waits for it)."""
+        shape = (opts.height, opts.width, 4)
+        films = [np.empty(shape, np.float32) for _ in range(4)]
+        self._ck(self.lib.lg_get_films(self.h, *[ptr(f) for f in films]))
+        return Films(*films)
+
     def fw_host(self, S: np.ndarray) -> np.ndarray:
         out = np.ascontiguousarray(S, dtype=np.float32).copy()
         self._ck(self.lib.lg_fw_host(self.h, ptr(out), out.shape[0]))

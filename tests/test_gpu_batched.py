@@ -1,0 +1,92 @@
+"""Many graphs of uneven size: the persistent batched Floyd-Warshall, its
+autotuner, and frame replay through a captured CUDA graph."""
+import numpy as np
+import pytest
+
+from lightgraph_gb300 import scenes
+from oracle import pyoracle as po
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def uneven_graphs():
+    """12 graphs, sizes log-uniform in [20, 700] (seed 3), points inside the
+    small scene's volume, connection radius 0.15."""
+    sc = scenes.small(n_points=16, width=32, height=32)
+    rng = np.random.default_rng(3)
+    sizes = np.exp(rng.uniform(np.log(20), np.log(700), 12)).astype(int)
+    pts = [scenes.points(sc.density.values, sc.density.voxel_size, int(n), seed=100 + g)
+           for g, n in enumerate(sizes)]
+    sc.points = pts
+    sc.radius = [0.15] * len(pts)
+    sc.opts.iter = len(pts)
+    return sc
+
+
+def solve_with(ctx, sc, schedule):
+    scenes.load_into(ctx, sc)
+    ctx.build_graphs(sc.points, sc.radius_sq, sc.max_connect)
+    S = ctx.march_edges(want=True)
+    ctx.set_fw_schedule(schedule)
+    dist = ctx.solve_paths(want=True)
+    used, ms = ctx.fw_schedule()
+    return S, dist, used, ms
+
+
+def test_schedules_bit_identical_and_match_oracle(gpu_ctx, uneven_graphs):
+    sc = uneven_graphs
+    S0, d0, u0, _ = solve_with(gpu_ctx, sc, 0)
+    _, d1, u1, _ = solve_with(gpu_ctx, sc, 1)
+    _, d2, u2, _ = solve_with(gpu_ctx, sc, 2)
+    assert (u0, u1, u2) == (0, 1, 2)
+    for g in range(len(sc.points)):
+        assert np.array_equal(d0[g], d1[g]), g
+        assert np.array_equal(d0[g], d2[g]), g
+        ref = po.fw_minplus_f32(S0[g])
+        np.fill_diagonal(ref, 0.0)
+        fin = np.isfinite(ref)
+        assert np.array_equal(np.isfinite(d1[g]), fin)
+        assert np.allclose(d1[g][fin], ref[fin], rtol=1e-6, atol=0), g
+
+
+def test_autotuner_picks_a_schedule(gpu_ctx, uneven_graphs):
+    S, d, used, ms = solve_with(gpu_ctx, uneven_graphs, -1)
+    assert used in (0, 1, 2)
+    assert ms[0] > 0 and ms[1] > 0
+    _, d0, _, _ = solve_with(gpu_ctx, uneven_graphs, 0)
+    for g in range(len(d)):
+        assert np.array_equal(d[g], d0[g])
+
+
+def test_many_graphs_full_frame(gpu_ctx, uneven_graphs):
+    """The multi-iteration frame (iter = 12 graphs into one splat) renders and
+    is identical whichever Floyd-Warshall schedule runs."""
+    sc = uneven_graphs
+    out = []
+    for schedule in (0, 1):
+        scenes.load_into(gpu_ctx, sc)
+        gpu_ctx.build_graphs(sc.points, sc.radius_sq, sc.max_connect)
+        gpu_ctx.set_fw_schedule(schedule)
+        gpu_ctx.frame_device(sc.opts, sc.max_connect)
+        out.append(gpu_ctx.films(sc.opts))
+    for k in ["rgba", "direct", "scatter", "emission"]:
+        assert np.array_equal(getattr(out[0], k), getattr(out[1], k))
+    assert np.isfinite(out[0].rgba).all()
+
+
+def test_graph_replay_matches_direct_launches(gpu_ctx):
+    sc = scenes.small(n_points=300, width=48, height=40, spp=2)
+    scenes.load_into(gpu_ctx, sc)
+    gpu_ctx.build_graphs(sc.points, sc.radius_sq, sc.max_connect)
+    gpu_ctx.set_graph_mode(False)
+    gpu_ctx.frame_device(sc.opts, sc.max_connect)
+    ref = gpu_ctx.films(sc.opts)
+    gpu_ctx.set_graph_mode(True)
+    for _ in range(3):  # run + capture, then two replays
+        gpu_ctx.frame_device(sc.opts, sc.max_connect)
+        got = gpu_ctx.films(sc.opts)
+        for k in ["rgba", "direct", "scatter", "emission"]:
+            assert np.array_equal(getattr(got, k), getattr(ref, k)), k
+    assert gpu_ctx.lib.lg_frame_launches(gpu_ctx.h) > 10
+    gpu_ctx.set_graph_mode(False)
