@@ -49,7 +49,38 @@ def parse():
     ap.add_argument("--small", action="store_true", help="the 128^3 / 1024-point / 256^2 case instead")
     ap.add_argument("--image", type=int, default=0, help="override the square image size (profiling runs)")
     ap.add_argument("--spp", type=int, default=0, help="override the samples per pixel (profiling runs)")
+    ap.add_argument("--serving", type=int, default=24, help="requests in the serving measurement (0: skip)")
+    ap.add_argument("--rate", type=float, default=50.0, help="Poisson arrival rate of the serving stream (req/s)")
     return ap.parse_args()
+
+
+def run_serving(n: int, rate: float):
+    """The mixed request stream (4 resident volumes 64^3..512^3, 512..8192
+    points, 128^2..1024^2 at 1-4 spp, 1-3 lights, Poisson arrivals, seed 4)
+    served one request at a time and with continuous batching (4 slots)."""
+    from lightgraph_gb300 import serve
+    out = {"stream": f"{n} requests, Poisson {rate} req/s, seed 4, volumes 64^3-512^3, 512-8192 points, "
+                     "128^2-1024^2 at 1-4 spp, 1-3 lights"}
+    vs = serve.make_volumes(None)
+    # single-request latency: each request alone on an idle server
+    for label, slots, realtime in (("alone", 1, False), ("plain", 1, True), ("batched", 4, True)):
+        srv = serve.Server(max_inflight=slots)
+        vs.ids = [srv.add_volume(g) for g in vs.grids]
+        stream = serve.request_stream(vs, n, rate, seed=4)
+        if label == "alone":
+            lat = []
+            for _, req in stream:
+                _, _, l = srv.wait(srv.submit(req), -1, False)
+                lat.append(l / 1e3)
+            out["alone_p50_ms"] = float(np.percentile(lat, 50))
+            out["alone_p99_ms"] = float(np.percentile(lat, 99))
+        else:
+            stats, _ = serve.run_stream(srv, stream, want_images=False, realtime=realtime)
+            out[label] = stats
+        srv.close()
+    out["batched_over_plain_renders_per_s"] = out["batched"]["renders_per_s"] / out["plain"]["renders_per_s"]
+    out["batched_p99_over_alone_p99"] = out["batched"]["p99_ms"] / out["alone_p99_ms"]
+    return out
 
 
 def dist_env():
@@ -362,6 +393,8 @@ def run_ours(args):
                         "peak_kind": "nominal (152 SMs x 128 lanes x 2 x 2.07 GHz)",
                         "frac": fw_tflops / NOMINAL_FP32_TFLOPS},
     }
+    if rank == 0 and args.serving > 0:
+        line["serving"] = run_serving(args.serving, args.rate)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         fw_rounds, stride = (128, 64) if not args.small else (256, 16)
         v, det, sample, threads = cpu_sample(sc, fw_rounds, stride)

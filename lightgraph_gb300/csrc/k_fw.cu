@@ -74,10 +74,21 @@ __device__ __forceinline__ float ld_or_inf(const float* d, int n, int ld, int i,
 struct PanelSmem {
     float Dg[kKB][kKB + 1];
     float T[kKB][kKB + 1];
+    float rowk[2][kKB];  // row k / column k of the diagonal tile, double buffered
+    float colk[2][kKB];
 };
 
 // Panel tile b of round kb: 0 = diagonal, 1..nt-1 = row panel, nt..2nt-2 =
-// column panel (the diagonal's index skipped). 256 threads.
+// column panel (the diagonal's index skipped). 256 threads, each owning the
+// 4x4 elements (ty + 16r, tx + 16c).
+//   1. The diagonal tile Dg is closed by 64 FW steps held in registers; step k
+//      only needs row k and column k, which do not change in step k, so their
+//      owners publish them to shared memory (double buffered, one barrier per
+//      step).
+//   2. With Dg* closed, the row panel is min(T, Dg* (x) T) and the column panel
+//      min(T, T (x) Dg*): every path that leaves the k-block for the last time
+//      at k' costs Dg*[k][k'] + T[k'][j], so one min-plus product (no per-k
+//      barrier) replaces the 64 sequential panel steps.
 template <bool kL2>
 __device__ __forceinline__ void fw_panel_tile(float* __restrict__ d, int n, int ld, int kb, int b, PanelSmem& sm) {
     const int nt = (n + kKB - 1) / kKB;
@@ -91,55 +102,116 @@ __device__ __forceinline__ void fw_panel_tile(float* __restrict__ d, int n, int 
         other = q < kb ? q : q + 1;
     }
     const int O0 = other * kKB;
-    for (int e = tid; e < kKB * kKB; e += 256) {
-        const int r = e >> 6, c = e & 63;
-        sm.Dg[r][c] = ld_or_inf<kL2>(d, n, ld, K0 + r, K0 + c);
-        if (kind == 1) sm.T[r][c] = ld_or_inf<kL2>(d, n, ld, K0 + r, O0 + c);
-        if (kind == 2) sm.T[r][c] = ld_or_inf<kL2>(d, n, ld, O0 + r, K0 + c);
+    float g[4][4];
+#pragma unroll
+    for (int r = 0; r < 4; ++r)
+#pragma unroll
+        for (int c = 0; c < 4; ++c) g[r][c] = ld_or_inf<kL2>(d, n, ld, K0 + ty + 16 * r, K0 + tx + 16 * c);
+    if (kind != 0) {
+        for (int e = tid; e < kKB * kKB; e += 256) {
+            const int r = e >> 6, c = e & 63;
+            sm.T[r][c] = kind == 1 ? ld_or_inf<kL2>(d, n, ld, K0 + r, O0 + c) : ld_or_inf<kL2>(d, n, ld, O0 + r, K0 + c);
+        }
     }
+    // publish row 0 and column 0 (owners: ty == 0 row, tx == 0 column)
+#pragma unroll
+    for (int c = 0; c < 4; ++c)
+        if (ty == 0) sm.rowk[0][tx + 16 * c] = g[0][c];
+#pragma unroll
+    for (int r = 0; r < 4; ++r)
+        if (tx == 0) sm.colk[0][ty + 16 * r] = g[r][0];
     __syncthreads();
-    // phase 1: close the diagonal tile
+    // 1. close the diagonal tile in registers
     for (int k = 0; k < kKB; ++k) {
+        const int buf = k & 1;
+        float rk[4], ck[4];
 #pragma unroll
-        for (int r = 0; r < 4; ++r) {
-            const int i = ty + 16 * r;
-            const float dik = sm.Dg[i][k];
+        for (int c = 0; c < 4; ++c) rk[c] = sm.rowk[buf][tx + 16 * c];
 #pragma unroll
-            for (int c = 0; c < 4; ++c) {
-                const int j = tx + 16 * c;
-                const float v = dik + sm.Dg[k][j];
-                if (v < sm.Dg[i][j]) sm.Dg[i][j] = v;
+        for (int r = 0; r < 4; ++r) ck[r] = sm.colk[buf][ty + 16 * r];
+#pragma unroll
+        for (int r = 0; r < 4; ++r)
+#pragma unroll
+            for (int c = 0; c < 4; ++c) g[r][c] = fminf(g[r][c], ck[r] + rk[c]);
+        const int k1 = k + 1;
+        if (k1 < kKB) {
+            // owners of row k+1 and column k+1 publish them for the next step
+            if ((k1 & 15) == ty) {
+#pragma unroll
+                for (int r = 0; r < 4; ++r)
+                    if (ty + 16 * r == k1) {
+#pragma unroll
+                        for (int c = 0; c < 4; ++c) sm.rowk[buf ^ 1][tx + 16 * c] = g[r][c];
+                    }
+            }
+            if ((k1 & 15) == tx) {
+#pragma unroll
+                for (int c = 0; c < 4; ++c)
+                    if (tx + 16 * c == k1) {
+#pragma unroll
+                        for (int r = 0; r < 4; ++r) sm.colk[buf ^ 1][ty + 16 * r] = g[r][c];
+                    }
             }
         }
         __syncthreads();
     }
     if (kind == 0) {
-        for (int e = tid; e < kKB * kKB; e += 256) {
-            const int r = e >> 6, c = e & 63;
-            if (K0 + r < n && K0 + c < n) d[(int64_t)(K0 + r) * ld + K0 + c] = sm.Dg[r][c];
-        }
-        return;
-    }
-    // phase 2: close one panel tile through the k-block
-    for (int k = 0; k < kKB; ++k) {
 #pragma unroll
-        for (int r = 0; r < 4; ++r) {
-            const int i = ty + 16 * r;
+        for (int r = 0; r < 4; ++r)
 #pragma unroll
             for (int c = 0; c < 4; ++c) {
-                const int j = tx + 16 * c;
-                const float v = (kind == 1) ? sm.Dg[i][k] + sm.T[k][j] : sm.T[i][k] + sm.Dg[k][j];
-                if (v < sm.T[i][j]) sm.T[i][j] = v;
+                const int gi = K0 + ty + 16 * r, gj = K0 + tx + 16 * c;
+                if (gi < n && gj < n) d[(int64_t)gi * ld + gj] = g[r][c];
             }
+        return;
+    }
+#pragma unroll
+    for (int r = 0; r < 4; ++r)
+#pragma unroll
+        for (int c = 0; c < 4; ++c) sm.Dg[ty + 16 * r][tx + 16 * c] = g[r][c];
+    __syncthreads();
+    // 2. one min-plus product against the closed diagonal tile
+    float acc[4][4];
+#pragma unroll
+    for (int r = 0; r < 4; ++r)
+#pragma unroll
+        for (int c = 0; c < 4; ++c) acc[r][c] = sm.T[ty + 16 * r][tx + 16 * c];
+    if (kind == 1) {
+#pragma unroll 4
+        for (int k = 0; k < kKB; ++k) {
+            float a[4], bb[4];
+#pragma unroll
+            for (int r = 0; r < 4; ++r) a[r] = sm.Dg[ty + 16 * r][k];
+#pragma unroll
+            for (int c = 0; c < 4; ++c) bb[c] = sm.T[k][tx + 16 * c];
+#pragma unroll
+            for (int r = 0; r < 4; ++r)
+#pragma unroll
+                for (int c = 0; c < 4; ++c) acc[r][c] = fminf(acc[r][c], a[r] + bb[c]);
         }
-        __syncthreads();
+    } else {
+#pragma unroll 4
+        for (int k = 0; k < kKB; ++k) {
+            float a[4], bb[4];
+#pragma unroll
+            for (int r = 0; r < 4; ++r) a[r] = sm.T[ty + 16 * r][k];
+#pragma unroll
+            for (int c = 0; c < 4; ++c) bb[c] = sm.Dg[k][tx + 16 * c];
+#pragma unroll
+            for (int r = 0; r < 4; ++r)
+#pragma unroll
+                for (int c = 0; c < 4; ++c) acc[r][c] = fminf(acc[r][c], a[r] + bb[c]);
+        }
     }
-    for (int e = tid; e < kKB * kKB; e += 256) {
-        const int r = e >> 6, c = e & 63;
-        const int gi = kind == 1 ? K0 + r : O0 + r;
-        const int gj = kind == 1 ? O0 + c : K0 + c;
-        if (gi < n && gj < n) d[(int64_t)gi * ld + gj] = sm.T[r][c];
-    }
+#pragma unroll
+    for (int r = 0; r < 4; ++r)
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+            const int i = ty + 16 * r, j = tx + 16 * c;
+            const int gi = kind == 1 ? K0 + i : O0 + i;
+            const int gj = kind == 1 ? O0 + j : K0 + j;
+            if (gi < n && gj < n) d[(int64_t)gi * ld + gj] = acc[r][c];
+        }
 }
 
 // Update tile (ti, tj) of round kb, 128x128. 256 threads = 8 warps (4 x 2),

@@ -1,0 +1,80 @@
+"""Serving: resident volumes, HBM-budget admission, concurrent requests.
+A request's image must be the same alone and in the mix."""
+import numpy as np
+import pytest
+
+from lightgraph_gb300 import LightGraphError, _capi
+from lightgraph_gb300 import serve
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def small_stream():
+    vs = serve.make_volumes(None, resolutions=(32, 64), pool=1500)
+    return vs
+
+
+def test_mixed_equals_alone(small_stream):
+    vs = small_stream
+    alone_srv = serve.Server(max_inflight=1)
+    mix_srv = serve.Server(max_inflight=4)
+    try:
+        for srv in (alone_srv, mix_srv):
+            vs.ids = [srv.add_volume(g) for g in vs.grids]
+            stream = serve.request_stream(vs, 8, rate=0, seed=4, n_min=64, n_max=600, images=(32, 48, 64))
+            stats, imgs = serve.run_stream(srv, stream, want_images=True, realtime=False)
+            assert stats["requests"] == 8
+            if srv is alone_srv:
+                alone = imgs
+            else:
+                mixed = imgs
+        for a, b in zip(alone, mixed):
+            assert a.shape == b.shape
+            assert np.array_equal(a, b)
+            assert np.isfinite(a).all()
+    finally:
+        alone_srv.close()
+        mix_srv.close()
+
+
+def test_budget_admission_and_errors(small_stream):
+    vs = small_stream
+    srv = serve.Server(max_inflight=3, queue_capacity=4, hbm_budget_bytes=64 << 20)
+    try:
+        vs.ids = [srv.add_volume(g) for g in vs.grids]
+        stream = serve.request_stream(vs, 4, rate=0, seed=9, n_min=64, n_max=200, images=(32,))
+        # a 64 MB budget admits these small requests one or two at a time;
+        # all complete
+        stats, imgs = serve.run_stream(srv, stream, want_images=True, realtime=False)
+        assert all(np.isfinite(i).all() for i in imgs)
+        # unknown ticket
+        with pytest.raises(LightGraphError):
+            srv.wait(123456, 0)
+        # a request larger than the whole budget is refused up front
+        big = serve.request_stream(vs, 1, rate=0, seed=1, n_min=3000, n_max=3000, images=(1024,))[0][1]
+        with pytest.raises(LightGraphError) as e:
+            srv.submit(big)
+        assert e.value.status == _capi.LG_ERR_NOMEM
+    finally:
+        srv.close()
+
+
+def test_queue_capacity(small_stream):
+    vs = small_stream
+    srv = serve.Server(max_inflight=1, queue_capacity=2)
+    try:
+        vs.ids = [srv.add_volume(g) for g in vs.grids]
+        stream = serve.request_stream(vs, 12, rate=0, seed=5, n_min=400, n_max=600, images=(64,))
+        tickets, busy = [], 0
+        for _, req in stream:
+            try:
+                tickets.append(srv.submit(req))
+            except LightGraphError as e:
+                assert e.status == _capi.LG_ERR_BUSY
+                busy += 1
+        for t in tickets:
+            srv.wait(t, -1, False)
+        assert busy > 0 and len(tickets) + busy == 12
+    finally:
+        srv.close()
