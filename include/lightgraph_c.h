@@ -323,6 +323,28 @@ lg_status lg_fw_device(float* dist, int n, int ld, void* stream);
 /* Host-memory convenience wrapper of lg_fw_device (copies in and out). */
 lg_status lg_fw_host(lg_ctx* ctx, float* dist, int n);
 
+/* Radiance diffusion that allocates nothing. This entry point has no
+ * counterpart in the reference. It exists for callers that cannot call
+ * cudaMalloc: processes whose device memory belongs to another allocator or a
+ * fixed arena, or plugins that must not change the device's memory footprint.
+ * The caller owns every input and output, in device memory:
+ *   dist_device    n x n optical depths after the path solve (leading
+ *                  dimension ld, diagonal 0, +inf = unreachable)
+ *   light_device   n x 3 vertex radiance (lg_vertex_light)
+ *   diffuse_device n x 3 result, the same as lg_diffuse's
+ *   extinction     the shader's extinction (<= 0 per channel)
+ * enqueued on `stream` (a cudaStream_t; NULL = legacy default stream).
+ * Scratch space is a fixed __device__ array inside the library sized for
+ * n <= LG_NOALLOC_MAX_POINTS (larger n returns LG_ERR_INVALID). Every GPU
+ * that loads the library keeps that array (about 1.7 MB) until the process
+ * exits. All calls share it, so calls that overlap on the GPU race; serialise
+ * them. The first call on each device looks up the array's device address, so
+ * make that first call before any CUDA graph capture on the device. */
+#define LG_NOALLOC_MAX_POINTS 8192
+lg_status lg_diffuse_noalloc(const float* dist_device, int n, int ld,
+                             const float* light_device, float* diffuse_device,
+                             const double extinction[3], void* stream);
+
 /* ------------------------------------------------------------------------- */
 /* Serving (no counterpart in the reference, which renders one frame per run) */
 /* ------------------------------------------------------------------------- */

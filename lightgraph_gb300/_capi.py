@@ -121,6 +121,7 @@ SIGNATURES = {
     "lg_fw_schedule": (I32, [P, C.POINTER(C.c_int), C.POINTER(D), C.c_int]),
     "lg_fw_device": (I32, [P, C.c_int, C.c_int, P]),
     "lg_fw_host": (I32, [P, P, C.c_int]),
+    "lg_diffuse_noalloc": (I32, [P, C.c_int, C.c_int, P, P, C.POINTER(D), P]),
     "lg_server_create": (I32, [C.POINTER(ServerOptsC), C.POINTER(P)]),
     "lg_server_destroy": (I32, [P]),
     "lg_server_last_error": (C.c_char_p, [P]),

@@ -29,7 +29,7 @@ LIB_NAME = "liblightgraph_gb300.so"
 ORACLE_NAME = "liblg_oracle.so"
 
 CU_SOURCES = ["lg_api.cu", "k_graph.cu", "k_march.cu", "k_fw.cu", "k_diffuse.cu", "k_splat.cu",
-              "k_render.cu", "k_grid.cu", "lg_server.cu"]
+              "k_render.cu", "k_grid.cu", "lg_server.cu", "lg_noalloc.cu"]
 CC_SOURCES = ["scene.cc", "lg_parse.cc"]
 CLI_SOURCE = "cli.cc"
 ORACLE_SOURCES = ["lg_oracle.cc"]
