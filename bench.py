@@ -62,8 +62,12 @@ def run_serving(n: int, rate: float):
     out = {"stream": f"{n} requests, Poisson {rate} req/s, seed 4, volumes 64^3-512^3, 512-8192 points, "
                      "128^2-1024^2 at 1-4 spp, 1-3 lights"}
     vs = serve.make_volumes(None)
-    # single-request latency: each request alone on an idle server
-    for label, slots, realtime in (("alone", 1, False), ("plain", 1, True), ("batched", 4, True)):
+    # single-request latency: each request alone on an idle server; "plain" and
+    # "batched" replay the Poisson arrivals; the *_capacity runs submit every
+    # request at once (throughput when the queue never drains)
+    runs = (("alone", 1, False), ("plain", 1, True), ("batched", 8, True), ("plain_capacity", 1, False),
+            ("batched_capacity", 8, False))
+    for label, slots, realtime in runs:
         srv = serve.Server(max_inflight=slots)
         vs.ids = [srv.add_volume(g) for g in vs.grids]
         stream = serve.request_stream(vs, n, rate, seed=4)
@@ -79,6 +83,8 @@ def run_serving(n: int, rate: float):
             out[label] = stats
         srv.close()
     out["batched_over_plain_renders_per_s"] = out["batched"]["renders_per_s"] / out["plain"]["renders_per_s"]
+    out["capacity_batched_over_plain"] = (out["batched_capacity"]["renders_per_s"] /
+                                          out["plain_capacity"]["renders_per_s"])
     out["batched_p99_over_alone_p99"] = out["batched"]["p99_ms"] / out["alone_p99_ms"]
     return out
 
@@ -371,6 +377,7 @@ def run_ours(args):
     render_bytes = (prim + shad) * 32.0 + W * H * 64.0
     achieved = render_bytes / (render_ms * 1e-3) / 1e9
     ld = (len(pts) + 127) // 128 * 128  # the solve runs on the 128-padded matrix
+    fw_sched, fw_tuned = ctx.fw_schedule()
     fw_flops = 2.0 * ld ** 3
     fw_tflops = fw_flops / (stage_ms[2] * 1e-3) / 1e12
     line = {
@@ -391,7 +398,10 @@ def run_ours(args):
         "fw_roofline": {"kernel": "k_fw_update+k_fw_panels", "bound": "fp32_alu", "n": int(ld),
                         "achieved": fw_tflops, "unit": "TFLOP/s", "peak": NOMINAL_FP32_TFLOPS,
                         "peak_kind": "nominal (152 SMs x 128 lanes x 2 x 2.07 GHz)",
-                        "frac": fw_tflops / NOMINAL_FP32_TFLOPS},
+                        "frac": fw_tflops / NOMINAL_FP32_TFLOPS,
+                        "schedule": {0: "per-round launches", 1: "persistent 1 CTA/SM",
+                                     2: "persistent 2 CTA/SM"}.get(fw_sched, str(fw_sched)),
+                        "autotuner_ms": [round(x, 4) for x in fw_tuned]},
     }
     if rank == 0 and args.serving > 0:
         line["serving"] = run_serving(args.serving, args.rate)

@@ -11,6 +11,7 @@
 namespace lg {
 
 // One thread per edge; grid.y = graph.
+template <int DT>
 __global__ void __launch_bounds__(128) k_edge_march(DevScene sc, const float* __restrict__ pts,
                                                     const GraphInfo* __restrict__ graphs,
                                                     const int2* __restrict__ edges,
@@ -46,7 +47,7 @@ __global__ void __launch_bounds__(128) k_edge_march(DevScene sc, const float* __
         float tau;
         bool dropped;
         uint32_t ns = 0;
-        if (march_fixed(G, r, sc.step1, scale, sh.dMax, sh.tau_drop, contrib, tau, dropped, ns)) {
+        if (march_fixed<DT>(G, r, sc.step1, scale, sh.dMax, sh.tau_drop, contrib, tau, dropped, ns)) {
             value = dropped ? kInf : tau;
         }
     }
@@ -56,6 +57,7 @@ __global__ void __launch_bounds__(128) k_edge_march(DevScene sc, const float* __
 }
 
 // One thread per vertex; grid.y = graph. Output L: 3 floats per vertex.
+template <int DT>
 __global__ void __launch_bounds__(128) k_vertex_light(DevScene sc, const float* __restrict__ pts,
                                                       const GraphInfo* __restrict__ graphs,
                                                       float* __restrict__ L) {
@@ -100,11 +102,11 @@ __global__ void __launch_bounds__(128) k_vertex_light(DevScene sc, const float* 
             float tau;
             bool dropped;
             uint32_t nsmp = 0;
-            if (!march_fixed(G, r, sc.step1, scale, sh.dMax, sh.tau_drop, contrib, tau, dropped, nsmp))
+            if (!march_fixed<DT>(G, r, sc.step1, scale, sh.dMax, sh.tau_drop, contrib, tau, dropped, nsmp))
                 continue;  // shadow ray misses the grid bbox: no contribution
             if (dropped) continue;
 #pragma unroll
-            for (int c = 0; c < 3; ++c) lum[c] += I[c] * __expf(-sh.a[c] * tau);
+            for (int c = 0; c < 3; ++c) lum[c] += I[c] * expf(-sh.a[c] * tau);
         }
 #pragma unroll
         for (int c = 0; c < 3; ++c) acc[c] += sh.albedo[c] * (lum[c] / (float)ns);
@@ -119,7 +121,9 @@ cudaError_t launch_edge_march(const DevScene& sc, const float* pts, const GraphI
                               const int32_t* edge_cnt, float* S, cudaStream_t st) {
     if (n_graphs == 0 || max_edges == 0) return cudaSuccess;
     dim3 grid((max_edges + 127) / 128, n_graphs);
-    k_edge_march<<<grid, 128, 0, st>>>(sc, pts, graphs, edges, edge_cnt, S);
+    if (sc.dens.dtype == 1) k_edge_march<1><<<grid, 128, 0, st>>>(sc, pts, graphs, edges, edge_cnt, S);
+    else if (sc.dens.dtype == 2) k_edge_march<2><<<grid, 128, 0, st>>>(sc, pts, graphs, edges, edge_cnt, S);
+    else k_edge_march<0><<<grid, 128, 0, st>>>(sc, pts, graphs, edges, edge_cnt, S);
     ++g_launch_counter;
     return cudaGetLastError();
 }
@@ -128,7 +132,9 @@ cudaError_t launch_vertex_light(const DevScene& sc, const float* pts, const Grap
                                 int n_graphs, int max_n, float* L, cudaStream_t st) {
     if (n_graphs == 0 || max_n == 0) return cudaSuccess;
     dim3 grid((max_n + 127) / 128, n_graphs);
-    k_vertex_light<<<grid, 128, 0, st>>>(sc, pts, graphs, L);
+    if (sc.dens.dtype == 1) k_vertex_light<1><<<grid, 128, 0, st>>>(sc, pts, graphs, L);
+    else if (sc.dens.dtype == 2) k_vertex_light<2><<<grid, 128, 0, st>>>(sc, pts, graphs, L);
+    else k_vertex_light<0><<<grid, 128, 0, st>>>(sc, pts, graphs, L);
     ++g_launch_counter;
     return cudaGetLastError();
 }

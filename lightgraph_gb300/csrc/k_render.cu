@@ -86,7 +86,7 @@ struct PixelSample {
 // One thread per pixel-sample ps = pixel * spp + s. kWrite = false only
 // counts the shading samples; kWrite = true accumulates the scatter and
 // emission AOVs and writes the shadow tasks at offsets[ps].
-template <bool kWrite>
+template <bool kWrite, int DT>
 __global__ void __launch_bounds__(128, 4) k_primary(DevScene sc, DevCamera cam, DevScatterGrid sg,
                                                  int32_t* __restrict__ counts, const int32_t* __restrict__ offsets,
                                                  ShadowTask* __restrict__ tasks, int64_t task_cap,
@@ -120,7 +120,7 @@ __global__ void __launch_bounds__(128, 4) k_primary(DevScene sc, DevCamera cam, 
                     const uint32_t n = n_iter++;
                     ++n_primary;
                     const float p[3] = {pr.e[0] + pT * pr.d[0], pr.e[1] + pT * pr.d[1], pr.e[2] + pT * pr.d[2]};
-                    const float rho = fminf(sample_index(G, p[0], p[1], p[2]) * sh.dS, sh.dMax);
+                    const float rho = fminf(sample_index_t<DT>(G, p[0], p[1], p[2]) * sh.dS, sh.dMax);
                     if (rho < cutoff) { pT += pStep; continue; }
                     float omdT[3], dT[3];
 #pragma unroll
@@ -179,6 +179,7 @@ __global__ void __launch_bounds__(128, 4) k_primary(DevScene sc, DevCamera cam, 
 
 // One thread per shadow task (grid-stride over the device-side total).
 // direct[t] = sum over lights of albedo * (sum_ls I * T_shadow / ns) * w.
+template <int DT>
 __global__ void __launch_bounds__(128, 4) k_shadow(DevScene sc, const ShadowTask* __restrict__ tasks,
                                                 const int32_t* __restrict__ total_ptr, int64_t task_cap,
                                                 float4* __restrict__ direct, unsigned long long* __restrict__ ctr) {
@@ -220,7 +221,7 @@ __global__ void __launch_bounds__(128, 4) k_shadow(DevScene sc, const ShadowTask
                     ++sspan;
                     for (float sT = step1 * ceilf(sa / step1); sT <= sb && sT + sStep > sT;) {
                         const uint32_t q = siter++;
-                        const float rs = fminf(sample_index(G, srr.e[0] + sT * srr.d[0], srr.e[1] + sT * srr.d[1],
+                        const float rs = fminf(sample_index_t<DT>(G, srr.e[0] + sT * srr.d[0], srr.e[1] + sT * srr.d[1],
                                                             srr.e[2] + sT * srr.d[2]) * scale,
                                                sh.dMax);
                         if (rs < cutoff) { sT += sStep; continue; }
@@ -291,8 +292,13 @@ cudaError_t launch_render_count(const DevScene& sc, const DevCamera& cam, const 
                                 cudaStream_t st) {
     const int64_t n_ps = (int64_t)cam.width * cam.height * cam.spp;
     if (n_ps == 0) return cudaSuccess;
-    k_primary<false><<<(unsigned)((n_ps + 127) / 128), 128, 0, st>>>(sc, cam, sg, counts, nullptr, nullptr, 0,
-                                                                     nullptr, nullptr);
+    const unsigned blocks = (unsigned)((n_ps + 127) / 128);
+    if (sc.dens.dtype == 1)
+        k_primary<false, 1><<<blocks, 128, 0, st>>>(sc, cam, sg, counts, nullptr, nullptr, 0, nullptr, nullptr);
+    else if (sc.dens.dtype == 2)
+        k_primary<false, 2><<<blocks, 128, 0, st>>>(sc, cam, sg, counts, nullptr, nullptr, 0, nullptr, nullptr);
+    else
+        k_primary<false, 0><<<blocks, 128, 0, st>>>(sc, cam, sg, counts, nullptr, nullptr, 0, nullptr, nullptr);
     ++g_launch_counter;
     return cudaGetLastError();
 }
@@ -306,9 +312,17 @@ cudaError_t launch_render_shade(const DevScene& sc, const DevCamera& cam, const 
     const int64_t n_pix = (int64_t)cam.width * cam.height;
     if (n_ps == 0) return cudaSuccess;
     PixelSample* pss = reinterpret_cast<PixelSample*>(pixel_samples);
-    k_primary<true><<<(unsigned)((n_ps + 127) / 128), 128, 0, st>>>(sc, cam, sg, nullptr, offsets, tasks, task_cap,
-                                                                    pss, counters);
-    k_shadow<<<sms * 16, 128, 0, st>>>(sc, tasks, total, task_cap, direct, counters);
+    const unsigned blocks = (unsigned)((n_ps + 127) / 128);
+    if (sc.dens.dtype == 1) {
+        k_primary<true, 1><<<blocks, 128, 0, st>>>(sc, cam, sg, nullptr, offsets, tasks, task_cap, pss, counters);
+        k_shadow<1><<<sms * 16, 128, 0, st>>>(sc, tasks, total, task_cap, direct, counters);
+    } else if (sc.dens.dtype == 2) {
+        k_primary<true, 2><<<blocks, 128, 0, st>>>(sc, cam, sg, nullptr, offsets, tasks, task_cap, pss, counters);
+        k_shadow<2><<<sms * 16, 128, 0, st>>>(sc, tasks, total, task_cap, direct, counters);
+    } else {
+        k_primary<true, 0><<<blocks, 128, 0, st>>>(sc, cam, sg, nullptr, offsets, tasks, task_cap, pss, counters);
+        k_shadow<0><<<sms * 16, 128, 0, st>>>(sc, tasks, total, task_cap, direct, counters);
+    }
     k_resolve<<<(unsigned)((n_pix + 127) / 128), 128, 0, st>>>(cam, offsets, counts, pss, direct, task_cap, rgba,
                                                               dfilm, sfilm, efilm);
     g_launch_counter += 3;

@@ -241,6 +241,11 @@ lg_status Ctx::upload_grid(int which, const lg_grid_desc* desc, const float* val
     }
     g.h = (float)desc->voxel_size;
     g.inv_h = (float)(1.0 / desc->voxel_size);
+    // the samplers address voxels with 32-bit offsets
+    if ((uint64_t)g.nb[0] * g.nb[1] * g.nb[2] * 512ull >= (1ull << 32))
+        return fail(LG_ERR_INVALID, "grid too large: the padded brick box must hold fewer than 2^32 voxels");
+    g.sy = (uint32_t)g.nb[0] * 512u;
+    g.sz = (uint32_t)g.nb[0] * (uint32_t)g.nb[1] * 512u;
     const int64_t nvox = (int64_t)desc->dims[0] * desc->dims[1] * desc->dims[2];
     const int64_t nbt = (int64_t)g.nb[0] * g.nb[1] * g.nb[2];
     const size_t esz = dtype == 0 ? 4 : 2;

@@ -35,7 +35,56 @@ struct DevGrid {
     float bbmin[3] = {0.f, 0.f, 0.f};    // leaf bbox in index space (origin of min leaf)
     float bbmax[3] = {0.f, 0.f, 0.f};    // ... max leaf origin + 8
     int has_leaves = 0;
+    uint32_t sy = 0, sz = 0;             // element strides of one brick step in y and z
 };
+
+template <int DT>
+__device__ __forceinline__ float ldv(const void* data, uint32_t off) {
+    if (DT == 0) return __ldg(reinterpret_cast<const float*>(data) + off);
+    if (DT == 1) return __half2float(__ldg(reinterpret_cast<const __half*>(data) + off));
+    return __bfloat162float(__ldg(reinterpret_cast<const __nv_bfloat16*>(data) + off));
+}
+
+// Trilinear sample for storage type DT without branches: per axis, the brick
+// and in-brick offsets of the two taps are computed once, the eight offsets
+// are sums of them, and taps outside the brick box read 0 through a
+// predicated load. Offsets are 32-bit (the upload rejects grids whose brick
+// box has 2^32 or more elements). Same taps and interpolation order as
+// sample_index.
+template <int DT>
+__device__ __forceinline__ float sample_index_t(const DevGrid& g, float px, float py, float pz) {
+    const float fx = floorf(px), fy = floorf(py), fz = floorf(pz);
+    const int ix = (int)fx, iy = (int)fy, iz = (int)fz;
+    const float wx = px - fx, wy = py - fy, wz = pz - fz;
+    const int bx0 = (ix >> 3) - g.blo[0], bx1 = ((ix + 1) >> 3) - g.blo[0];
+    const int by0 = (iy >> 3) - g.blo[1], by1 = ((iy + 1) >> 3) - g.blo[1];
+    const int bz0 = (iz >> 3) - g.blo[2], bz1 = ((iz + 1) >> 3) - g.blo[2];
+    const bool vx0 = (unsigned)bx0 < (unsigned)g.nb[0], vx1 = (unsigned)bx1 < (unsigned)g.nb[0];
+    const bool vy0 = (unsigned)by0 < (unsigned)g.nb[1], vy1 = (unsigned)by1 < (unsigned)g.nb[1];
+    const bool vz0 = (unsigned)bz0 < (unsigned)g.nb[2], vz1 = (unsigned)bz1 < (unsigned)g.nb[2];
+    const uint32_t ox0 = (uint32_t)bx0 * 512u + (uint32_t)(ix & 7);
+    const uint32_t ox1 = (uint32_t)bx1 * 512u + (uint32_t)((ix + 1) & 7);
+    const uint32_t oy0 = (uint32_t)by0 * g.sy + (uint32_t)(iy & 7) * 8u;
+    const uint32_t oy1 = (uint32_t)by1 * g.sy + (uint32_t)((iy + 1) & 7) * 8u;
+    const uint32_t oz0 = (uint32_t)bz0 * g.sz + (uint32_t)(iz & 7) * 64u;
+    const uint32_t oz1 = (uint32_t)bz1 * g.sz + (uint32_t)((iz + 1) & 7) * 64u;
+    const uint32_t o00 = oy0 + oz0, o10 = oy1 + oz0, o01 = oy0 + oz1, o11 = oy1 + oz1;
+    const bool v00 = vy0 && vz0, v10 = vy1 && vz0, v01 = vy0 && vz1, v11 = vy1 && vz1;
+    const void* D = g.data;
+    // v[x][y][z]
+    const float v000 = (vx0 && v00) ? ldv<DT>(D, ox0 + o00) : 0.f;
+    const float v100 = (vx1 && v00) ? ldv<DT>(D, ox1 + o00) : 0.f;
+    const float v010 = (vx0 && v10) ? ldv<DT>(D, ox0 + o10) : 0.f;
+    const float v110 = (vx1 && v10) ? ldv<DT>(D, ox1 + o10) : 0.f;
+    const float v001 = (vx0 && v01) ? ldv<DT>(D, ox0 + o01) : 0.f;
+    const float v101 = (vx1 && v01) ? ldv<DT>(D, ox1 + o01) : 0.f;
+    const float v011 = (vx0 && v11) ? ldv<DT>(D, ox0 + o11) : 0.f;
+    const float v111 = (vx1 && v11) ? ldv<DT>(D, ox1 + o11) : 0.f;
+    const float y00 = fmaf(v001 - v000, wz, v000), y01 = fmaf(v011 - v010, wz, v010);
+    const float y10 = fmaf(v101 - v100, wz, v100), y11 = fmaf(v111 - v110, wz, v110);
+    const float x0 = fmaf(y01 - y00, wy, y00), x1 = fmaf(y11 - y10, wy, y10);
+    return fmaf(x1 - x0, wx, x0);
+}
 
 __device__ __forceinline__ float load_voxel(const DevGrid& g, int64_t off) {
     if (g.dtype == 0) return __ldg(reinterpret_cast<const float*>(g.data) + off);
@@ -372,7 +421,7 @@ __device__ __forceinline__ void illuminate(const DevLight& L, const float p[3], 
 // caller. Returns false if the ray misses the leaf bbox. Sets dropped when
 // tau crosses sh.tau_drop (the reference's |T|^2 < cutoff test).
 // ---------------------------------------------------------------------------
-template <class Contrib>
+template <int DT, class Contrib>
 __device__ __forceinline__ bool march_fixed(const DevGrid& g, IRay r, float step, float scale,
                                             float dmax, float tau_drop, Contrib contrib,
                                             float& tau, bool& dropped, uint32_t& nsamples) {
@@ -385,7 +434,7 @@ __device__ __forceinline__ bool march_fixed(const DevGrid& g, IRay r, float step
     while (next_span(g, s, ta, tb)) {
         for (float t = step * ceilf(ta / step); t <= tb && t + step > t; t += step) {
             const float rho = fminf(
-                sample_index(g, r.e[0] + t * r.d[0], r.e[1] + t * r.d[1], r.e[2] + t * r.d[2]) * scale,
+                sample_index_t<DT>(g, r.e[0] + t * r.d[0], r.e[1] + t * r.d[1], r.e[2] + t * r.d[2]) * scale,
                 dmax);
             ++nsamples;
             float c;
