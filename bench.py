@@ -89,6 +89,18 @@ def run_serving(n: int, rate: float):
     return out
 
 
+def job_time_ms(t_ms: float, world: int, device: str = "cuda") -> float:
+    """The job's time over N replica ranks: the maximum of the ranks' times
+    (every rank runs the same number of frames)."""
+    if world <= 1:
+        return t_ms
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([t_ms], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def dist_env():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -308,6 +320,7 @@ def run_ours(args):
         ctx.frame_device(sc.opts, sc.max_connect)
     torch.cuda.synchronize()
     prim, shad = ctx.render_stats()
+    tasks_per_frame = ctx.shading_tasks()
 
     # timed region: K frames, grids and points resident
     lib.lg_set_profiling(ctx.h, 1)
@@ -322,25 +335,25 @@ def run_ours(args):
     ev1 = torch.cuda.Event(enable_timing=True)
     ev0.record(stream)
     buf = (C.c_double * len(STAGES))()
+    wbuf = (C.c_double * 4)()
+    wave_ms = np.zeros(4)
     for _ in range(args.steps):
         ctx.frame_device(sc.opts, sc.max_connect)
-        st = lib.lg_stage_times(ctx.h, buf, len(STAGES))
-        if st == 0:
+        if lib.lg_stage_times(ctx.h, buf, len(STAGES)) == 0:
             stage_ms += np.array(buf[:])
+        if lib.lg_render_wave_times(ctx.h, wbuf) == 0:
+            wave_ms += np.array(wbuf[:])
     ev1.record(stream)
     torch.cuda.synchronize()
     barrier()
     clk = clocks.stop()
     launches = ctx.kernel_launches() - launches0
     lib.lg_set_profiling(ctx.h, 0)
-    t_ms = ev0.elapsed_time(ev1)
-    if world > 1:
-        tt = torch.tensor([t_ms], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_ms = float(tt.item())
+    t_ms = job_time_ms(ev0.elapsed_time(ev1), world)
     ms_per_step = t_ms / args.steps
     value = ms_per_step / world
     stage_ms /= args.steps
+    wave_ms /= args.steps
 
     # e2e through the C ABI from pinned host memory
     pts = sc.points[0]
@@ -361,21 +374,20 @@ def run_ours(args):
                                  C.byref(cam), *[f.data_ptr() for f in films])
         if st != 0:
             raise RuntimeError(lib.lg_last_error(ctx.h).decode())
-    e2e_ms = (time.perf_counter() - t0) * 1e3 / args.steps
-    if world > 1:
-        tt = torch.tensor([e2e_ms], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        e2e_ms = float(tt.item())
+    e2e_ms = job_time_ms((time.perf_counter() - t0) * 1e3 / args.steps, world)
     e2e_value = e2e_ms / world
     h2d = pin_pts.numel() * 4 + offs.numel() * 8 + r2.numel() * 4
     d2h = sum(f.numel() * 4 for f in films)
 
     peaks, peak_kind = measured_peaks()
-    # dominant kernel: the render (k_render). Algorithmic bytes per launch:
-    # 8 taps x 4 B per density sample (primary + shadow) + 4 films x 16 B / px.
-    render_ms = stage_ms[6]
+    # dominant kernel: k_shadow (the shadow-ray wave of the render). Its
+    # algorithmic bytes per launch: 8 taps x 4 B per shadow density sample
+    # plus the 32 B task read and 16 B result write per shading sample.
+    shadow_ms = wave_ms[2]
+    shadow_bytes = shad * 32.0 + tasks_per_frame * 48.0
+    achieved = shadow_bytes / (shadow_ms * 1e-3) / 1e9
     render_bytes = (prim + shad) * 32.0 + W * H * 64.0
-    achieved = render_bytes / (render_ms * 1e-3) / 1e9
+    render_gbs = render_bytes / (stage_ms[6] * 1e-3) / 1e9
     ld = (len(pts) + 127) // 128 * 128  # the solve runs on the 128-padded matrix
     fw_sched, fw_tuned = ctx.fw_schedule()
     fw_flops = 2.0 * ld ** 3
@@ -389,12 +401,16 @@ def run_ours(args):
         "gpu_launches": int(launches),
         "clocks": clk,
         "stages_ms": {k: round(float(v), 4) for k, v in zip(STAGES, stage_ms)},
-        "roofline": {"kernel": "render waves (k_primary x2, k_shadow, k_resolve)", "bound": "hbm",
-                     "achieved": achieved,
+        "roofline": {"kernel": "k_shadow", "bound": "hbm", "achieved": achieved,
                      "peak": peaks.get("hbm_gbs"), "unit": "GB/s",
-                     "frac": achieved / peaks.get("hbm_gbs"), "peak_kind": peak_kind,
-                     "traffic": profile_traffic("k_render_production.txt"),
-                     "algorithmic_bytes": render_bytes, "samples": {"primary": prim, "shadow": shad}},
+                     "frac": achieved / peaks.get("hbm_gbs"), "peak_kind": peak_kind + " (burst copy)",
+                     "traffic": profile_traffic("k_shadow_production.txt"),
+                     "algorithmic_bytes": shadow_bytes, "launch_ms": shadow_ms,
+                     "samples": {"primary": prim, "shadow": shad, "shading_tasks": tasks_per_frame}},
+        "render_waves_ms": {"count_scan": wave_ms[0], "primary": wave_ms[1], "shadow": wave_ms[2],
+                            "resolve": wave_ms[3]},
+        "render_stage": {"ms": float(stage_ms[6]), "algorithmic_bytes": render_bytes, "achieved_gbs": render_gbs,
+                         "frac": render_gbs / peaks.get("hbm_gbs")},
         "fw_roofline": {"kernel": "k_fw_update+k_fw_panels", "bound": "fp32_alu", "n": int(ld),
                         "achieved": fw_tflops, "unit": "TFLOP/s", "peak": NOMINAL_FP32_TFLOPS,
                         "peak_kind": "nominal (152 SMs x 128 lanes x 2 x 2.07 GHz)",

@@ -278,10 +278,11 @@ lg_status lg_frame_device(lg_ctx* ctx, int max_connect, double point_voxel_size,
 lg_status lg_get_films(lg_ctx* ctx, float* rgba, float* direct, float* scatter,
                        float* emission);
 
-/* Statistics of the last render on this context (after a sync): number of
- * density samples taken by primary and shadow rays. */
+/* Statistics of the last render on this context (waits for it): density
+ * samples taken by primary and shadow rays, and primary samples that shaded
+ * (each casts the shadow rays of every light sample). Any pointer may be null. */
 lg_status lg_render_stats(lg_ctx* ctx, uint64_t* primary_samples,
-                          uint64_t* shadow_samples);
+                          uint64_t* shadow_samples, uint64_t* shading_samples);
 
 /* Stage timing of lg_frame_device, the equivalent of the reference's
  * tbb::tick_count prints (src/main.cc:553,589,125, src/LightGraph.h:268-585):
@@ -291,6 +292,9 @@ lg_status lg_render_stats(lg_ctx* ctx, uint64_t* primary_samples,
  * diffusion, splat, render. */
 lg_status lg_set_profiling(lg_ctx* ctx, int on);
 lg_status lg_stage_times(lg_ctx* ctx, double* ms, int n);
+/* The render stage of the last profiled frame split into its waves (ms):
+ * primary count + scan, primary shading, shadow rays, resolve. */
+lg_status lg_render_wave_times(lg_ctx* ctx, double ms[4]);
 
 /* Frame replay: when on, lg_frame_device runs the frame once, captures the
  * same launch sequence in a CUDA graph and replays it on later calls with the

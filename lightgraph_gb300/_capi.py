@@ -111,10 +111,11 @@ SIGNATURES = {
     "lg_render": (I32, [P, C.POINTER(CameraC), P, P, P, P]),
     "lg_render_frame": (I32, [P, C.c_int, P, P, P, C.c_int, D, C.POINTER(CameraC), P, P, P, P]),
     "lg_frame_device": (I32, [P, C.c_int, D, C.POINTER(CameraC)]),
-    "lg_render_stats": (I32, [P, C.POINTER(U64), C.POINTER(U64)]),
+    "lg_render_stats": (I32, [P, C.POINTER(U64), C.POINTER(U64), C.POINTER(U64)]),
     "lg_get_films": (I32, [P, P, P, P, P]),
     "lg_set_profiling": (I32, [P, C.c_int]),
     "lg_stage_times": (I32, [P, C.POINTER(D), C.c_int]),
+    "lg_render_wave_times": (I32, [P, C.POINTER(D)]),
     "lg_set_graph_mode": (I32, [P, C.c_int]),
     "lg_frame_launches": (U64, [P]),
     "lg_set_fw_schedule": (I32, [P, C.c_int]),

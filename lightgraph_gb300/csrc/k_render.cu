@@ -307,24 +307,29 @@ cudaError_t launch_render_shade(const DevScene& sc, const DevCamera& cam, const 
                                 const int32_t* counts, const int32_t* offsets, const int32_t* total,
                                 ShadowTask* tasks, int64_t task_cap, void* pixel_samples, float4* direct,
                                 float4* rgba, float4* dfilm, float4* sfilm, float4* efilm,
-                                unsigned long long* counters, int sms, cudaStream_t st) {
+                                unsigned long long* counters, int sms, cudaStream_t st, cudaEvent_t* marks) {
     const int64_t n_ps = (int64_t)cam.width * cam.height * cam.spp;
     const int64_t n_pix = (int64_t)cam.width * cam.height;
     if (n_ps == 0) return cudaSuccess;
     PixelSample* pss = reinterpret_cast<PixelSample*>(pixel_samples);
     const unsigned blocks = (unsigned)((n_ps + 127) / 128);
-    if (sc.dens.dtype == 1) {
+    auto mark = [&](int k) {
+        if (marks && marks[k]) cudaEventRecord(marks[k], st);
+    };
+    if (sc.dens.dtype == 1)
         k_primary<true, 1><<<blocks, 128, 0, st>>>(sc, cam, sg, nullptr, offsets, tasks, task_cap, pss, counters);
-        k_shadow<1><<<sms * 16, 128, 0, st>>>(sc, tasks, total, task_cap, direct, counters);
-    } else if (sc.dens.dtype == 2) {
+    else if (sc.dens.dtype == 2)
         k_primary<true, 2><<<blocks, 128, 0, st>>>(sc, cam, sg, nullptr, offsets, tasks, task_cap, pss, counters);
-        k_shadow<2><<<sms * 16, 128, 0, st>>>(sc, tasks, total, task_cap, direct, counters);
-    } else {
+    else
         k_primary<true, 0><<<blocks, 128, 0, st>>>(sc, cam, sg, nullptr, offsets, tasks, task_cap, pss, counters);
-        k_shadow<0><<<sms * 16, 128, 0, st>>>(sc, tasks, total, task_cap, direct, counters);
-    }
+    mark(0);
+    if (sc.dens.dtype == 1) k_shadow<1><<<sms * 16, 128, 0, st>>>(sc, tasks, total, task_cap, direct, counters);
+    else if (sc.dens.dtype == 2) k_shadow<2><<<sms * 16, 128, 0, st>>>(sc, tasks, total, task_cap, direct, counters);
+    else k_shadow<0><<<sms * 16, 128, 0, st>>>(sc, tasks, total, task_cap, direct, counters);
+    mark(1);
     k_resolve<<<(unsigned)((n_pix + 127) / 128), 128, 0, st>>>(cam, offsets, counts, pss, direct, task_cap, rgba,
                                                               dfilm, sfilm, efilm);
+    mark(2);
     g_launch_counter += 3;
     return cudaGetLastError();
 }

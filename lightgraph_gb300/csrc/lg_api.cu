@@ -195,6 +195,8 @@ extern "C" lg_status lg_destroy(lg_ctx* handle) {
     if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
     for (int k = 0; k <= Ctx::kStages; ++k)
         if (ctx->ev[k]) cudaEventDestroy(ctx->ev[k]);
+    for (int k = 0; k < 5; ++k)
+        if (ctx->wev[k]) cudaEventDestroy(ctx->wev[k]);
     cudaStreamDestroy(ctx->st);
     delete ctx;
     return LG_OK;
@@ -981,9 +983,11 @@ lg_status Ctx::render(const lg_camera* c) {
     CK(d_ps_scan.reserve(sizeof(int32_t) * (nps1 / 1024 + 2)), "render alloc");
     CK(d_ps_total.reserve(sizeof(int32_t) * 2), "render alloc");
     CK(d_ps_data.reserve(pixel_sample_bytes() * nps1), "render alloc");
+    wmark(0);
     CK(launch_render_count(sc, cam, sg, d_ps_count.as<int32_t>(), st), "render count");
     CK(launch_exclusive_scan(d_ps_count.as<int32_t>(), n_ps, d_ps_offset.as<int32_t>(), d_ps_scan.as<int32_t>(),
                              d_ps_total.as<int32_t>(), st), "render scan");
+    wmark(1);
     if (!capturing) {
         // size the shadow-task buffer from this frame's count (a captured
         // replay reuses the capacity of the run it was captured after)
@@ -1000,7 +1004,7 @@ lg_status Ctx::render(const lg_camera* c) {
     CK(launch_render_shade(sc, cam, sg, d_ps_count.as<int32_t>(), d_ps_offset.as<int32_t>(), d_ps_total.as<int32_t>(),
                            d_tasks.as<ShadowTask>(), cap, d_ps_data.p, d_task_direct.as<float4>(), d_rgba.as<float4>(),
                            d_direct.as<float4>(), d_scatter.as<float4>(), d_emission.as<float4>(),
-                           d_counters.as<unsigned long long>(), sms, st),
+                           d_counters.as<unsigned long long>(), sms, st, profiling ? wev + 2 : nullptr),
        "render");
     return LG_OK;
 }
@@ -1032,16 +1036,20 @@ extern "C" lg_status lg_get_films(lg_ctx* handle, float* rgba, float* direct, fl
     return ctx->download_films(rgba, direct, scatter, emission);
 }
 
-extern "C" lg_status lg_render_stats(lg_ctx* handle, uint64_t* primary, uint64_t* shadow) {
+extern "C" lg_status lg_render_stats(lg_ctx* handle, uint64_t* primary, uint64_t* shadow, uint64_t* shading) {
     Ctx* ctx = reinterpret_cast<Ctx*>(handle);
     GUARD(ctx);
     unsigned long long c[2] = {0, 0};
+    int32_t tasks = 0;
     if (ctx->d_counters.bytes >= sizeof c) {
         CK(cudaMemcpyAsync(c, ctx->d_counters.p, sizeof c, cudaMemcpyDeviceToHost, ctx->st), "counter download");
+        if (ctx->d_ps_total.bytes >= sizeof tasks)
+            CK(cudaMemcpyAsync(&tasks, ctx->d_ps_total.p, sizeof tasks, cudaMemcpyDeviceToHost, ctx->st), "task count");
         CK(cudaStreamSynchronize(ctx->st), "sync");
     }
     if (primary) *primary = c[0];
     if (shadow) *shadow = c[1];
+    if (shading) *shading = (uint64_t)tasks;
     return LG_OK;
 }
 
@@ -1125,6 +1133,20 @@ lg_status Ctx::frame_enqueue(double point_voxel_size, const lg_camera* camera) {
     return s;
 }
 
+extern "C" lg_status lg_render_wave_times(lg_ctx* handle, double ms[4]) {
+    Ctx* ctx = reinterpret_cast<Ctx*>(handle);
+    GUARD(ctx);
+    if (!ctx->ev_recorded || !ctx->wev[4]) return ctx->fail(LG_ERR_STATE, "no profiled frame");
+    if (!ms) return ctx->fail(LG_ERR_INVALID, "null output");
+    CK(cudaEventSynchronize(ctx->wev[4]), "event sync");
+    for (int k = 0; k < 4; ++k) {
+        float t = 0.f;
+        CK(cudaEventElapsedTime(&t, ctx->wev[k], ctx->wev[k + 1]), "event time");
+        ms[k] = t;
+    }
+    return LG_OK;
+}
+
 extern "C" lg_status lg_set_graph_mode(lg_ctx* handle, int on) {
     Ctx* ctx = reinterpret_cast<Ctx*>(handle);
     GUARD(ctx);
@@ -1172,6 +1194,7 @@ extern "C" lg_status lg_set_profiling(lg_ctx* handle, int on) {
     GUARD(ctx);
     if (on && !ctx->ev[0]) {
         for (int k = 0; k <= Ctx::kStages; ++k) CK(cudaEventCreate(&ctx->ev[k]), "event create");
+        for (int k = 0; k < 5; ++k) CK(cudaEventCreate(&ctx->wev[k]), "event create");
     }
     ctx->profiling = on != 0;
     ctx->graph_valid = false;

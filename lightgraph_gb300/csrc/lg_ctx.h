@@ -138,6 +138,11 @@ struct Ctx {
     void mark(int k) {
         if (profiling && ev[k]) cudaEventRecord(ev[k], st);
     }
+    // render waves: count + scan, primary, shadow, resolve
+    cudaEvent_t wev[5] = {};
+    void wmark(int k) {
+        if (profiling && wev[k]) cudaEventRecord(wev[k], st);
+    }
 
     lg_status fail(lg_status s, const char* fmt, ...);
     lg_status cuda(cudaError_t e, const char* what);

@@ -117,7 +117,8 @@ cudaError_t launch_render_shade(const DevScene& sc, const DevCamera& cam, const 
                                 const int32_t* counts, const int32_t* offsets, const int32_t* total,
                                 ShadowTask* tasks, int64_t task_cap, void* pixel_samples, float4* direct,
                                 float4* rgba, float4* dfilm, float4* sfilm, float4* efilm,
-                                unsigned long long* counters, int sms, cudaStream_t st);
+                                unsigned long long* counters, int sms, cudaStream_t st,
+                                cudaEvent_t* marks = nullptr);
 // Exclusive scan of n int32 (block_sums: n/1024 + 1 ints); *total = sum.
 cudaError_t launch_exclusive_scan(const int32_t* in, int64_t n, int32_t* out, int32_t* block_sums, int32_t* total,
                                   cudaStream_t st);

@@ -361,9 +361,16 @@ class Context:
         return Films(*films)
 
     def render_stats(self):
+        """(primary density samples, shadow density samples) of the last render."""
         a, b = C.c_uint64(), C.c_uint64()
-        self._ck(self.lib.lg_render_stats(self.h, C.byref(a), C.byref(b)))
+        self._ck(self.lib.lg_render_stats(self.h, C.byref(a), C.byref(b), None))
         return a.value, b.value
+
+    def shading_tasks(self) -> int:
+        """Primary samples of the last render that cast shadow rays."""
+        t = C.c_uint64()
+        self._ck(self.lib.lg_render_stats(self.h, None, None, C.byref(t)))
+        return t.value
 
     def render_frame(self, points: Sequence[np.ndarray], radius_sq: Sequence[float], opts: SceneSettings,
                      max_connect: int = 12, point_voxel_size: float = 0.0) -> Films:
