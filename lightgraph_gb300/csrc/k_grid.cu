@@ -2,9 +2,11 @@
 //
 // Grids: a dense box of voxels (what a FloatGrid's active region looks like
 // once copied to a dense array) is re-tiled into 8^3 bricks with one brick of
-// zero padding on every side, stored as FP32, FP16 or BF16. The leaf bitmap
-// marks the bricks that are leaves of the VDB tree: given explicitly, or
-// "any voxel non-zero" (a dense grid converted to a VDB keeps exactly those).
+// zero padding on every side; every cell of the bricks stores the eight
+// values of its trilinear footprint as one record, in FP32, FP16 or BF16.
+// The leaf bitmap marks the bricks that are leaves of the VDB tree: given
+// explicitly, or "any voxel non-zero" (a dense grid converted to a VDB keeps
+// exactly those).
 //
 // Environment map: EnvLight's constructor (src/Light.h:150-177) weights each
 // texel's luminance by sin(theta) and builds a Distribution2D
@@ -15,6 +17,8 @@
 
 namespace lg {
 
+// One thread per cell record: gathers the cell's eight voxel values from the
+// dense staging array (0 outside it) and writes them as one record.
 __global__ void k_pack_bricks(const float* __restrict__ dense, int dx, int dy, int dz, int ox, int oy,
                               int oz, DevGrid g, void* __restrict__ bricks) {
     const int64_t total = (int64_t)g.nb[0] * g.nb[1] * g.nb[2] * 512;
@@ -27,12 +31,32 @@ __global__ void k_pack_bricks(const float* __restrict__ dense, int dx, int dy, i
     const int x = (g.blo[0] + bx) * 8 + (l & 7) - ox;
     const int y = (g.blo[1] + by) * 8 + ((l >> 3) & 7) - oy;
     const int z = (g.blo[2] + bz) * 8 + (l >> 6) - oz;
-    float v = 0.f;
-    if ((unsigned)x < (unsigned)dx && (unsigned)y < (unsigned)dy && (unsigned)z < (unsigned)dz)
-        v = dense[((int64_t)z * dy + y) * dx + x];
-    if (g.dtype == 0) reinterpret_cast<float*>(bricks)[t] = v;
-    else if (g.dtype == 1) reinterpret_cast<__half*>(bricks)[t] = __float2half_rn(v);
-    else reinterpret_cast<__nv_bfloat16*>(bricks)[t] = __float2bfloat16_rn(v);
+    float v[8];
+#pragma unroll
+    for (int c = 0; c < 8; ++c) {
+        const int xa = x + (c & 1), ya = y + ((c >> 1) & 1), za = z + (c >> 2);
+        v[c] = ((unsigned)xa < (unsigned)dx && (unsigned)ya < (unsigned)dy && (unsigned)za < (unsigned)dz)
+                   ? dense[((int64_t)za * dy + ya) * dx + xa]
+                   : 0.f;
+    }
+    if (g.dtype == 0) {
+        float4* o = reinterpret_cast<float4*>(bricks) + 2 * t;
+        o[0] = make_float4(v[0], v[1], v[2], v[3]);
+        o[1] = make_float4(v[4], v[5], v[6], v[7]);
+    } else {
+        uint32_t w[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            if (g.dtype == 1) {
+                const __half2 h = __floats2half2_rn(v[2 * i], v[2 * i + 1]);
+                w[i] = *reinterpret_cast<const uint32_t*>(&h);
+            } else {
+                const __nv_bfloat162 h = __floats2bfloat162_rn(v[2 * i], v[2 * i + 1]);
+                w[i] = *reinterpret_cast<const uint32_t*>(&h);
+            }
+        }
+        reinterpret_cast<uint4*>(bricks)[t] = make_uint4(w[0], w[1], w[2], w[3]);
+    }
 }
 
 cudaError_t launch_pack_bricks(const float* dense, const int dims[3], const int origin[3],

@@ -21,6 +21,8 @@
 // passes the dropout depth. Random numbers come from counter-based streams
 // keyed by (seed, pixel, sample, loop iteration), so results do not depend on
 // the launch shape; the reference's render RNG depends on TBB's row split.
+#include <atomic>
+
 #include "lg_kernels.h"
 
 namespace lg {
@@ -95,7 +97,6 @@ __global__ void __launch_bounds__(128, 4) k_primary(DevScene sc, DevCamera cam, 
     const int64_t n_ps = (int64_t)cam.width * cam.height * cam.spp;
     uint32_t n_primary = 0;
     if (ps < n_ps) {
-        const int s = (int)(ps % cam.spp);
         const int64_t pix = ps / cam.spp;
         const int i = (int)(pix % cam.width), j = (int)(pix / cam.width);
         const DevGrid& G = sc.dens;
@@ -107,7 +108,7 @@ __global__ void __launch_bounds__(128, 4) k_primary(DevScene sc, DevCamera cam, 
         IRay pr;
         if (primary_ray(sc, cam, i, j, stream, pr)) {
             LeafDDA dda;
-            dda_init(dda, pr);
+            dda_init(dda, pr, G);
             float ta, tb;
             uint32_t span_ord = 0, n_iter = 0;
             bool pdrop = false;
@@ -179,8 +180,10 @@ __global__ void __launch_bounds__(128, 4) k_primary(DevScene sc, DevCamera cam, 
 
 // One thread per shadow task (grid-stride over the device-side total).
 // direct[t] = sum over lights of albedo * (sum_ls I * T_shadow / ns) * w.
-template <int DT>
-__global__ void __launch_bounds__(128, 4) k_shadow(DevScene sc, const ShadowTask* __restrict__ tasks,
+// kEnv = false leaves the environment-light branch out (no light of the
+// scene is an environment light), which frees registers for occupancy.
+template <int DT, bool kEnv>
+__global__ void __launch_bounds__(128, 8) k_shadow(DevScene sc, const ShadowTask* __restrict__ tasks,
                                                 const int32_t* __restrict__ total_ptr, int64_t task_cap,
                                                 float4* __restrict__ direct, unsigned long long* __restrict__ ctr) {
     const int64_t total = min((int64_t)*total_ptr, task_cap);
@@ -201,7 +204,7 @@ __global__ void __launch_bounds__(128, 4) k_shadow(DevScene sc, const ShadowTask
             for (int ls = 0; ls < Lk.samples; ++ls) {
                 const uint32_t sub = shadow_key(stream, tk.n, (uint32_t)k, (uint32_t)ls);
                 float ldir[3], I[3], dist;
-                if (Lk.type == 2) {
+                if (kEnv && Lk.type == 2) {
                     env_illuminate(sc.env, Lk, draw_sub(sub, kTagEnvU), draw_sub(sub, kTagEnvV), ldir, I);
                     dist = kInf;
                 } else {
@@ -212,7 +215,7 @@ __global__ void __launch_bounds__(128, 4) k_shadow(DevScene sc, const ShadowTask
                           dist * G.inv_h);
                 if (!clip_to_bbox(G, srr)) continue;
                 LeafDDA sd;
-                dda_init(sd, srr);
+                dda_init(sd, srr, G);
                 float sa, sb, tau = 0.f;
                 uint32_t sspan = 0, siter = 0;
                 bool sdrop = false;
@@ -303,6 +306,29 @@ cudaError_t launch_render_count(const DevScene& sc, const DevCamera& cam, const 
     return cudaGetLastError();
 }
 
+// Resident CTAs per SM of the k_shadow instance for (dtype, env), from the
+// occupancy calculator (once per instance; it enqueues no work, so it may run
+// while a stream is being captured).
+static int shadow_ctas_per_sm(int dtype, bool env) {
+    static std::atomic<int> cache[3][2];
+    std::atomic<int>& c = cache[dtype < 0 || dtype > 2 ? 0 : dtype][env ? 1 : 0];
+    if (c.load() == 0) {
+        int n = 0;
+        cudaError_t e;
+        if (env) {
+            e = dtype == 1   ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_shadow<1, true>, 128, 0)
+                : dtype == 2 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_shadow<2, true>, 128, 0)
+                             : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_shadow<0, true>, 128, 0);
+        } else {
+            e = dtype == 1   ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_shadow<1, false>, 128, 0)
+                : dtype == 2 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_shadow<2, false>, 128, 0)
+                             : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_shadow<0, false>, 128, 0);
+        }
+        c.store((e == cudaSuccess && n > 0) ? n : 8);
+    }
+    return c.load();
+}
+
 cudaError_t launch_render_shade(const DevScene& sc, const DevCamera& cam, const DevScatterGrid& sg,
                                 const int32_t* counts, const int32_t* offsets, const int32_t* total,
                                 ShadowTask* tasks, int64_t task_cap, void* pixel_samples, float4* direct,
@@ -323,9 +349,19 @@ cudaError_t launch_render_shade(const DevScene& sc, const DevCamera& cam, const 
     else
         k_primary<true, 0><<<blocks, 128, 0, st>>>(sc, cam, sg, nullptr, offsets, tasks, task_cap, pss, counters);
     mark(0);
-    if (sc.dens.dtype == 1) k_shadow<1><<<sms * 16, 128, 0, st>>>(sc, tasks, total, task_cap, direct, counters);
-    else if (sc.dens.dtype == 2) k_shadow<2><<<sms * 16, 128, 0, st>>>(sc, tasks, total, task_cap, direct, counters);
-    else k_shadow<0><<<sms * 16, 128, 0, st>>>(sc, tasks, total, task_cap, direct, counters);
+    bool env = false;
+    for (int k = 0; k < sc.n_lights; ++k) env = env || sc.lights[k].type == 2;
+    // one resident wave of CTAs; the threads stride over the tasks
+    const unsigned sblocks = (unsigned)sms * (unsigned)shadow_ctas_per_sm(sc.dens.dtype, env);
+    if (env) {
+        if (sc.dens.dtype == 1) k_shadow<1, true><<<sblocks, 128, 0, st>>>(sc, tasks, total, task_cap, direct, counters);
+        else if (sc.dens.dtype == 2) k_shadow<2, true><<<sblocks, 128, 0, st>>>(sc, tasks, total, task_cap, direct, counters);
+        else k_shadow<0, true><<<sblocks, 128, 0, st>>>(sc, tasks, total, task_cap, direct, counters);
+    } else {
+        if (sc.dens.dtype == 1) k_shadow<1, false><<<sblocks, 128, 0, st>>>(sc, tasks, total, task_cap, direct, counters);
+        else if (sc.dens.dtype == 2) k_shadow<2, false><<<sblocks, 128, 0, st>>>(sc, tasks, total, task_cap, direct, counters);
+        else k_shadow<0, false><<<sblocks, 128, 0, st>>>(sc, tasks, total, task_cap, direct, counters);
+    }
     mark(1);
     k_resolve<<<(unsigned)((n_pix + 127) / 128), 128, 0, st>>>(cam, offsets, counts, pss, direct, task_cap, rgba,
                                                               dfilm, sfilm, efilm);

@@ -243,17 +243,21 @@ lg_status Ctx::upload_grid(int which, const lg_grid_desc* desc, const float* val
     }
     g.h = (float)desc->voxel_size;
     g.inv_h = (float)(1.0 / desc->voxel_size);
-    // the samplers address voxels with 32-bit offsets
+    // the samplers address cell records with 32-bit indices
     if ((uint64_t)g.nb[0] * g.nb[1] * g.nb[2] * 512ull >= (1ull << 32))
         return fail(LG_ERR_INVALID, "grid too large: the padded brick box must hold fewer than 2^32 voxels");
+    for (int a = 0; a < 3; ++a) {
+        g.vlo[a] = g.blo[a] * 8;
+        g.vn[a] = (uint32_t)g.nb[a] * 8u;
+    }
     g.sy = (uint32_t)g.nb[0] * 512u;
     g.sz = (uint32_t)g.nb[0] * (uint32_t)g.nb[1] * 512u;
     const int64_t nvox = (int64_t)desc->dims[0] * desc->dims[1] * desc->dims[2];
     const int64_t nbt = (int64_t)g.nb[0] * g.nb[1] * g.nb[2];
-    const size_t esz = dtype == 0 ? 4 : 2;
+    const size_t rec = (size_t)cell_record_bytes(dtype);
     CK(staging.reserve(sizeof(float) * nvox), "grid staging alloc");
     CK(cudaMemcpyAsync(staging.p, values, sizeof(float) * nvox, cudaMemcpyHostToDevice, st), "grid upload");
-    CK(gs.bricks.reserve(esz * nbt * 512), "brick alloc");
+    CK(gs.bricks.reserve(rec * nbt * 512), "brick alloc");
     CK(gs.bits.reserve(sizeof(uint32_t) * ((nbt + 31) / 32 + 1)), "leaf bitmap alloc");
     CK(cudaMemsetAsync(gs.bits.p, 0, sizeof(uint32_t) * ((nbt + 31) / 32 + 1), st), "leaf bitmap clear");
     const uint8_t* d_mask = nullptr;
