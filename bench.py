@@ -335,8 +335,8 @@ def run_ours(args):
     ev1 = torch.cuda.Event(enable_timing=True)
     ev0.record(stream)
     buf = (C.c_double * len(STAGES))()
-    wbuf = (C.c_double * 4)()
-    wave_ms = np.zeros(4)
+    wbuf = (C.c_double * 5)()
+    wave_ms = np.zeros(5)
     for _ in range(args.steps):
         ctx.frame_device(sc.opts, sc.max_connect)
         if lib.lg_stage_times(ctx.h, buf, len(STAGES)) == 0:
@@ -382,9 +382,11 @@ def run_ours(args):
     peaks, peak_kind = measured_peaks()
     # dominant kernel: k_shadow (the shadow-ray wave of the render). Its
     # algorithmic bytes per launch: 8 taps x 4 B per shadow density sample
-    # plus the 32 B task read and 16 B result write per shading sample.
-    shadow_ms = wave_ms[2]
-    shadow_bytes = shad * 32.0 + tasks_per_frame * 48.0
+    # plus, per shading sample and light, the 4 B order entry and 32 B task
+    # read and the 16 B result write.
+    n_lights = len(sc.lights)
+    shadow_ms = wave_ms[3]
+    shadow_bytes = shad * 32.0 + tasks_per_frame * n_lights * 52.0
     achieved = shadow_bytes / (shadow_ms * 1e-3) / 1e9
     render_bytes = (prim + shad) * 32.0 + W * H * 64.0
     render_gbs = render_bytes / (stage_ms[6] * 1e-3) / 1e9
@@ -407,8 +409,8 @@ def run_ours(args):
                      "traffic": profile_traffic("k_shadow_production.txt"),
                      "algorithmic_bytes": shadow_bytes, "launch_ms": shadow_ms,
                      "samples": {"primary": prim, "shadow": shad, "shading_tasks": tasks_per_frame}},
-        "render_waves_ms": {"count_scan": wave_ms[0], "primary": wave_ms[1], "shadow": wave_ms[2],
-                            "resolve": wave_ms[3]},
+        "render_waves_ms": {"count_scan": wave_ms[0], "primary": wave_ms[1], "ray_order": wave_ms[2],
+                            "shadow": wave_ms[3], "resolve": wave_ms[4]},
         "render_stage": {"ms": float(stage_ms[6]), "algorithmic_bytes": render_bytes, "achieved_gbs": render_gbs,
                          "frac": render_gbs / peaks.get("hbm_gbs")},
         "fw_roofline": {"kernel": "k_fw_update+k_fw_panels", "bound": "fp32_alu", "n": int(ld),

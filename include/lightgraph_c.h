@@ -293,8 +293,9 @@ lg_status lg_render_stats(lg_ctx* ctx, uint64_t* primary_samples,
 lg_status lg_set_profiling(lg_ctx* ctx, int on);
 lg_status lg_stage_times(lg_ctx* ctx, double* ms, int n);
 /* The render stage of the last profiled frame split into its waves (ms):
- * primary count + scan, primary shading, shadow rays, resolve. */
-lg_status lg_render_wave_times(lg_ctx* ctx, double ms[4]);
+ * primary count + scan, primary shading, shadow-ray ordering, shadow rays,
+ * resolve. */
+lg_status lg_render_wave_times(lg_ctx* ctx, double ms[5]);
 
 /* Frame replay: when on, lg_frame_device runs the frame once, captures the
  * same launch sequence in a CUDA graph and replays it on later calls with the

@@ -68,7 +68,8 @@ cudaError_t launch_pack_bricks(const float* dense, const int dims[3], const int 
     return cudaGetLastError();
 }
 
-// One thread per brick of the box; warp ballots form the 32-bit words.
+// One thread per brick of the box; leaf bricks set their bit of the bitmap
+// (which has a one-brick margin, cleared beforehand) with an atomic OR.
 // bbox (6 ints: min xyz, max xyz brick coordinates) is reduced with atomics.
 __global__ void k_leaf_bits(const float* __restrict__ dense, int dx, int dy, int dz, int ox, int oy,
                             int oz, const uint8_t* __restrict__ leaf_mask, DevGrid g,
@@ -107,9 +108,11 @@ __global__ void k_leaf_bits(const float* __restrict__ dense, int dx, int dy, int
             }
         }
     }
-    const unsigned m = __ballot_sync(0xffffffffu, leaf);
-    if ((threadIdx.x & 31) == 0 && b < nbt) bits[b >> 5] = m;
     if (leaf) {
+        const uint32_t lin = ((uint32_t)(cz - g.blo[2] + 1) * (uint32_t)g.lby + (uint32_t)(cy - g.blo[1] + 1)) *
+                                 (uint32_t)g.lbx +
+                             (uint32_t)(cx - g.blo[0] + 1);
+        atomicOr(bits + (lin >> 5), 1u << (lin & 31u));
         atomicMin(bbox + 0, cx);
         atomicMin(bbox + 1, cy);
         atomicMin(bbox + 2, cz);

@@ -143,8 +143,8 @@ __global__ void __launch_bounds__(128, 4) k_primary(DevScene sc, DevCamera cam, 
                             tk.p[0] = p[0]; tk.p[1] = p[1]; tk.p[2] = p[2];
 #pragma unroll
                             for (int c = 0; c < 3; ++c) tk.w[c] = pT3[c] * omdT[c];
-                            tk.n = n;
-                            tk.ps = (uint32_t)ps;
+                            tk.sa = stream.a;
+                            tk.iw = shadow_iter_word(stream, n);
                             tasks[t] = tk;
                         }
 #pragma unroll
@@ -178,72 +178,160 @@ __global__ void __launch_bounds__(128, 4) k_primary(DevScene sc, DevCamera cam, 
     }
 }
 
-// One thread per shadow task (grid-stride over the device-side total).
-// direct[t] = sum over lights of albedo * (sum_ls I * T_shadow / ns) * w.
+// --- shadow-ray ordering ---------------------------------------------------
+
+__device__ __forceinline__ uint32_t spread_bits16(uint32_t v) {
+    v &= 0xFFFFu;
+    v = (v | (v << 8)) & 0x00FF00FFu;
+    v = (v | (v << 4)) & 0x0F0F0F0Fu;
+    v = (v | (v << 2)) & 0x33333333u;
+    v = (v | (v << 1)) & 0x55555555u;
+    return v;
+}
+__device__ __forceinline__ int clamp_bin(float x, int n) { return min(max((int)x, 0), n - 1); }
+
+// Key of the shadow ray of light b for the task at index-space position p.
+__device__ __forceinline__ int64_t ray_key(const RayBin& b, const float p[3], int64_t t) {
+    if (b.kind == 2) return b.key_off + (t >> b.shift);
+    int64_t uv;
+    float depth;
+    if (b.kind == 0) {
+        const float u = p[0] * b.U[0] + p[1] * b.U[1] + p[2] * b.U[2] - b.u0;
+        const float v = p[0] * b.V[0] + p[1] * b.V[1] + p[2] * b.V[2] - b.v0;
+        uv = spread_bits16((uint32_t)clamp_bin(u * b.inv_bs, b.ns)) |
+             (spread_bits16((uint32_t)clamp_bin(v * b.inv_bs, b.ns)) << 1);
+        depth = p[0] * b.D[0] + p[1] * b.D[1] + p[2] * b.D[2] - b.d0;
+    } else {
+        const float w0 = p[0] - b.O[0], w1 = p[1] - b.O[1], w2 = p[2] - b.O[2];
+        const float a0 = fabsf(w0), a1 = fabsf(w1), a2 = fabsf(w2);
+        int face;
+        float m, x, y;
+        if (a0 >= a1 && a0 >= a2) { face = w0 < 0.f; m = a0; x = w1; y = w2; }
+        else if (a1 >= a2) { face = 2 + (w1 < 0.f); m = a1; x = w0; y = w2; }
+        else { face = 4 + (w2 < 0.f); m = a2; x = w0; y = w1; }
+        const float inv = m > 0.f ? 0.5f / m : 0.f;
+        uv = (int64_t)face * b.ns * b.ns +
+             (spread_bits16((uint32_t)clamp_bin((x * inv + 0.5f) * (float)b.ns, b.ns)) |
+              (spread_bits16((uint32_t)clamp_bin((y * inv + 0.5f) * (float)b.ns, b.ns)) << 1));
+        depth = sqrtf(w0 * w0 + w1 * w1 + w2 * w2) - b.d0;
+    }
+    return b.key_off + uv * b.nd + clamp_bin(depth * b.inv_ds, b.nd);
+}
+
+// Warp-aggregated counting sort passes (lanes with equal keys share one
+// atomic). Within a key the order is whatever the atomics give; every ray's
+// result goes to its own slot, so results do not depend on it.
+__global__ void __launch_bounds__(256) k_ray_bins(const ShadowTask* __restrict__ tasks,
+                                                  const int32_t* __restrict__ total_ptr, int64_t task_cap,
+                                                  RayBins rb, int32_t* __restrict__ counts,
+                                                  int32_t* __restrict__ order) {
+    const int64_t total = min((int64_t)*total_ptr, task_cap);
+    const int lane = threadIdx.x & 31;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < total; base += stride) {
+        const int64_t t = base + threadIdx.x;
+        const bool valid = t < total;
+        float p[3] = {0.f, 0.f, 0.f};
+        if (valid) {
+            const float4 q = __ldg(reinterpret_cast<const float4*>(tasks + t));
+            p[0] = q.x;
+            p[1] = q.y;
+            p[2] = q.z;
+        }
+        for (int k = 0; k < rb.n; ++k) {
+            const unsigned long long key = valid ? (unsigned long long)ray_key(rb.b[k], p, t) : ~0ull;
+            const unsigned grp = __match_any_sync(0xffffffffu, key);
+            if (!valid) continue;
+            const int leader = __ffs(grp) - 1;
+            if (order == nullptr) {
+                if (lane == leader) atomicAdd(counts + key, __popc(grp));
+            } else {
+                int32_t pos = 0;
+                if (lane == leader) pos = atomicAdd(counts + key, __popc(grp));
+                pos = __shfl_sync(grp, pos, leader);
+                order[pos + __popc(grp & ((1u << lane) - 1u))] = (int32_t)t;
+            }
+        }
+    }
+}
+
+cudaError_t launch_ray_bins(const ShadowTask* tasks, const int32_t* total, int64_t task_cap, const RayBins& rb,
+                            int32_t* counts, int32_t* order, int sms, cudaStream_t st) {
+    k_ray_bins<<<(unsigned)sms * 8u, 256, 0, st>>>(tasks, total, task_cap, rb, counts, order);
+    ++g_launch_counter;
+    return cudaGetLastError();
+}
+
+// --- shadow rays -------------------------------------------------------------
+
+// One thread per (light k, ordered slot r): the shadow rays of light k (all
+// its samples) from task order[k * total + r]. The threads in flight march
+// neighbouring rays. direct[k * task_cap + t] = albedo * (sum_ls I * T / ns) * w.
 // kEnv = false leaves the environment-light branch out (no light of the
 // scene is an environment light), which frees registers for occupancy.
 template <int DT, bool kEnv>
 __global__ void __launch_bounds__(128, 8) k_shadow(DevScene sc, const ShadowTask* __restrict__ tasks,
                                                 const int32_t* __restrict__ total_ptr, int64_t task_cap,
-                                                float4* __restrict__ direct, unsigned long long* __restrict__ ctr) {
+                                                const int32_t* __restrict__ order, float4* __restrict__ direct,
+                                                unsigned long long* __restrict__ ctr) {
     const int64_t total = min((int64_t)*total_ptr, task_cap);
+    const int64_t n_rays = total * sc.n_lights;
     const DevGrid& G = sc.dens;
     const DevShader& sh = sc.sh;
     const float step1 = sc.step1, cutoff = sc.cutoff;
     const float scale = sh.dS * sh.shadowDS;
     uint32_t n_shadow = 0;
-    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total;
-         t += (int64_t)gridDim.x * blockDim.x) {
+    for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n_rays;
+         r += (int64_t)gridDim.x * blockDim.x) {
+        const int k = (int)(r / total);
+        const int64_t t = order[r];
         const ShadowTask tk = tasks[t];
-        const Stream stream = make_stream(sc.seed, kDomainPixel | (uint64_t)tk.ps);
-        const float pw[3] = {tk.p[0] * G.h + G.wo[0], tk.p[1] * G.h + G.wo[1], tk.p[2] * G.h + G.wo[2]};
-        float acc[3] = {0.f, 0.f, 0.f};
-        for (int k = 0; k < sc.n_lights; ++k) {
-            const DevLight& Lk = sc.lights[k];
-            float lum[3] = {0.f, 0.f, 0.f};
-            for (int ls = 0; ls < Lk.samples; ++ls) {
-                const uint32_t sub = shadow_key(stream, tk.n, (uint32_t)k, (uint32_t)ls);
-                float ldir[3], I[3], dist;
-                if (kEnv && Lk.type == 2) {
-                    env_illuminate(sc.env, Lk, draw_sub(sub, kTagEnvU), draw_sub(sub, kTagEnvV), ldir, I);
-                    dist = kInf;
-                } else {
-                    illuminate(Lk, pw, ldir, I, dist);
-                }
-                IRay srr;
-                make_iray(srr, tk.p[0], tk.p[1], tk.p[2], -ldir[0], -ldir[1], -ldir[2], kDelta * G.inv_h,
-                          dist * G.inv_h);
-                if (!clip_to_bbox(G, srr)) continue;
-                LeafDDA sd;
-                dda_init(sd, srr, G);
-                float sa, sb, tau = 0.f;
-                uint32_t sspan = 0, siter = 0;
-                bool sdrop = false;
-                while (!sdrop && next_span(G, sd, sa, sb)) {
-                    float sStep = jitter_step(step1, draw_sub(sub, kTagShadowSpan | sspan));
-                    ++sspan;
-                    for (float sT = step1 * ceilf(sa / step1); sT <= sb && sT + sStep > sT;) {
-                        const uint32_t q = siter++;
-                        const float rs = fminf(sample_index_t<DT>(G, srr.e[0] + sT * srr.d[0], srr.e[1] + sT * srr.d[1],
-                                                            srr.e[2] + sT * srr.d[2]) * scale,
-                                               sh.dMax);
-                        if (rs < cutoff) { sT += sStep; continue; }
-                        tau += rs * sStep;
-                        if (tau > sh.tau_drop) { sdrop = true; break; }
-                        sStep = jitter_step(step1, draw_sub(sub, kTagShadowStep | q));
-                        sT += sStep;
-                    }
-                }
-                n_shadow += siter;
-                if (sdrop) continue;
-#pragma unroll
-                for (int c = 0; c < 3; ++c) lum[c] += I[c] * __expf(-sh.a[c] * tau);
+        const DevLight& Lk = sc.lights[k];
+        float lum[3] = {0.f, 0.f, 0.f};
+        for (int ls = 0; ls < Lk.samples; ++ls) {
+            const uint32_t sub = shadow_key_from(tk.sa, tk.iw, (uint32_t)k, (uint32_t)ls);
+            float ldir[3], I[3], dist;
+            if (kEnv && Lk.type == 2) {
+                env_illuminate(sc.env, Lk, draw_sub(sub, kTagEnvU), draw_sub(sub, kTagEnvV), ldir, I);
+                dist = kInf;
+            } else {
+                const float pw[3] = {tk.p[0] * G.h + G.wo[0], tk.p[1] * G.h + G.wo[1], tk.p[2] * G.h + G.wo[2]};
+                illuminate(Lk, pw, ldir, I, dist);
             }
-            const float inv_ns = 1.f / (float)Lk.samples;
+            IRay srr;
+            make_iray(srr, tk.p[0], tk.p[1], tk.p[2], -ldir[0], -ldir[1], -ldir[2], kDelta * G.inv_h,
+                      dist * G.inv_h);
+            if (!clip_to_bbox(G, srr)) continue;  // the reference skips the light sample
+            LeafDDA sd;
+            dda_init(sd, srr, G);
+            float sa, sb, tau = 0.f;
+            uint32_t sspan = 0, siter = 0;
+            bool sdrop = false;
+            while (!sdrop && next_span(G, sd, sa, sb)) {
+                float sStep = jitter_step(step1, draw_sub(sub, kTagShadowSpan | sspan));
+                ++sspan;
+                for (float sT = step1 * ceilf(sa / step1); sT <= sb && sT + sStep > sT;) {
+                    const uint32_t q = siter++;
+                    const float rs = fminf(sample_index_t<DT>(G, srr.e[0] + sT * srr.d[0], srr.e[1] + sT * srr.d[1],
+                                                              srr.e[2] + sT * srr.d[2]) * scale,
+                                           sh.dMax);
+                    if (rs < cutoff) { sT += sStep; continue; }
+                    tau += rs * sStep;
+                    if (tau > sh.tau_drop) { sdrop = true; break; }
+                    sStep = jitter_step(step1, draw_sub(sub, kTagShadowStep | q));
+                    sT += sStep;
+                }
+            }
+            n_shadow += siter;
+            if (sdrop) continue;
 #pragma unroll
-            for (int c = 0; c < 3; ++c) acc[c] += sh.albedo[c] * (lum[c] * inv_ns) * tk.w[c];
+            for (int c = 0; c < 3; ++c) lum[c] += I[c] * __expf(-sh.a[c] * tau);
         }
-        direct[t] = make_float4(acc[0], acc[1], acc[2], 0.f);
+        const float inv_ns = 1.f / (float)Lk.samples;
+        float o[3];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) o[c] = sh.albedo[c] * (lum[c] * inv_ns) * tk.w[c];
+        direct[(int64_t)k * task_cap + t] = make_float4(o[0], o[1], o[2], 0.f);
     }
     if (ctr) {
         unsigned long long q = n_shadow;
@@ -253,11 +341,12 @@ __global__ void __launch_bounds__(128, 8) k_shadow(DevScene sc, const ShadowTask
     }
 }
 
-// One thread per pixel: the antialiasing average in sample order.
+// One thread per pixel: the antialiasing average in sample order. A task's
+// direct light is the sum of its lights' contributions in light order.
 __global__ void __launch_bounds__(128) k_resolve(DevCamera cam, const int32_t* __restrict__ offsets,
                                                  const int32_t* __restrict__ counts,
                                                  const PixelSample* __restrict__ pss,
-                                                 const float4* __restrict__ direct, int64_t task_cap,
+                                                 const float4* __restrict__ direct, int n_lights, int64_t task_cap,
                                                  float4* __restrict__ rgba, float4* __restrict__ dfilm,
                                                  float4* __restrict__ sfilm, float4* __restrict__ efilm) {
     const int64_t pix = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -271,10 +360,16 @@ __global__ void __launch_bounds__(128) k_resolve(DevCamera cam, const int32_t* _
         float d[3] = {0.f, 0.f, 0.f};
         const int64_t b = offsets[ps], e = min((int64_t)b + counts[ps], task_cap);
         for (int64_t t = b; t < e; ++t) {
-            const float4 v = direct[t];
-            d[0] += v.x;
-            d[1] += v.y;
-            d[2] += v.z;
+            float acc[3] = {0.f, 0.f, 0.f};
+            for (int k = 0; k < n_lights; ++k) {
+                const float4 v = direct[(int64_t)k * task_cap + t];
+                acc[0] += v.x;
+                acc[1] += v.y;
+                acc[2] += v.z;
+            }
+            d[0] += acc[0];
+            d[1] += acc[1];
+            d[2] += acc[2];
         }
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
@@ -331,8 +426,8 @@ static int shadow_ctas_per_sm(int dtype, bool env) {
 
 cudaError_t launch_render_shade(const DevScene& sc, const DevCamera& cam, const DevScatterGrid& sg,
                                 const int32_t* counts, const int32_t* offsets, const int32_t* total,
-                                ShadowTask* tasks, int64_t task_cap, void* pixel_samples, float4* direct,
-                                float4* rgba, float4* dfilm, float4* sfilm, float4* efilm,
+                                ShadowTask* tasks, int64_t task_cap, void* pixel_samples, const RayOrder& ro,
+                                float4* direct, float4* rgba, float4* dfilm, float4* sfilm, float4* efilm,
                                 unsigned long long* counters, int sms, cudaStream_t st, cudaEvent_t* marks) {
     const int64_t n_ps = (int64_t)cam.width * cam.height * cam.spp;
     const int64_t n_pix = (int64_t)cam.width * cam.height;
@@ -342,31 +437,46 @@ cudaError_t launch_render_shade(const DevScene& sc, const DevCamera& cam, const 
     auto mark = [&](int k) {
         if (marks && marks[k]) cudaEventRecord(marks[k], st);
     };
+    cudaError_t e;
     if (sc.dens.dtype == 1)
         k_primary<true, 1><<<blocks, 128, 0, st>>>(sc, cam, sg, nullptr, offsets, tasks, task_cap, pss, counters);
     else if (sc.dens.dtype == 2)
         k_primary<true, 2><<<blocks, 128, 0, st>>>(sc, cam, sg, nullptr, offsets, tasks, task_cap, pss, counters);
     else
         k_primary<true, 0><<<blocks, 128, 0, st>>>(sc, cam, sg, nullptr, offsets, tasks, task_cap, pss, counters);
+    ++g_launch_counter;
     mark(0);
-    bool env = false;
-    for (int k = 0; k < sc.n_lights; ++k) env = env || sc.lights[k].type == 2;
-    // one resident wave of CTAs; the threads stride over the tasks
-    const unsigned sblocks = (unsigned)sms * (unsigned)shadow_ctas_per_sm(sc.dens.dtype, env);
-    if (env) {
-        if (sc.dens.dtype == 1) k_shadow<1, true><<<sblocks, 128, 0, st>>>(sc, tasks, total, task_cap, direct, counters);
-        else if (sc.dens.dtype == 2) k_shadow<2, true><<<sblocks, 128, 0, st>>>(sc, tasks, total, task_cap, direct, counters);
-        else k_shadow<0, true><<<sblocks, 128, 0, st>>>(sc, tasks, total, task_cap, direct, counters);
-    } else {
-        if (sc.dens.dtype == 1) k_shadow<1, false><<<sblocks, 128, 0, st>>>(sc, tasks, total, task_cap, direct, counters);
-        else if (sc.dens.dtype == 2) k_shadow<2, false><<<sblocks, 128, 0, st>>>(sc, tasks, total, task_cap, direct, counters);
-        else k_shadow<0, false><<<sblocks, 128, 0, st>>>(sc, tasks, total, task_cap, direct, counters);
+    // order the shadow rays: count keys, scan, scatter task indices
+    if (ro.rb.n > 0) {
+        if ((e = cudaMemsetAsync(ro.key_counts, 0, sizeof(int32_t) * ro.n_keys, st)) != cudaSuccess) return e;
+        if ((e = launch_ray_bins(tasks, total, task_cap, ro.rb, ro.key_counts, nullptr, sms, st)) != cudaSuccess)
+            return e;
+        if ((e = launch_exclusive_scan(ro.key_counts, ro.n_keys, ro.key_offsets, ro.key_scan, ro.key_total, st)) !=
+            cudaSuccess)
+            return e;
+        if ((e = launch_ray_bins(tasks, total, task_cap, ro.rb, ro.key_offsets, ro.order, sms, st)) != cudaSuccess)
+            return e;
     }
     mark(1);
-    k_resolve<<<(unsigned)((n_pix + 127) / 128), 128, 0, st>>>(cam, offsets, counts, pss, direct, task_cap, rgba,
-                                                              dfilm, sfilm, efilm);
+    bool env = false;
+    for (int k = 0; k < sc.n_lights; ++k) env = env || sc.lights[k].type == 2;
+    // one resident wave of CTAs; the threads stride over the rays
+    const unsigned sblocks = (unsigned)sms * (unsigned)shadow_ctas_per_sm(sc.dens.dtype, env);
+    if (env) {
+        if (sc.dens.dtype == 1) k_shadow<1, true><<<sblocks, 128, 0, st>>>(sc, tasks, total, task_cap, ro.order, direct, counters);
+        else if (sc.dens.dtype == 2) k_shadow<2, true><<<sblocks, 128, 0, st>>>(sc, tasks, total, task_cap, ro.order, direct, counters);
+        else k_shadow<0, true><<<sblocks, 128, 0, st>>>(sc, tasks, total, task_cap, ro.order, direct, counters);
+    } else {
+        if (sc.dens.dtype == 1) k_shadow<1, false><<<sblocks, 128, 0, st>>>(sc, tasks, total, task_cap, ro.order, direct, counters);
+        else if (sc.dens.dtype == 2) k_shadow<2, false><<<sblocks, 128, 0, st>>>(sc, tasks, total, task_cap, ro.order, direct, counters);
+        else k_shadow<0, false><<<sblocks, 128, 0, st>>>(sc, tasks, total, task_cap, ro.order, direct, counters);
+    }
+    ++g_launch_counter;
     mark(2);
-    g_launch_counter += 3;
+    k_resolve<<<(unsigned)((n_pix + 127) / 128), 128, 0, st>>>(cam, offsets, counts, pss, direct, sc.n_lights,
+                                                              task_cap, rgba, dfilm, sfilm, efilm);
+    ++g_launch_counter;
+    mark(3);
     return cudaGetLastError();
 }
 

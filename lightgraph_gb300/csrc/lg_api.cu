@@ -108,6 +108,82 @@ static void post_rotate(double M[3][3], int axis, double ang) {
 }
 
 // PerspectiveCamera as main.cc:96-102 builds it (src/Renderer.h:148-171,232-239).
+// Shadow-ray ordering keys of every light of the scene (see RayBin): about
+// 8 x 8 voxel (u, v) bins for distant lights, a cube map of about 4 voxels per
+// bin at the far side of the leaf bbox (at most 128^2 per face) for point
+// lights, and depth bins of about 16 voxels (at most 32).
+static RayBins ray_bins(const DevScene& sc, int64_t cap) {
+    RayBins rb{};
+    rb.n = sc.n_lights;
+    const DevGrid& G = sc.dens;
+    double corner[8][3];
+    for (int c = 0; c < 8; ++c)
+        for (int a = 0; a < 3; ++a) corner[c][a] = ((c >> a) & 1) ? G.bbmax[a] : G.bbmin[a];
+    auto dot = [](const double* x, const double* y) { return x[0] * y[0] + x[1] * y[1] + x[2] * y[2]; };
+    auto depth_bins = [](RayBin& b, double lo, double hi) {
+        const double range = std::max(hi - lo, 1e-3);
+        b.nd = (int)std::min(32.0, std::max(1.0, std::ceil(range / 16.0)));
+        b.d0 = (float)lo;
+        b.inv_ds = (float)(b.nd / range);
+    };
+    int64_t off = 0;
+    for (int k = 0; k < sc.n_lights; ++k) {
+        RayBin& b = rb.b[k];
+        const DevLight& L = sc.lights[k];
+        if (L.type == 0) {
+            b.kind = 0;
+            double D[3] = {-(double)L.dir[0], -(double)L.dir[1], -(double)L.dir[2]};
+            const double nD = std::sqrt(dot(D, D));
+            for (double& x : D) x /= nD > 0 ? nD : 1.0;
+            int m = 0;
+            for (int a = 1; a < 3; ++a)
+                if (std::fabs(D[a]) < std::fabs(D[m])) m = a;
+            double e[3] = {0, 0, 0};
+            e[m] = 1.0;
+            double U[3] = {D[1] * e[2] - D[2] * e[1], D[2] * e[0] - D[0] * e[2], D[0] * e[1] - D[1] * e[0]};
+            const double nU = std::sqrt(dot(U, U));
+            for (double& x : U) x /= nU;
+            const double V[3] = {D[1] * U[2] - D[2] * U[1], D[2] * U[0] - D[0] * U[2], D[0] * U[1] - D[1] * U[0]};
+            double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+            for (int c = 0; c < 8; ++c) {
+                const double q[3] = {dot(corner[c], U), dot(corner[c], V), dot(corner[c], D)};
+                for (int a = 0; a < 3; ++a) { lo[a] = std::min(lo[a], q[a]); hi[a] = std::max(hi[a], q[a]); }
+            }
+            const double range = std::max({hi[0] - lo[0], hi[1] - lo[1], 1e-3});
+            b.ns = 1;
+            while (b.ns < 128 && b.ns * 8.0 < range) b.ns *= 2;
+            b.inv_bs = (float)(b.ns / range);
+            b.u0 = (float)lo[0];
+            b.v0 = (float)lo[1];
+            for (int a = 0; a < 3; ++a) { b.U[a] = (float)U[a]; b.V[a] = (float)V[a]; b.D[a] = (float)D[a]; }
+            depth_bins(b, lo[2], hi[2]);
+            b.nkeys = (int64_t)b.ns * b.ns * b.nd;
+        } else if (L.type == 1) {
+            b.kind = 1;
+            double O[3];
+            for (int a = 0; a < 3; ++a) O[a] = ((double)L.pos[a] - G.wo[a]) * G.inv_h;
+            double dmax = 0.0;
+            for (int c = 0; c < 8; ++c) {
+                const double w[3] = {corner[c][0] - O[0], corner[c][1] - O[1], corner[c][2] - O[2]};
+                dmax = std::max(dmax, std::sqrt(dot(w, w)));
+            }
+            b.ns = 4;
+            while (b.ns < 128 && b.ns * 4.0 < dmax) b.ns *= 2;
+            for (int a = 0; a < 3; ++a) b.O[a] = (float)O[a];
+            depth_bins(b, 0.0, dmax);
+            b.nkeys = 6 * (int64_t)b.ns * b.ns * b.nd;
+        } else {
+            b.kind = 2;
+            b.shift = 0;
+            while ((cap >> b.shift) > 65536) ++b.shift;
+            b.nkeys = (cap >> b.shift) + 1;
+        }
+        b.key_off = off;
+        off += b.nkeys;
+    }
+    return rb;
+}
+
 static DevCamera make_camera(const lg_camera& c) {
     const double d2r = 3.14159265358979323846 / 180.0;
     double M[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
@@ -195,7 +271,7 @@ extern "C" lg_status lg_destroy(lg_ctx* handle) {
     if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
     for (int k = 0; k <= Ctx::kStages; ++k)
         if (ctx->ev[k]) cudaEventDestroy(ctx->ev[k]);
-    for (int k = 0; k < 5; ++k)
+    for (int k = 0; k <= Ctx::kWaves; ++k)
         if (ctx->wev[k]) cudaEventDestroy(ctx->wev[k]);
     cudaStreamDestroy(ctx->st);
     delete ctx;
@@ -258,8 +334,12 @@ lg_status Ctx::upload_grid(int which, const lg_grid_desc* desc, const float* val
     CK(staging.reserve(sizeof(float) * nvox), "grid staging alloc");
     CK(cudaMemcpyAsync(staging.p, values, sizeof(float) * nvox, cudaMemcpyHostToDevice, st), "grid upload");
     CK(gs.bricks.reserve(rec * nbt * 512), "brick alloc");
-    CK(gs.bits.reserve(sizeof(uint32_t) * ((nbt + 31) / 32 + 1)), "leaf bitmap alloc");
-    CK(cudaMemsetAsync(gs.bits.p, 0, sizeof(uint32_t) * ((nbt + 31) / 32 + 1), st), "leaf bitmap clear");
+    g.lbx = g.nb[0] + 2;
+    g.lby = g.nb[1] + 2;
+    g.nbits = (uint32_t)((int64_t)g.lbx * g.lby * (g.nb[2] + 2));
+    const size_t bit_words = (size_t)g.nbits / 32 + 1;
+    CK(gs.bits.reserve(sizeof(uint32_t) * bit_words), "leaf bitmap alloc");
+    CK(cudaMemsetAsync(gs.bits.p, 0, sizeof(uint32_t) * bit_words, st), "leaf bitmap clear");
     const uint8_t* d_mask = nullptr;
     if (desc->leaf_mask) {
         const int64_t nl = (int64_t)nleaf[0] * nleaf[1] * nleaf[2];
@@ -992,23 +1072,51 @@ lg_status Ctx::render(const lg_camera* c) {
     CK(launch_exclusive_scan(d_ps_count.as<int32_t>(), n_ps, d_ps_offset.as<int32_t>(), d_ps_scan.as<int32_t>(),
                              d_ps_total.as<int32_t>(), st), "render scan");
     wmark(1);
+    const int64_t n_lights = std::max(sc.n_lights, 1);
     if (!capturing) {
-        // size the shadow-task buffer from this frame's count (a captured
+        // size the shadow-task buffers from this frame's count (a captured
         // replay reuses the capacity of the run it was captured after)
         int32_t total = 0;
         CK(cudaMemcpyAsync(&total, d_ps_total.p, sizeof total, cudaMemcpyDeviceToHost, st), "render total");
         CK(cudaStreamSynchronize(st), "render total sync");
         if (total < 0) return fail(LG_ERR_INVALID, "more than 2^31 shading samples in one frame");
+        if ((int64_t)total * n_lights > INT32_MAX)
+            return fail(LG_ERR_INVALID, "more than 2^31 shadow-ray groups in one frame");
         CK(d_tasks.reserve(sizeof(ShadowTask) * std::max<int64_t>(total, 1)), "shadow task alloc");
-        CK(d_task_direct.reserve(sizeof(float4) * std::max<int64_t>(total, 1)), "shadow task alloc");
     }
+    const int64_t cap = std::min<int64_t>((int64_t)(d_tasks.bytes / sizeof(ShadowTask)), INT32_MAX / n_lights);
+    RayOrder ro{};
+    ro.rb = ray_bins(sc, cap);
+    ro.n_keys = 0;
+    for (int k = 0; k < ro.rb.n; ++k) ro.n_keys += ro.rb.b[k].nkeys;
+    const size_t order_bytes = sizeof(int32_t) * (size_t)(n_lights * cap);
+    const size_t direct_bytes = sizeof(float4) * (size_t)(n_lights * cap);
+    const size_t key_bytes = sizeof(int32_t) * (size_t)std::max<int64_t>(ro.n_keys, 1);
+    const size_t scan_bytes = sizeof(int32_t) * (size_t)(std::max<int64_t>(ro.n_keys, 1) / 1024 + 2);
+    if (!capturing) {
+        CK(d_task_direct.reserve(direct_bytes), "shadow task alloc");
+        CK(d_ray_order.reserve(order_bytes), "ray order alloc");
+        CK(d_ray_counts.reserve(key_bytes), "ray order alloc");
+        CK(d_ray_offsets.reserve(key_bytes), "ray order alloc");
+        CK(d_ray_scan.reserve(scan_bytes), "ray order alloc");
+        CK(d_ray_total.reserve(sizeof(int32_t) * 2), "ray order alloc");
+    } else if (d_task_direct.bytes < direct_bytes || d_ray_order.bytes < order_bytes ||
+               d_ray_counts.bytes < key_bytes || d_ray_offsets.bytes < key_bytes || d_ray_scan.bytes < scan_bytes ||
+               d_ray_total.bytes < sizeof(int32_t) * 2) {
+        return fail(LG_ERR_STATE, "render buffers changed size during graph capture");
+    }
+    ro.key_counts = d_ray_counts.as<int32_t>();
+    ro.key_offsets = d_ray_offsets.as<int32_t>();
+    ro.key_scan = d_ray_scan.as<int32_t>();
+    ro.key_total = d_ray_total.as<int32_t>();
+    ro.order = d_ray_order.as<int32_t>();
     int sms = 0;
     CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device), "device query");
-    const int64_t cap = (int64_t)(d_tasks.bytes / sizeof(ShadowTask));
     CK(launch_render_shade(sc, cam, sg, d_ps_count.as<int32_t>(), d_ps_offset.as<int32_t>(), d_ps_total.as<int32_t>(),
-                           d_tasks.as<ShadowTask>(), cap, d_ps_data.p, d_task_direct.as<float4>(), d_rgba.as<float4>(),
-                           d_direct.as<float4>(), d_scatter.as<float4>(), d_emission.as<float4>(),
-                           d_counters.as<unsigned long long>(), sms, st, profiling ? wev + 2 : nullptr),
+                           d_tasks.as<ShadowTask>(), cap, d_ps_data.p, ro, d_task_direct.as<float4>(),
+                           d_rgba.as<float4>(), d_direct.as<float4>(), d_scatter.as<float4>(),
+                           d_emission.as<float4>(), d_counters.as<unsigned long long>(), sms, st,
+                           profiling ? wev + 2 : nullptr),
        "render");
     return LG_OK;
 }
@@ -1137,13 +1245,13 @@ lg_status Ctx::frame_enqueue(double point_voxel_size, const lg_camera* camera) {
     return s;
 }
 
-extern "C" lg_status lg_render_wave_times(lg_ctx* handle, double ms[4]) {
+extern "C" lg_status lg_render_wave_times(lg_ctx* handle, double ms[5]) {
     Ctx* ctx = reinterpret_cast<Ctx*>(handle);
     GUARD(ctx);
-    if (!ctx->ev_recorded || !ctx->wev[4]) return ctx->fail(LG_ERR_STATE, "no profiled frame");
+    if (!ctx->ev_recorded || !ctx->wev[Ctx::kWaves]) return ctx->fail(LG_ERR_STATE, "no profiled frame");
     if (!ms) return ctx->fail(LG_ERR_INVALID, "null output");
-    CK(cudaEventSynchronize(ctx->wev[4]), "event sync");
-    for (int k = 0; k < 4; ++k) {
+    CK(cudaEventSynchronize(ctx->wev[Ctx::kWaves]), "event sync");
+    for (int k = 0; k < Ctx::kWaves; ++k) {
         float t = 0.f;
         CK(cudaEventElapsedTime(&t, ctx->wev[k], ctx->wev[k + 1]), "event time");
         ms[k] = t;
@@ -1198,7 +1306,7 @@ extern "C" lg_status lg_set_profiling(lg_ctx* handle, int on) {
     GUARD(ctx);
     if (on && !ctx->ev[0]) {
         for (int k = 0; k <= Ctx::kStages; ++k) CK(cudaEventCreate(&ctx->ev[k]), "event create");
-        for (int k = 0; k < 5; ++k) CK(cudaEventCreate(&ctx->wev[k]), "event create");
+        for (int k = 0; k <= Ctx::kWaves; ++k) CK(cudaEventCreate(&ctx->wev[k]), "event create");
     }
     ctx->profiling = on != 0;
     ctx->graph_valid = false;

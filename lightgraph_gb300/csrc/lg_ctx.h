@@ -128,6 +128,8 @@ struct Ctx {
     int film_w = 0, film_h = 0;
     DevBuf d_rgba, d_direct, d_scatter, d_emission, d_counters;
     DevBuf d_ps_count, d_ps_offset, d_ps_scan, d_ps_total, d_ps_data, d_tasks, d_task_direct;
+    // shadow-ray ordering: key histogram, its scan, the ordered task indices
+    DevBuf d_ray_counts, d_ray_offsets, d_ray_scan, d_ray_total, d_ray_order;
     bool capturing = false;  // inside a CUDA graph capture: no host syncs
 
     // stage timing: events recorded on the stream around each stage of a frame
@@ -138,8 +140,9 @@ struct Ctx {
     void mark(int k) {
         if (profiling && ev[k]) cudaEventRecord(ev[k], st);
     }
-    // render waves: count + scan, primary, shadow, resolve
-    cudaEvent_t wev[5] = {};
+    // render waves: count + scan, primary, ray ordering, shadow, resolve
+    static constexpr int kWaves = 5;
+    cudaEvent_t wev[kWaves + 1] = {};
     void wmark(int k) {
         if (profiling && wev[k]) cudaEventRecord(wev[k], st);
     }

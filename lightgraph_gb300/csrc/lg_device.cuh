@@ -45,6 +45,12 @@ struct DevGrid {
     float bbmax[3] = {0.f, 0.f, 0.f};    // ... max leaf origin + 8
     int has_leaves = 0;
     uint32_t sy = 0, sz = 0;             // record strides of one brick step in y and z
+    // The leaf bitmap covers the brick box plus a margin of one brick on
+    // every side (bits 0), so a walker one cell off the box reads "no leaf"
+    // without per-axis bounds checks: bit ((z + 1) * lby + y + 1) * lbx + x + 1
+    // for box brick (x, y, z).
+    int lbx = 0, lby = 0;                // bitmap cells per row and per column (nb + 2)
+    uint32_t nbits = 0;                  // bitmap cells
 };
 
 // Bytes of one cell record for storage type dtype.
@@ -128,14 +134,10 @@ __device__ __forceinline__ float sample_world(const DevGrid& g, float wx, float 
                         (wz - g.wo[2]) * g.inv_h);
 }
 
-// Leaf test for brick (bx, by, bz) relative to the box's first brick (false
-// outside the box).
-__device__ __forceinline__ bool is_leaf(const DevGrid& g, int bx, int by, int bz) {
-    if ((unsigned)bx >= (unsigned)g.nb[0] || (unsigned)by >= (unsigned)g.nb[1] ||
-        (unsigned)bz >= (unsigned)g.nb[2])
-        return false;
-    const uint32_t b = ((uint32_t)bz * (uint32_t)g.nb[1] + (uint32_t)by) * (uint32_t)g.nb[0] + (uint32_t)bx;
-    return (__ldg(g.leafbits + (b >> 5)) >> (b & 31)) & 1u;
+// Leaf test for bitmap cell lin (false outside the bitmap).
+__device__ __forceinline__ bool is_leaf(const DevGrid& g, int lin) {
+    if ((unsigned)lin >= g.nbits) return false;
+    return (__ldg(g.leafbits + ((unsigned)lin >> 5)) >> ((unsigned)lin & 31u)) & 1u;
 }
 
 // ---------------------------------------------------------------------------
@@ -180,21 +182,23 @@ __device__ __forceinline__ bool clip_to_bbox(const DevGrid& g, IRay& r) {
 }
 
 // Per-axis state is kept in scalars (no runtime-indexed arrays), so the
-// walker lives in registers. Cells are bricks, numbered relative to the box's
-// first brick.
+// walker lives in registers. The current cell is its bitmap index lin; a step
+// along an axis adds that axis's increment (+-1, +-lbx, +-lbx * lby).
 struct LeafDDA {
     float t, tmax;
     float nx, ny, nz;   // next crossing time per axis
     float dx, dy, dz;   // crossing interval per axis
-    int cx, cy, cz;     // current leaf cell
-    int sx, sy, sz;     // cell step per axis
+    int lin;            // current leaf cell (bitmap index)
+    int ix, iy, iz;     // bitmap increment of one step per axis
     bool open;          // a span has started
     float start;        // its start time
     bool done;
 };
 
-__device__ __forceinline__ void dda_axis(float e, float d, float inv, float t0, int blo, int& c, int& step,
-                                         float& next, float& delta) {
+// Cell coordinate of the ray start along one axis (bitmap coordinates), the
+// step direction, the first crossing time and the crossing interval.
+__device__ __forceinline__ int dda_axis(float e, float d, float inv, float t0, int blo, int& step, float& next,
+                                        float& delta) {
     const float p = e + t0 * d;
     const int ca = ((int)floorf(p)) >> 3;
     if (d == 0.f) {
@@ -210,7 +214,7 @@ __device__ __forceinline__ void dda_axis(float e, float d, float inv, float t0, 
         next = t0 + ((float)(ca * 8) - p) * inv;
         delta = -8.f * inv;
     }
-    c = ca - blo;
+    return ca - blo + 1;
 }
 
 __device__ __forceinline__ void dda_init(LeafDDA& s, const IRay& r, const DevGrid& g) {
@@ -219,15 +223,24 @@ __device__ __forceinline__ void dda_init(LeafDDA& s, const IRay& r, const DevGri
     s.open = false;
     s.start = 0.f;
     s.done = false;
-    dda_axis(r.e[0], r.d[0], r.inv[0], r.t0, g.blo[0], s.cx, s.sx, s.nx, s.dx);
-    dda_axis(r.e[1], r.d[1], r.inv[1], r.t0, g.blo[1], s.cy, s.sy, s.ny, s.dy);
-    dda_axis(r.e[2], r.d[2], r.inv[2], r.t0, g.blo[2], s.cz, s.sz, s.nz, s.dz);
+    int sx, sy, sz;
+    const int cx = dda_axis(r.e[0], r.d[0], r.inv[0], r.t0, g.blo[0], sx, s.nx, s.dx);
+    const int cy = dda_axis(r.e[1], r.d[1], r.inv[1], r.t0, g.blo[1], sy, s.ny, s.dy);
+    const int cz = dda_axis(r.e[2], r.d[2], r.inv[2], r.t0, g.blo[2], sz, s.nz, s.dz);
+    const bool in = (unsigned)cx < (unsigned)g.lbx && (unsigned)cy < (unsigned)g.lby &&
+                    (unsigned)cz < (unsigned)(g.nb[2] + 2);
+    // a start cell off the bitmap (not reached by rays clipped to the leaf
+    // bbox) is mapped past its end, where every cell reads "no leaf"
+    s.lin = in ? (cz * g.lby + cy) * g.lbx + cx : (int)g.nbits;
+    s.ix = sx;
+    s.iy = sy * g.lbx;
+    s.iz = sz * g.lbx * g.lby;
 }
 
 // Next span [ta, tb] of consecutive leaf cells with tb - ta > kDelta.
 __device__ __forceinline__ bool next_span(const DevGrid& g, LeafDDA& s, float& ta, float& tb) {
     while (!s.done) {
-        const bool leaf = is_leaf(g, s.cx, s.cy, s.cz);
+        const bool leaf = is_leaf(g, s.lin);
         if (leaf) {
             if (!s.open) { s.open = true; s.start = s.t; }
         } else if (s.open) {
@@ -240,9 +253,9 @@ __device__ __forceinline__ bool next_span(const DevGrid& g, LeafDDA& s, float& t
         const bool ay = !(s.nx < s.ny) && (s.ny < s.nz);
         const bool az = !ax && !ay;
         s.t = ax ? s.nx : (ay ? s.ny : s.nz);
-        if (ax) { s.nx += s.dx; s.cx += s.sx; }
-        if (ay) { s.ny += s.dy; s.cy += s.sy; }
-        if (az) { s.nz += s.dz; s.cz += s.sz; }
+        if (ax) { s.nx += s.dx; s.lin += s.ix; }
+        if (ay) { s.ny += s.dy; s.lin += s.iy; }
+        if (az) { s.nz += s.dz; s.lin += s.iz; }
         if (!(s.t <= s.tmax)) {
             s.done = true;
             if (s.open && s.tmax - s.start > kDelta) { ta = s.start; tb = s.tmax; return true; }

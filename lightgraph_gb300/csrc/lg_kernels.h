@@ -104,19 +104,55 @@ struct DevScatterGrid {
 struct ShadowTask {
     float p[3];    // index-space position
     float w[3];    // pTrans * (1 - dT) per channel
-    uint32_t n;    // primary loop iteration (keys the shadow random streams)
-    uint32_t ps;   // pixel * spp + sample
+    uint32_t sa;   // the pixel-sample stream's first word and the primary
+    uint32_t iw;   // iteration's word: they key the shadow random streams
 };
 static_assert(sizeof(ShadowTask) == 32, "ShadowTask is two 16-byte words");
 size_t pixel_sample_bytes();
+// Ordering of the shadow rays of one light: tasks are counting-sorted by a
+// key that groups rays which cross the same part of the volume, so the rays
+// in flight share cache lines and the lanes of a warp walk similar paths.
+//   kind 0 (distant light, parallel rays): (u, v) bin of the start point
+//          projected on the plane normal to the ray direction D, in Morton
+//          order, then the depth bin along D;
+//   kind 1 (point light, rays through O): cube-map face and (s, t) bin of the
+//          direction from O to the start point, then the distance bin;
+//   kind 2 (environment light, random directions): task order in buckets of
+//          2^shift tasks.
+struct RayBin {
+    int kind, ns, nd, shift;  // ns: (u, v) or (s, t) bins per side (power of two), nd: depth bins
+    float U[3], V[3], D[3];   // kind 0: orthonormal basis, D the ray direction
+    float O[3];               // kind 1: light position (index space)
+    float u0, v0, inv_bs;     // kind 0: projected origin, 1 / bin size
+    float d0, inv_ds;         // depth origin, 1 / depth bin size
+    int64_t key_off, nkeys;   // this light's keys in the combined histogram
+};
+struct RayBins {
+    RayBin b[kMaxLights];
+    int n;
+};
+// Count pass (order == null: counts[key] += rays) or scatter pass (counts
+// holds the exclusive scan; order[counts[key]++] = task) over all lights.
+cudaError_t launch_ray_bins(const ShadowTask* tasks, const int32_t* total, int64_t task_cap, const RayBins& rb,
+                            int32_t* counts, int32_t* order, int sms, cudaStream_t st);
 // Wave 1: counts[ps] = shading samples of each pixel-sample.
 cudaError_t launch_render_count(const DevScene& sc, const DevCamera& cam, const DevScatterGrid& sg, int32_t* counts,
                                 cudaStream_t st);
-// Waves 2-4 given the exclusive scan of the counts (offsets, device total).
+// Shadow-ray ordering buffers: key_counts and key_offsets hold rb's keys,
+// key_scan the scan's block sums (keys / 1024 + 2), order n_lights * task_cap.
+struct RayOrder {
+    RayBins rb;
+    int64_t n_keys;
+    int32_t *key_counts, *key_offsets, *key_scan, *key_total, *order;
+};
+// Waves 2-5 given the exclusive scan of the counts (offsets, device total):
+// primary shading, shadow-ray ordering, shadow rays, resolve. direct holds
+// n_lights * task_cap per-light contributions. marks (4 events, optional)
+// are recorded after each wave.
 cudaError_t launch_render_shade(const DevScene& sc, const DevCamera& cam, const DevScatterGrid& sg,
                                 const int32_t* counts, const int32_t* offsets, const int32_t* total,
-                                ShadowTask* tasks, int64_t task_cap, void* pixel_samples, float4* direct,
-                                float4* rgba, float4* dfilm, float4* sfilm, float4* efilm,
+                                ShadowTask* tasks, int64_t task_cap, void* pixel_samples, const RayOrder& ro,
+                                float4* direct, float4* rgba, float4* dfilm, float4* sfilm, float4* efilm,
                                 unsigned long long* counters, int sms, cudaStream_t st,
                                 cudaEvent_t* marks = nullptr);
 // Exclusive scan of n int32 (block_sums: n/1024 + 1 ints); *total = sum.

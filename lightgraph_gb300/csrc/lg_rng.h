@@ -74,9 +74,15 @@ LG_HD float draw(Stream s, uint32_t key) { return u01(hash32(s.a ^ hash32(s.b + 
 
 // Sub-stream of a shadow ray: keyed by the primary iteration n, light k and
 // light sample ls (render), or by light k and sample ls with n = 0 (vertices).
+// The key splits into a per-iteration part (s.a and shadow_iter_word(s, n))
+// and the light terms, so a caller can carry the two words instead of the
+// stream and the iteration.
+LG_HD uint32_t shadow_iter_word(Stream s, uint32_t n) { return hash32(s.b ^ (kTagShadowRay | (n & 0x0FFFFFFFu))); }
+LG_HD uint32_t shadow_key_from(uint32_t sa, uint32_t iter_word, uint32_t k, uint32_t ls) {
+    return hash32(sa ^ (iter_word + k * 0x9E3779B9u + ls * 0x85EBCA6Bu));
+}
 LG_HD uint32_t shadow_key(Stream s, uint32_t n, uint32_t k, uint32_t ls) {
-    return hash32(s.a ^ hash32(s.b ^ (kTagShadowRay | (n & 0x0FFFFFFFu))) + k * 0x9E3779B9u +
-                  ls * 0x85EBCA6Bu);
+    return shadow_key_from(s.a, shadow_iter_word(s, n), k, ls);
 }
 
 LG_HD float draw_sub(uint32_t sub, uint32_t key) { return u01(hash32(sub ^ hash32(key))); }
