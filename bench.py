@@ -49,6 +49,7 @@ def parse():
     ap.add_argument("--small", action="store_true", help="the 128^3 / 1024-point / 256^2 case instead")
     ap.add_argument("--image", type=int, default=0, help="override the square image size (profiling runs)")
     ap.add_argument("--spp", type=int, default=0, help="override the samples per pixel (profiling runs)")
+    ap.add_argument("--res", type=int, default=0, help="override the production grid resolution (profiling runs)")
     ap.add_argument("--serving", type=int, default=24, help="requests in the serving measurement (0: skip)")
     ap.add_argument("--rate", type=float, default=50.0, help="Poisson arrival rate of the serving stream (req/s)")
     return ap.parse_args()
@@ -108,9 +109,9 @@ def dist_env():
     return rank, world, local
 
 
-def make_scene(small: bool, image: int = 0, spp: int = 0):
+def make_scene(small: bool, image: int = 0, spp: int = 0, res: int = 0):
     from lightgraph_gb300 import scenes
-    sc = scenes.small() if small else scenes.production()
+    sc = scenes.small() if small else (scenes.production(res=res) if res > 0 else scenes.production())
     if image > 0:
         sc.opts.width = sc.opts.height = image
     if spp > 0:
@@ -120,13 +121,15 @@ def make_scene(small: bool, image: int = 0, spp: int = 0):
 
 def workload_config(sc, small):
     o = sc.opts
-    return {"workload": ("small 128^3 sphere-fBm" if small else "production 512^3 sparse cumulus") +
+    res = sc.info["res"]
+    return {"workload": ("small 128^3 sphere-fBm" if small else f"production {res}^3 sparse cumulus") +
             f", {len(sc.points[0])}-point LightGraph, {o.width}x{o.height} at {o.samples} spp",
             "grid": f"{sc.info['res']}^3, voxel {sc.info['voxel']:.5g}, active voxels {sc.info['active_voxels']}",
             "graph_points": len(sc.points[0]), "connect_radius": sc.radius[0], "max_connect": sc.max_connect,
             "image": [o.width, o.height], "spp": o.samples, "lights": [l.spec for l in sc.lights],
             "steps_per_frame": list(o.step), "precision": "fp32 grids, fp32 math",
-            "l2": "inputs larger than L2 (density bricks ~575 MB > 129 MB), no flush" if not small else
+            "l2": "inputs larger than L2 (density cell records: 32 B per voxel, active leaves ~620 MB at 512^3 "
+                  "> 129 MB L2), no flush" if not small else
                   "small case: grid fits L2",
             "parallelism": "replicas (independent frames per GPU)"}
 
@@ -269,7 +272,7 @@ def run_reference(args):
     rank, world, local = dist_env()
     if rank != 0:
         return 0
-    sc = make_scene(args.small, args.image, args.spp)
+    sc = make_scene(args.small, args.image, args.spp, args.res)
     fw_rounds, stride = (32, 256) if not args.small else (64, 32)
     vals = []
     for _ in range(args.warmup):
@@ -305,7 +308,7 @@ def run_ours(args):
     if world > 1:
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     torch.cuda.set_device(local)
-    sc = make_scene(args.small, args.image, args.spp)
+    sc = make_scene(args.small, args.image, args.spp, args.res)
     ctx = Context(local)
     scenes.load_into(ctx, sc)
     ctx.build_graphs(sc.points, sc.radius_sq, sc.max_connect)

@@ -218,28 +218,31 @@ __device__ __forceinline__ int64_t ray_key(const RayBin& b, const float p[3], in
     return b.key_off + uv * b.nd + clamp_bin(depth * b.inv_ds, b.nd);
 }
 
-// Warp-aggregated counting sort passes (lanes with equal keys share one
-// atomic). Within a key the order is whatever the atomics give; every ray's
-// result goes to its own slot, so results do not depend on it.
+// Warp-aggregated counting sort passes over units of kRayUnit consecutive
+// tasks (neighbouring shading samples of one primary ray, keyed by the first
+// one), so lanes with equal keys share one atomic. Within a key the order is
+// whatever the atomics give; every ray's result goes to its own slot, so
+// results do not depend on it.
 __global__ void __launch_bounds__(256) k_ray_bins(const ShadowTask* __restrict__ tasks,
                                                   const int32_t* __restrict__ total_ptr, int64_t task_cap,
                                                   RayBins rb, int32_t* __restrict__ counts,
                                                   int32_t* __restrict__ order) {
     const int64_t total = min((int64_t)*total_ptr, task_cap);
+    const int64_t n_units = (total + kRayUnit - 1) / kRayUnit;
     const int lane = threadIdx.x & 31;
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < total; base += stride) {
-        const int64_t t = base + threadIdx.x;
-        const bool valid = t < total;
+    for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < n_units; base += stride) {
+        const int64_t u = base + threadIdx.x;
+        const bool valid = u < n_units;
         float p[3] = {0.f, 0.f, 0.f};
         if (valid) {
-            const float4 q = __ldg(reinterpret_cast<const float4*>(tasks + t));
+            const float4 q = __ldg(reinterpret_cast<const float4*>(tasks + u * kRayUnit));
             p[0] = q.x;
             p[1] = q.y;
             p[2] = q.z;
         }
         for (int k = 0; k < rb.n; ++k) {
-            const unsigned long long key = valid ? (unsigned long long)ray_key(rb.b[k], p, t) : ~0ull;
+            const unsigned long long key = valid ? (unsigned long long)ray_key(rb.b[k], p, u * kRayUnit) : ~0ull;
             const unsigned grp = __match_any_sync(0xffffffffu, key);
             if (!valid) continue;
             const int leader = __ffs(grp) - 1;
@@ -249,7 +252,7 @@ __global__ void __launch_bounds__(256) k_ray_bins(const ShadowTask* __restrict__
                 int32_t pos = 0;
                 if (lane == leader) pos = atomicAdd(counts + key, __popc(grp));
                 pos = __shfl_sync(grp, pos, leader);
-                order[pos + __popc(grp & ((1u << lane) - 1u))] = (int32_t)t;
+                order[pos + __popc(grp & ((1u << lane) - 1u))] = (int32_t)u;
             }
         }
     }
@@ -265,8 +268,9 @@ cudaError_t launch_ray_bins(const ShadowTask* tasks, const int32_t* total, int64
 // --- shadow rays -------------------------------------------------------------
 
 // One thread per (light k, ordered slot r): the shadow rays of light k (all
-// its samples) from task order[k * total + r]. The threads in flight march
-// neighbouring rays. direct[k * task_cap + t] = albedo * (sum_ls I * T / ns) * w.
+// its samples) from task kRayUnit * order[k * n_units + r / kRayUnit] +
+// r % kRayUnit. The threads in flight march neighbouring rays.
+// direct[k * task_cap + t] = albedo * (sum_ls I * T / ns) * w.
 // kEnv = false leaves the environment-light branch out (no light of the
 // scene is an environment light), which frees registers for occupancy.
 template <int DT, bool kEnv>
@@ -275,7 +279,9 @@ __global__ void __launch_bounds__(128, 8) k_shadow(DevScene sc, const ShadowTask
                                                 const int32_t* __restrict__ order, float4* __restrict__ direct,
                                                 unsigned long long* __restrict__ ctr) {
     const int64_t total = min((int64_t)*total_ptr, task_cap);
-    const int64_t n_rays = total * sc.n_lights;
+    const int64_t n_units = (total + kRayUnit - 1) / kRayUnit;
+    const int64_t per_light = n_units * kRayUnit;
+    const int64_t n_rays = per_light * sc.n_lights;
     const DevGrid& G = sc.dens;
     const DevShader& sh = sc.sh;
     const float step1 = sc.step1, cutoff = sc.cutoff;
@@ -283,8 +289,10 @@ __global__ void __launch_bounds__(128, 8) k_shadow(DevScene sc, const ShadowTask
     uint32_t n_shadow = 0;
     for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n_rays;
          r += (int64_t)gridDim.x * blockDim.x) {
-        const int k = (int)(r / total);
-        const int64_t t = order[r];
+        const int k = (int)(r / per_light);
+        const int64_t rr = r - k * per_light;
+        const int64_t t = (int64_t)order[k * n_units + rr / kRayUnit] * kRayUnit + rr % kRayUnit;
+        if (t >= total) continue;
         const ShadowTask tk = tasks[t];
         const DevLight& Lk = sc.lights[k];
         float lum[3] = {0.f, 0.f, 0.f};
@@ -341,16 +349,19 @@ __global__ void __launch_bounds__(128, 8) k_shadow(DevScene sc, const ShadowTask
     }
 }
 
-// One thread per pixel: the antialiasing average in sample order. A task's
-// direct light is the sum of its lights' contributions in light order.
+// One warp per pixel: for each sample in order, lane l sums the sample's
+// tasks l, l + 32, ... (a task's direct light is the sum of its lights'
+// contributions in light order), a butterfly reduction combines the lanes and
+// lane 0 (whose summation order is fixed) forms the antialiasing averages.
 __global__ void __launch_bounds__(128) k_resolve(DevCamera cam, const int32_t* __restrict__ offsets,
                                                  const int32_t* __restrict__ counts,
                                                  const PixelSample* __restrict__ pss,
                                                  const float4* __restrict__ direct, int n_lights, int64_t task_cap,
                                                  float4* __restrict__ rgba, float4* __restrict__ dfilm,
                                                  float4* __restrict__ sfilm, float4* __restrict__ efilm) {
-    const int64_t pix = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (pix >= (int64_t)cam.width * cam.height) return;
+    const int64_t pix = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (pix >= (int64_t)cam.width * cam.height) return;  // uniform across the warp
     const float ratio = 1.f / (float)cam.spp;
     float tAA[3] = {0.f, 0.f, 0.f}, lAA[3] = {0.f, 0.f, 0.f}, dAA[3] = {0.f, 0.f, 0.f};
     float sAA[3] = {0.f, 0.f, 0.f}, eAA[3] = {0.f, 0.f, 0.f};
@@ -359,7 +370,7 @@ __global__ void __launch_bounds__(128) k_resolve(DevCamera cam, const int32_t* _
         const PixelSample o = pss[ps];
         float d[3] = {0.f, 0.f, 0.f};
         const int64_t b = offsets[ps], e = min((int64_t)b + counts[ps], task_cap);
-        for (int64_t t = b; t < e; ++t) {
+        for (int64_t t = b + lane; t < e; t += 32) {
             float acc[3] = {0.f, 0.f, 0.f};
             for (int k = 0; k < n_lights; ++k) {
                 const float4 v = direct[(int64_t)k * task_cap + t];
@@ -372,6 +383,10 @@ __global__ void __launch_bounds__(128) k_resolve(DevCamera cam, const int32_t* _
             d[2] += acc[2];
         }
 #pragma unroll
+        for (int off = 16; off > 0; off >>= 1)
+#pragma unroll
+            for (int c = 0; c < 3; ++c) d[c] += __shfl_xor_sync(0xffffffffu, d[c], off);
+#pragma unroll
         for (int c = 0; c < 3; ++c) {
             lAA[c] += (d[c] + o.scat[c] + o.emis[c]) * ratio;
             dAA[c] += d[c] * ratio;
@@ -380,6 +395,7 @@ __global__ void __launch_bounds__(128) k_resolve(DevCamera cam, const int32_t* _
             tAA[c] += o.trans[c] * ratio;
         }
     }
+    if (lane != 0) return;
     if (rgba) rgba[pix] = make_float4(lAA[0], lAA[1], lAA[2], 1.f - (tAA[0] + tAA[1] + tAA[2]) / 3.f);
     if (dfilm) dfilm[pix] = make_float4(dAA[0], dAA[1], dAA[2], 0.f);
     if (sfilm) sfilm[pix] = make_float4(sAA[0], sAA[1], sAA[2], 0.f);
@@ -473,8 +489,8 @@ cudaError_t launch_render_shade(const DevScene& sc, const DevCamera& cam, const 
     }
     ++g_launch_counter;
     mark(2);
-    k_resolve<<<(unsigned)((n_pix + 127) / 128), 128, 0, st>>>(cam, offsets, counts, pss, direct, sc.n_lights,
-                                                              task_cap, rgba, dfilm, sfilm, efilm);
+    k_resolve<<<(unsigned)((n_pix * 32 + 127) / 128), 128, 0, st>>>(cam, offsets, counts, pss, direct, sc.n_lights,
+                                                                   task_cap, rgba, dfilm, sfilm, efilm);
     ++g_launch_counter;
     mark(3);
     return cudaGetLastError();

@@ -131,6 +131,7 @@ struct RayBins {
     RayBin b[kMaxLights];
     int n;
 };
+constexpr int kRayUnit = 2;  // consecutive tasks ordered as one unit
 // Count pass (order == null: counts[key] += rays) or scatter pass (counts
 // holds the exclusive scan; order[counts[key]++] = task) over all lights.
 cudaError_t launch_ray_bins(const ShadowTask* tasks, const int32_t* total, int64_t task_cap, const RayBins& rb,
@@ -139,7 +140,8 @@ cudaError_t launch_ray_bins(const ShadowTask* tasks, const int32_t* total, int64
 cudaError_t launch_render_count(const DevScene& sc, const DevCamera& cam, const DevScatterGrid& sg, int32_t* counts,
                                 cudaStream_t st);
 // Shadow-ray ordering buffers: key_counts and key_offsets hold rb's keys,
-// key_scan the scan's block sums (keys / 1024 + 2), order n_lights * task_cap.
+// key_scan the scan's block sums (keys / 1024 + 2), order n_lights * units
+// (units of kRayUnit tasks).
 struct RayOrder {
     RayBins rb;
     int64_t n_keys;
