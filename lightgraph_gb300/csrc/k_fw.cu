@@ -27,10 +27,11 @@
 //                      k_fw_update);
 //   fw_solve_batched : many matrices of different sizes in ONE persistent
 //                      launch (k_fw_persistent). CTAs claim work items from a
-//                      queue ordered round by round; an item waits (bounded)
-//                      on per-graph completion counters for the items it
-//                      depends on, which always come earlier in the queue, so
-//                      the schedule cannot deadlock whatever the residency.
+//                      queue ordered round by round with a one-round
+//                      look-ahead; an item waits (bounded) on the version
+//                      counters of the 64 x 64 blocks it reads, whose writers
+//                      always come earlier in the queue, so the schedule
+//                      cannot deadlock whatever the residency.
 #include <algorithm>
 
 #include "lg_kernels.h"
@@ -386,13 +387,25 @@ cudaError_t fw_solve(float* d, int n, int ld, cudaStream_t st) {
 // ---------------------------------------------------------------------------
 
 // Each CTA claims items until the queue is empty. An item is
-// {graph, round, kind (0 panel, 1 update), tile}. Dependencies:
-//   panel  (g, r) : all update items of (g, r - 1) done
-//   update (g, r) : all panel items of (g, r) done
-// both earlier in the queue. Waits spin at most kSpinLimit polls (with
-// nanosleep) and then raise err[0] = 1; every CTA checks err[0] before each
-// item, so a stalled queue ends the launch instead of hanging the GPU.
-constexpr uint32_t kSpinLimit = 1u << 24;  // x ~200 ns sleeps: several seconds
+// {graph, round, kind (0 panel, 1 update), tile}. Every 64 x 64 block of a
+// graph has a version counter: the number of rounds whose writes to it are
+// done (round r writes each block once, by its panel tile when the block is
+// in row or column block r, else by the update tile holding it). An item of
+// round r waits for exactly the blocks it reads:
+//   panel  (r, X)    : blocks (r, r) and X at version >= r;
+//   update (r, tile) : its A and B panel blocks (column / row block r) at
+//                      version >= r + 1 and its own blocks outside row and
+//                      column block r at version >= r.
+// The queue is ordered with a one-round look-ahead: the update tiles of round
+// r that hold row or column block r + 1 come first, then the panel tiles of
+// round r + 1, then the rest of round r's update tiles. Every item's
+// dependencies come earlier in the queue, so the holder of the earliest
+// unfinished item can always proceed: the schedule cannot deadlock whatever
+// the residency, and panels overlap the bulk of the previous round's update.
+// Waits spin at most kSpinLimit polls (with nanosleep) and then raise
+// err[0] = 1; every CTA checks err[0] before each item, so a stalled queue
+// ends the launch instead of hanging the GPU.
+constexpr uint32_t kSpinLimit = 1u << 24;  // x ~100-200 ns sleeps: seconds
 
 __device__ __forceinline__ uint32_t ld_acquire(const uint32_t* p) {
     uint32_t v;
@@ -400,11 +413,24 @@ __device__ __forceinline__ uint32_t ld_acquire(const uint32_t* p) {
     return v;
 }
 
+// Bounded wait for *v >= target; false (and err set) when it gives up.
+__device__ __forceinline__ bool wait_version(const uint32_t* v, uint32_t target, uint32_t* err) {
+    uint32_t spins = 0;
+    while (ld_acquire(v) < target) {
+        if (++spins > kSpinLimit || ld_acquire(err) != 0) {
+            atomicExch(err, 1u);
+            return false;
+        }
+        __nanosleep(100);
+    }
+    return true;
+}
+
 __global__ void __launch_bounds__(256, 2) k_fw_persistent(float* __restrict__ base, const FwGraph* __restrict__ gs,
                                                           const int4* __restrict__ items, int n_items,
                                                           uint32_t* __restrict__ sync) {
-    // sync layout: [0] queue head, [1] error flag, [2 + 2g] panels done of
-    // graph g, [3 + 2g] updates done of graph g
+    // sync layout: [0] queue head, [1] error flag, then per graph g the nt^2
+    // block versions at sync + 2 + gs[g].vofs (row-major blocks)
     extern __shared__ float4 fw_smem[];
     float2* As = reinterpret_cast<float2*>(fw_smem);
     float2* Bs = As + 32 * (kTile + kApad);
@@ -423,38 +449,68 @@ __global__ void __launch_bounds__(256, 2) k_fw_persistent(float* __restrict__ ba
         if (it >= n_items || s_abort) break;
         const int4 w = items[it];
         const FwGraph g = gs[w.x];
+        uint32_t* ver = sync + 2 + g.vofs;
+        const int r = w.y, nt = g.nt;
         if (threadIdx.x == 0) {
-            const uint32_t* ctr;
-            uint32_t target;
-            if (w.z == 0) {  // panel: wait for the previous round's updates
-                ctr = sync + 3 + 2 * w.x;
-                target = (uint32_t)w.y * (uint32_t)(g.nu * g.nu);
-            } else {         // update: wait for this round's panels
-                ctr = sync + 2 + 2 * w.x;
-                target = (uint32_t)(w.y + 1) * (uint32_t)(2 * g.nt - 1);
-            }
-            uint32_t spins = 0;
-            while (ld_acquire(ctr) < target) {
-                if (++spins > kSpinLimit || ld_acquire(err) != 0) {
-                    atomicExch(err, 1u);
-                    s_abort = 1;
-                    break;
+            bool ok = true;
+            if (w.z == 0) {
+                int bi = r, bj = r;  // the block this panel tile writes
+                if (w.w > 0) {
+                    int q = w.w - 1;
+                    const bool col = q >= nt - 1;
+                    if (col) q -= nt - 1;
+                    const int other = q < r ? q : q + 1;
+                    bi = col ? other : r;
+                    bj = col ? r : other;
                 }
-                __nanosleep(200);
+                ok = wait_version(ver + r * nt + r, (uint32_t)r, err) &&
+                     wait_version(ver + bi * nt + bj, (uint32_t)r, err);
+            } else {
+                const int ti = w.w / g.nu, tj = w.w % g.nu;
+                for (int a = 0; a < 2 && ok; ++a) {
+                    const int bi = 2 * ti + a, bj = 2 * tj + a;
+                    if (bi < nt) ok = wait_version(ver + bi * nt + r, (uint32_t)r + 1u, err);
+                    if (ok && bj < nt) ok = wait_version(ver + r * nt + bj, (uint32_t)r + 1u, err);
+                }
+                for (int a = 0; a < 2 && ok; ++a)
+                    for (int c = 0; c < 2 && ok; ++c) {
+                        const int bi = 2 * ti + a, bj = 2 * tj + c;
+                        if (bi < nt && bj < nt && bi != r && bj != r)
+                            ok = wait_version(ver + bi * nt + bj, (uint32_t)r, err);
+                    }
             }
+            if (!ok) s_abort = 1;
         }
         __syncthreads();
         if (s_abort) break;
         float* d = base + g.off;
         if (w.z == 0) {
-            fw_panel_tile<true>(d, g.n, g.ld, w.y, w.w, psm);
+            fw_panel_tile<true>(d, g.n, g.ld, r, w.w, psm);
         } else {
-            fw_update_tile<true>(d, g.n, g.ld, w.y, w.w / g.nu, w.w % g.nu, As, Bs);
+            fw_update_tile<true>(d, g.n, g.ld, r, w.w / g.nu, w.w % g.nu, As, Bs);
         }
+        __threadfence();
         __syncthreads();
         if (threadIdx.x == 0) {
-            __threadfence();
-            atomicAdd(sync + 2 + 2 * w.x + w.z, 1u);
+            if (w.z == 0) {
+                int bi = r, bj = r;
+                if (w.w > 0) {
+                    int q = w.w - 1;
+                    const bool col = q >= nt - 1;
+                    if (col) q -= nt - 1;
+                    const int other = q < r ? q : q + 1;
+                    bi = col ? other : r;
+                    bj = col ? r : other;
+                }
+                atomicAdd(ver + bi * nt + bj, 1u);
+            } else {
+                const int ti = w.w / g.nu, tj = w.w % g.nu;
+                for (int a = 0; a < 2; ++a)
+                    for (int c = 0; c < 2; ++c) {
+                        const int bi = 2 * ti + a, bj = 2 * tj + c;
+                        if (bi < nt && bj < nt && bi != r && bj != r) atomicAdd(ver + bi * nt + bj, 1u);
+                    }
+            }
         }
     }
 }
@@ -463,27 +519,45 @@ size_t fw_batched_items(const FwGraph* graphs, int n_graphs, int4* items) {
     int max_nt = 0;
     for (int g = 0; g < n_graphs; ++g) max_nt = std::max(max_nt, graphs[g].nt);
     size_t k = 0;
+    auto emit = [&](int g, int r, int kind, int t) {
+        if (items) items[k] = make_int4(g, r, kind, t);
+        ++k;
+    };
+    auto panels = [&](int r) {
+        for (int g = 0; g < n_graphs; ++g)
+            if (r < graphs[g].nt)
+                for (int b = 0; b < 2 * graphs[g].nt - 1; ++b) emit(g, r, 0, b);
+    };
+    // prio: the update tiles of round r holding row or column block r + 1
+    auto updates = [&](int r, bool prio) {
+        for (int g = 0; g < n_graphs; ++g) {
+            const FwGraph& G = graphs[g];
+            if (r >= G.nt || G.nt < 2) continue;
+            const int tn = (r + 1) / 2;
+            for (int t = 0; t < G.nu * G.nu; ++t) {
+                const int ti = t / G.nu, tj = t % G.nu;
+                const bool p = r + 1 < G.nt && (ti == tn || tj == tn);
+                if (p == prio) emit(g, r, 1, t);
+            }
+        }
+    };
+    panels(0);
     for (int r = 0; r < max_nt; ++r) {
-        for (int g = 0; g < n_graphs; ++g) {
-            if (r >= graphs[g].nt) continue;
-            for (int b = 0; b < 2 * graphs[g].nt - 1; ++b) {
-                if (items) items[k] = make_int4(g, r, 0, b);
-                ++k;
-            }
-        }
-        for (int g = 0; g < n_graphs; ++g) {
-            if (r >= graphs[g].nt || graphs[g].nt < 2) continue;
-            for (int t = 0; t < graphs[g].nu * graphs[g].nu; ++t) {
-                if (items) items[k] = make_int4(g, r, 1, t);
-                ++k;
-            }
-        }
+        updates(r, true);
+        panels(r + 1);
+        updates(r, false);
     }
     return k;
 }
 
+size_t fw_sync_words(const FwGraph* graphs, int n_graphs) {
+    size_t w = 2;
+    for (int g = 0; g < n_graphs; ++g) w += (size_t)graphs[g].nt * graphs[g].nt;
+    return w;
+}
+
 cudaError_t fw_solve_batched(float* base, const FwGraph* graphs, const int4* items, int n_items, uint32_t* sync,
-                             int n_graphs, int ctas, cudaStream_t st) {
+                             size_t sync_words, int ctas, cudaStream_t st) {
     static bool attr_set = false;
     if (!attr_set) {
         cudaError_t e = cudaFuncSetAttribute(k_fw_persistent, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -491,7 +565,7 @@ cudaError_t fw_solve_batched(float* base, const FwGraph* graphs, const int4* ite
         if (e != cudaSuccess) return e;
         attr_set = true;
     }
-    cudaError_t e = cudaMemsetAsync(sync, 0, sizeof(uint32_t) * (2 + 2 * (size_t)n_graphs), st);
+    cudaError_t e = cudaMemsetAsync(sync, 0, sizeof(uint32_t) * sync_words, st);
     if (e != cudaSuccess) return e;
     if (n_items == 0) return cudaSuccess;
     k_fw_persistent<<<ctas, 256, kUpdateSmem, st>>>(base, graphs, items, n_items, sync);

@@ -681,7 +681,7 @@ static lg_status run_fw_schedule(Ctx* ctx, float* base, int choice) {
     int sms = 0;
     CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device), "device query");
     CK(fw_solve_batched(base, ctx->d_fwg.as<FwGraph>(), ctx->d_fw_items.as<int4>(), ctx->fw_items_n,
-                        ctx->d_fw_sync.as<uint32_t>(), ctx->n_graphs, choice * sms, ctx->st),
+                        ctx->d_fw_sync.as<uint32_t>(), ctx->fw_sync_n, choice * sms, ctx->st),
        "batched floyd-warshall");
     return LG_OK;
 }
@@ -690,6 +690,7 @@ lg_status Ctx::solve_paths_batched(int choice) {
     Ctx* ctx = this;
     if (!fw_queue_valid) {
         std::vector<FwGraph> fg(n_graphs);
+        int64_t vofs = 0;
         for (int g = 0; g < n_graphs; ++g) {
             const GraphInfo& gi = h_graphs[g];
             fg[g].off = gi.s_off;
@@ -697,13 +698,16 @@ lg_status Ctx::solve_paths_batched(int choice) {
             fg[g].ld = gi.ld;
             fg[g].nt = gi.n == 0 ? 0 : gi.ld / 64;
             fg[g].nu = gi.n == 0 ? 0 : gi.ld / 128;
+            fg[g].vofs = vofs;
+            vofs += (int64_t)fg[g].nt * fg[g].nt;
         }
         const size_t n_items = fw_batched_items(fg.data(), n_graphs, nullptr);
         std::vector<int4> items(std::max<size_t>(n_items, 1));
         fw_batched_items(fg.data(), n_graphs, items.data());
+        fw_sync_n = fw_sync_words(fg.data(), n_graphs);
         CK(d_fwg.reserve(sizeof(FwGraph) * n_graphs), "fw queue alloc");
         CK(d_fw_items.reserve(sizeof(int4) * items.size()), "fw queue alloc");
-        CK(d_fw_sync.reserve(sizeof(uint32_t) * (2 + 2 * (size_t)n_graphs)), "fw queue alloc");
+        CK(d_fw_sync.reserve(sizeof(uint32_t) * fw_sync_n), "fw queue alloc");
         CK(cudaMemcpyAsync(d_fwg.p, fg.data(), sizeof(FwGraph) * n_graphs, cudaMemcpyHostToDevice, st), "fw queue upload");
         CK(cudaMemcpyAsync(d_fw_items.p, items.data(), sizeof(int4) * items.size(), cudaMemcpyHostToDevice, st),
            "fw queue upload");

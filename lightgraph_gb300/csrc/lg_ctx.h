@@ -96,6 +96,7 @@ struct Ctx {
     // batched Floyd-Warshall: work queue, counters and the autotuned schedule
     DevBuf d_fwg, d_fw_items, d_fw_sync, d_fw_tune;
     int fw_items_n = 0;
+    size_t fw_sync_n = 2;  // uint32 words of d_fw_sync
     bool fw_queue_valid = false;
     // schedule per (graph count, largest n): 0 = per-graph launches,
     // k > 0 = persistent with k CTAs per SM

@@ -43,16 +43,19 @@ cudaError_t fw_solve(float* d, int n, int ld, cudaStream_t st);
 
 // Batched: many matrices in one persistent launch.
 struct FwGraph {
-    int64_t off;  // first float of the matrix
+    int64_t off;   // first float of the matrix
     int32_t n, ld;
-    int32_t nt;   // k-blocks of 64
-    int32_t nu;   // update tiles of 128 per side
+    int32_t nt;    // k-blocks of 64
+    int32_t nu;    // update tiles of 128 per side
+    int64_t vofs;  // first of the graph's nt^2 block version counters
 };
 // Writes the work queue (if items != null) and returns its length.
 size_t fw_batched_items(const FwGraph* graphs, int n_graphs, int4* items);
-// sync: 2 + 2 * n_graphs uint32 (cleared here). ctas: persistent CTAs.
+// uint32 words of the batched solve's sync buffer: 2 + sum of nt^2.
+size_t fw_sync_words(const FwGraph* graphs, int n_graphs);
+// sync: fw_sync_words uint32 (cleared here). ctas: persistent CTAs.
 cudaError_t fw_solve_batched(float* base, const FwGraph* graphs, const int4* items, int n_items, uint32_t* sync,
-                             int n_graphs, int ctas, cudaStream_t st);
+                             size_t sync_words, int ctas, cudaStream_t st);
 int fw_persistent_ctas_per_sm();
 cudaError_t launch_set_diag(float* S, const GraphInfo* graphs, int n_graphs, int max_n,
                             cudaStream_t st);
