@@ -416,7 +416,8 @@ def run_ours(args):
                             "shadow": wave_ms[3], "resolve": wave_ms[4]},
         "render_stage": {"ms": float(stage_ms[6]), "algorithmic_bytes": render_bytes, "achieved_gbs": render_gbs,
                          "frac": render_gbs / peaks.get("hbm_gbs")},
-        "fw_roofline": {"kernel": "k_fw_update+k_fw_panels", "bound": "fp32_alu", "n": int(ld),
+        "fw_roofline": {"kernel": "k_fw_update+k_fw_panels" if fw_sched == 0 else "k_fw_persistent",
+                        "bound": "fp32_alu", "n": int(ld),
                         "achieved": fw_tflops, "unit": "TFLOP/s", "peak": NOMINAL_FP32_TFLOPS,
                         "peak_kind": "nominal (152 SMs x 128 lanes x 2 x 2.07 GHz)",
                         "frac": fw_tflops / NOMINAL_FP32_TFLOPS,
