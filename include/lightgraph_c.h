@@ -186,6 +186,48 @@ uint64_t lg_kernel_launches(const lg_ctx* ctx);
 /* Stage 1: LightGraph solve (LightGraph::operator(), src/LightGraph.h:158-196) */
 /* ------------------------------------------------------------------------- */
 
+/* Dart throwing of the LightGraph points: the constants of
+ * LightGraph::scatterPoints (src/LightGraph.h:22-28, src/main.cc:60-61) and
+ * RandGen's seeds (src/RandGen.h:28-30). */
+typedef struct lg_scatter_opts {
+    uint32_t scatter_count;  /* candidates per iteration, PC_SCATTER_COUNT 1000000       */
+    uint32_t target_size;    /* stop once more are accepted, TARGET_PC_SIZE 750          */
+    uint32_t n_estimates;    /* radius updates per iteration, PC_GROWTH_NUMBER_OF_ESTIMATE 100 */
+    uint32_t hard_limit;     /* point capacity per iteration, PC_SIZE_HARD_LIMIT 1000    */
+    float growth_power;      /* PC_GROWTH_FUNC_POWER 0.17                                */
+    float density_cutoff;    /* PC_DENSITY_CUTOFF 0.001                                  */
+    float min_dist_mult;     /* MIN_DIST_MULT 0.13 (x mean active-bbox edge)             */
+    float connect_mult;      /* CONNECT_SEARCH_RADIUS_MULT 1.7                            */
+    uint32_t seed_base;      /* iteration i's mt19937 is seeded with seed_base + i, 854123 */
+    uint32_t _pad0;
+} lg_scatter_opts;
+lg_status lg_scatter_opts_default(lg_scatter_opts* out);
+
+/* RandGen::operator() (src/RandGen.h:37-39) on the host: n draws of the
+ * mt19937 seeded with seed, as the uniform floats the reference reads (out)
+ * and as raw 32-bit outputs (raw); either may be NULL. */
+lg_status lg_randgen_draws(uint32_t seed, int64_t n, float* out, uint32_t* raw);
+
+/* LightGraph::scatterPoints (src/LightGraph.h:206-274) for iterations
+ * first_iter .. first_iter + n_iter - 1, on the density grid uploaded in ctx
+ * (sampled as the reference's BoxSampler, inside its active-voxel bbox):
+ * the same mt19937 streams, candidate order, adaptive minimum distance and
+ * early stop, so the accepted points are the reference's.
+ *   points   : n_iter x hard_limit x 3 floats (optional); iteration i's
+ *              counts[i] points start at i * hard_limit * 3
+ *   counts   : n_iter accepted-point counts (optional)
+ *   radius_sq: n_iter values (minDist * connect_mult)^2, the graph build's
+ *              searchRadiusConnectSquared (src/LightGraph.h:170-171) (optional) */
+lg_status lg_scatter_points(lg_ctx* ctx, const lg_scatter_opts* opts, int first_iter, int n_iter, float* points,
+                            int32_t* counts, float* radius_sq);
+
+/* lg_scatter_points followed by lg_build_graphs on its output: the loop of
+ * LightGraph::operator() up to buildGraph (src/LightGraph.h:158-177) for
+ * n_iter iterations at once, each iteration one graph.
+ *   counts: n_iter point counts (optional) */
+lg_status lg_scatter_graphs(lg_ctx* ctx, const lg_scatter_opts* opts, int first_iter, int n_iter, int max_connect,
+                            int32_t* counts);
+
 /* Loads n_graphs point sets (the output of LightGraph::scatterPoints,
  * src/LightGraph.h:206-274, injected by the caller) and connects each with the
  * reference's greedy rule: pairs closer than sqrt(radius_sq[g]) in FP64, at

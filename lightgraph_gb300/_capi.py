@@ -69,6 +69,13 @@ class CameraC(C.Structure):
                 ("width", C.c_int32), ("height", C.c_int32), ("samples", C.c_int32), ("_pad0", C.c_int32)]
 
 
+class ScatterOptsC(C.Structure):
+    _fields_ = [("scatter_count", C.c_uint32), ("target_size", C.c_uint32), ("n_estimates", C.c_uint32),
+                ("hard_limit", C.c_uint32), ("growth_power", C.c_float), ("density_cutoff", C.c_float),
+                ("min_dist_mult", C.c_float), ("connect_mult", C.c_float), ("seed_base", C.c_uint32),
+                ("_pad0", C.c_uint32)]
+
+
 class ServerOptsC(C.Structure):
     _fields_ = [("device", C.c_int32), ("max_inflight", C.c_int32), ("queue_capacity", C.c_int32),
                 ("_pad0", C.c_int32), ("hbm_budget_bytes", C.c_uint64)]
@@ -98,6 +105,10 @@ SIGNATURES = {
     "lg_set_lights": (I32, [P, C.POINTER(LightC), C.c_int, P, C.c_int, C.c_int]),
     "lg_set_shader": (I32, [P, C.POINTER(ShaderC)]),
     "lg_set_settings": (I32, [P, C.POINTER(SettingsC)]),
+    "lg_scatter_opts_default": (I32, [C.POINTER(ScatterOptsC)]),
+    "lg_randgen_draws": (I32, [C.c_uint32, I64, P, P]),
+    "lg_scatter_points": (I32, [P, C.POINTER(ScatterOptsC), C.c_int, C.c_int, P, P, P]),
+    "lg_scatter_graphs": (I32, [P, C.POINTER(ScatterOptsC), C.c_int, C.c_int, C.c_int, P]),
     "lg_build_graphs": (I32, [P, C.c_int, P, P, P, C.c_int, P, P]),
     "lg_march_edges": (I32, [P, P]),
     "lg_solve_paths": (I32, [P, P]),
@@ -115,7 +126,7 @@ SIGNATURES = {
     "lg_get_films": (I32, [P, P, P, P, P]),
     "lg_set_profiling": (I32, [P, C.c_int]),
     "lg_stage_times": (I32, [P, C.POINTER(D), C.c_int]),
-    "lg_render_wave_times": (I32, [P, C.POINTER(D)]),
+    "lg_render_wave_times": (I32, [P, C.POINTER(D)]),  # 5 doubles
     "lg_set_graph_mode": (I32, [P, C.c_int]),
     "lg_frame_launches": (U64, [P]),
     "lg_set_fw_schedule": (I32, [P, C.c_int]),

@@ -29,14 +29,15 @@ LIB_NAME = "liblightgraph_gb300.so"
 ORACLE_NAME = "liblg_oracle.so"
 
 CU_SOURCES = ["lg_api.cu", "k_graph.cu", "k_march.cu", "k_fw.cu", "k_diffuse.cu", "k_splat.cu",
-              "k_render.cu", "k_grid.cu", "lg_server.cu", "lg_noalloc.cu"]
+              "k_render.cu", "k_grid.cu", "k_dart.cu", "lg_server.cu", "lg_noalloc.cu"]
 CC_SOURCES = ["scene.cc", "lg_parse.cc"]
 CLI_SOURCE = "cli.cc"
 ORACLE_SOURCES = ["lg_oracle.cc"]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
-                     "-I" + INCLUDE, "-I" + CSRC]
+# host code: no FP contraction, so host arithmetic rounds the same on x86 and Arm
+NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
+                     "--expt-relaxed-constexpr", "-I" + INCLUDE, "-I" + CSRC]
 GXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-fopenmp", "-ffp-contract=off", "-I" + INCLUDE, "-I" + CSRC]
 
 

@@ -13,6 +13,8 @@
 // (src/Sampling.h:128-167): per-row Distribution1D CDFs and a marginal CDF
 // over the rows' integrals (src/Sampling.h:76-93). The prefix sums run in
 // FP64 on the device (the reference uses FP32) and are stored as FP32.
+#include <climits>
+
 #include "lg_kernels.h"
 
 namespace lg {
@@ -129,6 +131,43 @@ cudaError_t launch_leaf_bits(const float* dense, const int dims[3], const int or
     const unsigned blocks = (unsigned)((nbt + 255) / 256);
     k_leaf_bits<<<blocks, 256, 0, st>>>(dense, dims[0], dims[1], dims[2], origin[0], origin[1], origin[2],
                                         leaf_mask, g, bits, bbox);
+    ++g_launch_counter;
+    return cudaGetLastError();
+}
+
+// Bounding box of the non-zero voxels of the dense staging array (the active
+// voxels of a dense grid converted to a VDB), in the array's own coordinates:
+// bbox = {min x, y, z, max x, y, z}, pre-set to +/-INT_MAX. One thread per
+// voxel; warp reductions, then one atomic per warp and bound.
+__global__ void k_voxel_bbox(const float* __restrict__ dense, int dx, int dy, int dz, int* __restrict__ bbox) {
+    const int64_t n = (int64_t)dx * dy * dz;
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const bool on = i < n && dense[i] != 0.f;
+    int x = INT_MAX, y = INT_MAX, z = INT_MAX;
+    if (on) {
+        x = (int)(i % dx);
+        y = (int)((i / dx) % dy);
+        z = (int)(i / ((int64_t)dx * dy));
+    }
+    const int mnx = __reduce_min_sync(0xffffffffu, x), mny = __reduce_min_sync(0xffffffffu, y),
+              mnz = __reduce_min_sync(0xffffffffu, z);
+    const int mxx = __reduce_max_sync(0xffffffffu, on ? x : INT_MIN),
+              mxy = __reduce_max_sync(0xffffffffu, on ? y : INT_MIN),
+              mxz = __reduce_max_sync(0xffffffffu, on ? z : INT_MIN);
+    if ((threadIdx.x & 31) == 0 && mnx != INT_MAX) {
+        atomicMin(bbox + 0, mnx);
+        atomicMin(bbox + 1, mny);
+        atomicMin(bbox + 2, mnz);
+        atomicMax(bbox + 3, mxx);
+        atomicMax(bbox + 4, mxy);
+        atomicMax(bbox + 5, mxz);
+    }
+}
+
+cudaError_t launch_voxel_bbox(const float* dense, const int dims[3], int* bbox, cudaStream_t st) {
+    const int64_t n = (int64_t)dims[0] * dims[1] * dims[2];
+    if (n == 0) return cudaSuccess;
+    k_voxel_bbox<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(dense, dims[0], dims[1], dims[2], bbox);
     ++g_launch_counter;
     return cudaGetLastError();
 }

@@ -12,6 +12,7 @@
 #include <vector>
 
 #include "lg_ctx.h"
+#include "lg_mt.h"
 
 namespace lg {
 uint64_t g_launch_counter = 0;
@@ -347,7 +348,8 @@ lg_status Ctx::upload_grid(int which, const lg_grid_desc* desc, const float* val
         CK(cudaMemcpyAsync(mask_staging.p, desc->leaf_mask, nl, cudaMemcpyHostToDevice, st), "leaf mask upload");
         d_mask = mask_staging.as<uint8_t>();
     }
-    int bbox_init[6] = {INT_MAX, INT_MAX, INT_MAX, INT_MIN, INT_MIN, INT_MIN};
+    int bbox_init[12] = {INT_MAX, INT_MAX, INT_MAX, INT_MIN, INT_MIN, INT_MIN,
+                         INT_MAX, INT_MAX, INT_MAX, INT_MIN, INT_MIN, INT_MIN};
     CK(small.reserve(64), "small alloc");
     CK(cudaMemcpyAsync(small.p, bbox_init, sizeof bbox_init, cudaMemcpyHostToDevice, st), "bbox init");
     g.data = gs.bricks.p;
@@ -355,7 +357,8 @@ lg_status Ctx::upload_grid(int which, const lg_grid_desc* desc, const float* val
     CK(launch_pack_bricks(staging.as<float>(), desc->dims, desc->origin, g, gs.bricks.p, st), "pack bricks");
     CK(launch_leaf_bits(staging.as<float>(), desc->dims, desc->origin, d_mask, g, gs.bits.as<uint32_t>(),
                         small.as<int>(), st), "leaf bitmap");
-    int bbox[6];
+    CK(launch_voxel_bbox(staging.as<float>(), desc->dims, small.as<int>() + 6, st), "active voxel bbox");
+    int bbox[12];
     CK(cudaMemcpyAsync(bbox, small.p, sizeof bbox, cudaMemcpyDeviceToHost, st), "bbox download");
     CK(cudaStreamSynchronize(st), "grid upload sync");
     staging.release();
@@ -363,6 +366,11 @@ lg_status Ctx::upload_grid(int which, const lg_grid_desc* desc, const float* val
     for (int a = 0; a < 3; ++a) {
         g.bbmin[a] = g.has_leaves ? (float)(bbox[a] * 8) : 0.f;
         g.bbmax[a] = g.has_leaves ? (float)(bbox[3 + a] * 8 + 8) : 0.f;
+    }
+    gs.has_active = bbox[6] <= bbox[9];
+    for (int a = 0; a < 3; ++a) {
+        gs.vbbox[a] = gs.has_active ? bbox[6 + a] + desc->origin[a] : 0;
+        gs.vbbox[3 + a] = gs.has_active ? bbox[9 + a] + desc->origin[a] : 0;
     }
     gs.g = g;
     gs.desc = *desc;
@@ -604,6 +612,149 @@ lg_status Ctx::build_edges() {
        "greedy connect");
     graphs_built = true;
     return LG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// dart throwing (LightGraph::scatterPoints)
+// ---------------------------------------------------------------------------
+
+extern "C" lg_status lg_scatter_opts_default(lg_scatter_opts* o) {
+    if (!o) return LG_ERR_INVALID;
+    *o = lg_scatter_opts{};
+    o->scatter_count = 1000000;  // PC_SCATTER_COUNT (src/main.cc:61)
+    o->target_size = 750;        // TARGET_PC_SIZE (src/LightGraph.h:25)
+    o->n_estimates = 100;        // PC_GROWTH_NUMBER_OF_ESTIMATE (src/LightGraph.h:26)
+    o->hard_limit = 1000;        // PC_SIZE_HARD_LIMIT (src/LightGraph.h:22)
+    o->growth_power = 0.17f;     // PC_GROWTH_FUNC_POWER (src/LightGraph.h:27)
+    o->density_cutoff = 0.001f;  // PC_DENSITY_CUTOFF (src/LightGraph.h:24)
+    o->min_dist_mult = 0.13f;    // MIN_DIST_MULT (src/main.cc:60)
+    o->connect_mult = 1.7f;      // CONNECT_SEARCH_RADIUS_MULT (src/LightGraph.h:23)
+    o->seed_base = 854123;       // RandGen engines (src/RandGen.h:28-30)
+    return LG_OK;
+}
+
+extern "C" lg_status lg_randgen_draws(uint32_t seed, int64_t n, float* out, uint32_t* raw) {
+    if (n < 0) return LG_ERR_INVALID;
+    Mt19937 mt(seed);
+    for (int64_t k = 0; k < n; ++k) {
+        const uint32_t x = mt.next();
+        if (raw) raw[k] = x;
+        if (out) out[k] = mt_canonical_float(x);
+    }
+    return LG_OK;
+}
+
+lg_status Ctx::scatter_points(const lg_scatter_opts& o, int first_iter, int n_iter) {
+    Ctx* ctx = this;
+    const GridStore& gs = D();
+    if (!gs.valid) return fail(LG_ERR_STATE, "no density grid uploaded");
+    if (n_iter < 1 || first_iter < 0) return fail(LG_ERR_INVALID, "bad iteration range");
+    if (o.n_estimates < 1 || o.scatter_count < o.n_estimates)
+        return fail(LG_ERR_INVALID, "scatter_count must be >= n_estimates >= 1");
+    if (o.hard_limit < 1 || o.hard_limit > 4096 || o.target_size >= o.hard_limit)
+        return fail(LG_ERR_INVALID, "need target_size < hard_limit <= 4096");
+    if (!gs.has_active) return fail(LG_ERR_STATE, "the density grid has no active voxel");
+    // world bbox of the active voxels (Transform::indexToWorld of
+    // evalActiveVoxelBoundingBox, src/main.cc:512) and the starting minimum
+    // distance (src/main.cc:514-518), in the reference's float / double types
+    double bbmin[3], bbmax[3];
+    float bbsize[3];
+    for (int a = 0; a < 3; ++a) {
+        bbmin[a] = gs.desc.world_origin[a] + (double)gs.vbbox[a] * gs.desc.voxel_size;
+        bbmax[a] = gs.desc.world_origin[a] + (double)gs.vbbox[3 + a] * gs.desc.voxel_size;
+        bbsize[a] = (float)(bbmax[a] - bbmin[a]);
+    }
+    const float avg = (bbsize[0] + bbsize[1] + bbsize[2]) / 3.0f;
+    const float min_dist = o.min_dist_mult * avg;
+    // expected sizes at the radius updates (n + 1) % batch == 0
+    // (src/LightGraph.h:220-222, 240-245), with the C library's pow
+    const uint32_t batch = o.scatter_count / o.n_estimates;
+    const uint32_t n_upd = o.scatter_count / batch;
+    std::vector<uint32_t> expected(n_upd + 1);
+    for (uint32_t k = 0; k < n_upd; ++k) {
+        const uint64_t n = (uint64_t)(k + 1) * batch - 1;
+        expected[k] = (uint32_t)(o.target_size * std::pow((double)n / (double)o.scatter_count, (double)o.growth_power));
+    }
+    DartParams prm{};
+    prm.scatter_count = o.scatter_count;
+    prm.target = o.target_size;
+    prm.batch = batch;
+    prm.hard_limit = o.hard_limit;
+    prm.cutoff = o.density_cutoff;
+    prm.min_dist_sq0 = min_dist * min_dist;
+    prm.seed_base = o.seed_base;
+    prm.first_iter = first_iter;
+    for (int a = 0; a < 3; ++a) {
+        prm.bbmin[a] = bbmin[a];
+        prm.bbsize[a] = bbsize[a];
+        prm.wo[a] = gs.desc.world_origin[a];
+    }
+    prm.h = gs.desc.voxel_size;
+    const size_t npts = (size_t)n_iter * o.hard_limit * 3;
+    CK(d_dart_pts.reserve(sizeof(float) * npts), "dart alloc");
+    CK(d_dart_cnt.reserve(sizeof(int32_t) * n_iter), "dart alloc");
+    CK(d_dart_m2.reserve(sizeof(float) * n_iter), "dart alloc");
+    CK(d_dart_expected.reserve(sizeof(uint32_t) * expected.size()), "dart alloc");
+    CK(cudaMemcpyAsync(d_dart_expected.p, expected.data(), sizeof(uint32_t) * expected.size(), cudaMemcpyHostToDevice,
+                       st), "dart upload");
+    CK(launch_dart(gs.g, prm, n_iter, d_dart_expected.as<uint32_t>(), d_dart_pts.as<float>(), d_dart_cnt.as<int32_t>(),
+                   d_dart_m2.as<float>(), st), "dart throwing");
+    h_dart_pts.resize(npts);
+    h_dart_cnt.resize(n_iter);
+    h_dart_m2.resize(n_iter);
+    CK(cudaMemcpyAsync(h_dart_pts.data(), d_dart_pts.p, sizeof(float) * npts, cudaMemcpyDeviceToHost, st),
+       "dart download");
+    CK(cudaMemcpyAsync(h_dart_cnt.data(), d_dart_cnt.p, sizeof(int32_t) * n_iter, cudaMemcpyDeviceToHost, st),
+       "dart download");
+    CK(cudaMemcpyAsync(h_dart_m2.data(), d_dart_m2.p, sizeof(float) * n_iter, cudaMemcpyDeviceToHost, st),
+       "dart download");
+    CK(cudaStreamSynchronize(st), "dart sync");
+    return LG_OK;
+}
+
+// searchRadiusConnectSquared of an iteration from its last accepted squared
+// minimum distance (src/LightGraph.h:170-171, 268-269), in float.
+static float connect_radius_sq(float last_m2, float connect_mult) {
+    const float min_dist = std::sqrt(last_m2);
+    const float r = min_dist * connect_mult;
+    return r * r;
+}
+
+extern "C" lg_status lg_scatter_points(lg_ctx* handle, const lg_scatter_opts* opts, int first_iter, int n_iter,
+                                       float* points, int32_t* counts, float* radius_sq) {
+    Ctx* ctx = reinterpret_cast<Ctx*>(handle);
+    GUARD(ctx);
+    if (!opts) return ctx->fail(LG_ERR_INVALID, "null options");
+    lg_status s = ctx->scatter_points(*opts, first_iter, n_iter);
+    if (s != LG_OK) return s;
+    if (points) std::memcpy(points, ctx->h_dart_pts.data(), sizeof(float) * ctx->h_dart_pts.size());
+    if (counts) std::memcpy(counts, ctx->h_dart_cnt.data(), sizeof(int32_t) * n_iter);
+    if (radius_sq)
+        for (int i = 0; i < n_iter; ++i) radius_sq[i] = connect_radius_sq(ctx->h_dart_m2[i], opts->connect_mult);
+    return LG_OK;
+}
+
+extern "C" lg_status lg_scatter_graphs(lg_ctx* handle, const lg_scatter_opts* opts, int first_iter, int n_iter,
+                                       int max_connect, int32_t* counts) {
+    Ctx* ctx = reinterpret_cast<Ctx*>(handle);
+    GUARD(ctx);
+    if (!opts) return ctx->fail(LG_ERR_INVALID, "null options");
+    lg_status s = ctx->scatter_points(*opts, first_iter, n_iter);
+    if (s != LG_OK) return s;
+    std::vector<int64_t> offs(n_iter + 1, 0);
+    std::vector<float> r2(n_iter);
+    for (int i = 0; i < n_iter; ++i) {
+        offs[i + 1] = offs[i] + ctx->h_dart_cnt[i];
+        r2[i] = connect_radius_sq(ctx->h_dart_m2[i], opts->connect_mult);
+    }
+    std::vector<float> pts((size_t)offs[n_iter] * 3);
+    for (int i = 0; i < n_iter; ++i)
+        std::memcpy(pts.data() + 3 * offs[i], ctx->h_dart_pts.data() + (size_t)i * opts->hard_limit * 3,
+                    sizeof(float) * 3 * ctx->h_dart_cnt[i]);
+    if (counts) std::memcpy(counts, ctx->h_dart_cnt.data(), sizeof(int32_t) * n_iter);
+    s = ctx->load_graphs(n_iter, pts.data(), offs.data(), r2.data(), max_connect);
+    if (s != LG_OK) return s;
+    return ctx->build_edges();
 }
 
 extern "C" lg_status lg_build_graphs(lg_ctx* handle, int n_graphs, const float* points,

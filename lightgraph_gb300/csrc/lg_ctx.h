@@ -53,6 +53,10 @@ struct GridStore {
     lg_grid_desc desc{};
     bool valid = false;
     int version = 0;
+    // bounding box of the non-zero (active) voxels, index coordinates
+    // {min x, y, z, max x, y, z}; has_active false when every voxel is 0
+    int vbbox[6] = {0, 0, 0, 0, 0, 0};
+    bool has_active = false;
 };
 
 struct Ctx {
@@ -157,6 +161,11 @@ struct Ctx {
     lg_status load_graphs(int n_graphs, const float* points, const int64_t* offsets, const float* radius_sq,
                           int max_connect);
     lg_status build_edges();
+    // LightGraph::scatterPoints for n_iter iterations into h_dart_* (host)
+    lg_status scatter_points(const lg_scatter_opts& o, int first_iter, int n_iter);
+    DevBuf d_dart_pts, d_dart_cnt, d_dart_m2, d_dart_expected;
+    std::vector<float> h_dart_pts, h_dart_m2;
+    std::vector<int32_t> h_dart_cnt;
     lg_status march_edges();
     lg_status solve_paths();
     lg_status vertex_light();

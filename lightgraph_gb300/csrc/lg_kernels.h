@@ -164,6 +164,26 @@ cudaError_t launch_render_shade(const DevScene& sc, const DevCamera& cam, const 
 cudaError_t launch_exclusive_scan(const int32_t* in, int64_t n, int32_t* out, int32_t* block_sums, int32_t* total,
                                   cudaStream_t st);
 
+// Bounding box of the non-zero voxels of a dense array (array coordinates;
+// bbox pre-set to +/-INT_MAX).
+cudaError_t launch_voxel_bbox(const float* dense, const int dims[3], int* bbox, cudaStream_t st);
+
+// Dart throwing (LightGraph::scatterPoints), one CTA per iteration.
+struct DartParams {
+    uint32_t scatter_count, target, batch, hard_limit;
+    float cutoff, min_dist_sq0;
+    uint32_t seed_base;
+    int first_iter;
+    double bbmin[3];  // active-voxel bbox, world space
+    float bbsize[3];
+    double wo[3], h;  // the grid's world origin and voxel size
+};
+// expected: the expected sizes at the scatter_count / batch radius updates;
+// out_pts: n_iter x hard_limit x 3 floats; out_last_m2: the squared minimum
+// distance of each iteration's last accepted point.
+cudaError_t launch_dart(const DevGrid& g, const DartParams& prm, int n_iter, const uint32_t* expected, float* out_pts,
+                        int32_t* out_count, float* out_last_m2, cudaStream_t st);
+
 // Environment map CDFs (FP64 prefix sums)
 cudaError_t launch_env_cdf(const float* rgb, int w, int h, float* cond_func, float* cond_cdf,
                            float* cond_int, float* marg_func, float* marg_cdf, float* marg_int,

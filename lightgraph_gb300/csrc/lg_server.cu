@@ -12,6 +12,7 @@
 //   - every kernel is deterministic and every random number is keyed by the
 //     request's own seed, so a request's films are the same alone or in the
 //     mix.
+#include <algorithm>
 #include <chrono>
 #include <condition_variable>
 #include <cstring>
@@ -244,6 +245,8 @@ extern "C" lg_status lg_server_add_volume(lg_server* srv, const lg_grid_desc* de
     std::swap(v->dens.bits.bytes, c.dens.bits.bytes);
     v->dens.g = c.dens.g;
     v->dens.desc = c.dens.desc;
+    std::copy(c.dens.vbbox, c.dens.vbbox + 6, v->dens.vbbox);
+    v->dens.has_active = c.dens.has_active;
     v->dens.valid = true;
     v->dens.version = 1;
     c.dens.valid = false;

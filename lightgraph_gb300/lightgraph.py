@@ -294,6 +294,27 @@ class Context:
         self._ck(self.lib.lg_set_lights(self.h, arr, len(lights), ptr(env), ew, eh))
 
     # stage 1
+    def scatter_points(self, first_iter: int, n_iter: int, opts: "_capi.ScatterOptsC | None" = None):
+        """LightGraph::scatterPoints for iterations first_iter.. (see lg_scatter_points):
+        returns (list of point arrays, radius_sq per iteration)."""
+        o = opts if opts is not None else scatter_opts()
+        pts = np.zeros((n_iter, o.hard_limit, 3), np.float32)
+        cnt = np.zeros(n_iter, np.int32)
+        r2 = np.zeros(n_iter, np.float32)
+        self._ck(self.lib.lg_scatter_points(self.h, C.byref(o), first_iter, n_iter, _capi.ptr(pts), _capi.ptr(cnt),
+                                            _capi.ptr(r2)))
+        return [pts[i, :cnt[i]].copy() for i in range(n_iter)], r2
+
+    def scatter_graphs(self, first_iter: int, n_iter: int, max_connect: int = 12,
+                       opts: "_capi.ScatterOptsC | None" = None) -> np.ndarray:
+        """scatter_points, then loads the iterations as graphs and connects
+        them; returns the point count of each iteration."""
+        o = opts if opts is not None else scatter_opts()
+        cnt = np.zeros(n_iter, np.int32)
+        self._ck(self.lib.lg_scatter_graphs(self.h, C.byref(o), first_iter, n_iter, max_connect, ptr(cnt)))
+        self._graph_sizes = [int(c) for c in cnt]
+        return cnt
+
     def build_graphs(self, points: Sequence[np.ndarray], radius_sq: Sequence[float], max_connect: int = 12,
                      want_adjacency: bool = False):
         pts, offs = _pack_points(points)
@@ -433,6 +454,25 @@ def _split_square(buf: np.ndarray, sizes: Sequence[int]):
     return out
 
 
+def scatter_opts(**kw) -> "_capi.ScatterOptsC":
+    """The reference's dart-throwing constants (lg_scatter_opts_default), with overrides."""
+    o = _capi.ScatterOptsC()
+    _capi.load().lg_scatter_opts_default(C.byref(o))
+    for k, v in kw.items():
+        setattr(o, k, v)
+    return o
+
+
+def randgen_draws(seed: int, n: int):
+    """RandGen::operator() for the engine seeded with seed: (floats, raw uint32)."""
+    out = np.zeros(n, np.float32)
+    raw = np.zeros(n, np.uint32)
+    st = _capi.load().lg_randgen_draws(seed, n, _capi.ptr(out), _capi.ptr(raw))
+    if st != 0:
+        raise RuntimeError(f"lg_randgen_draws failed ({st})")
+    return out, raw
+
+
 # ---------------------------------------------------------------------------
 # the reference's classes
 # ---------------------------------------------------------------------------
@@ -446,6 +486,12 @@ class LightGraph:
     def __init__(self, ctx: Context, max_connect: int = 12):
         self.ctx = ctx
         self.max_connect = max_connect
+
+    def scatterPoints(self, first_iter: int, n_iter: int = 1, opts=None):
+        """LightGraph::scatterPoints (src/LightGraph.h:206-274) for n_iter
+        iterations: the point clouds and each searchRadiusConnect."""
+        pts, r2 = self.ctx.scatter_points(first_iter, n_iter, opts)
+        return pts, [float(np.sqrt(np.float32(x))) for x in r2]
 
     def __call__(self, point_clouds: Sequence[np.ndarray], search_radius: Sequence[float]):
         r2 = [np.float32(r) * np.float32(r) for r in search_radius]

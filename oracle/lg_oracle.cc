@@ -11,6 +11,8 @@
 #include <cstring>
 #include <limits>
 #include <vector>
+#include <climits>
+#include <random>
 
 namespace {
 
@@ -399,6 +401,85 @@ void illuminate(const lg_light& L, const V3& p, V3& ldir, V3& I, double& dist) {
 }  // namespace
 
 extern "C" int lgo_threads(void) { return omp_get_max_threads(); }
+
+// ---------------------------------------------------------------------------
+// scatterPoints (src/LightGraph.h:206-274) with RandGen (src/RandGen.h:16-44):
+// the same std::mt19937 engines (seeded seed_base + iteration) read through
+// std::uniform_real_distribution<float>(0, 1) of this host's C++ library, the
+// active-voxel bbox of the grid (src/main.cc:512-518) and float / double types
+// as the reference declares them.
+// ---------------------------------------------------------------------------
+extern "C" void lgo_randgen_draws(uint32_t seed, int64_t n, float* out, uint32_t* raw) {
+    std::mt19937 eng(seed), eng2(seed);
+    std::uniform_real_distribution<float> uni(0.0f, 1.0f);
+    for (int64_t k = 0; k < n; ++k) {
+        if (raw) raw[k] = (uint32_t)eng2();
+        if (out) out[k] = uni(eng);
+    }
+}
+
+extern "C" void lgo_scatter_points(const lgo_grid* dens, const lg_scatter_opts* o, int first_iter, int n_iter,
+                                   float* points, int32_t* counts, float* last_min_dist_sq) {
+    Grid g;
+    g.init(dens);
+    int vmin[3] = {INT32_MAX, INT32_MAX, INT32_MAX}, vmax[3] = {INT32_MIN, INT32_MIN, INT32_MIN};
+    for (int z = 0; z < g.dims[2]; ++z)
+        for (int y = 0; y < g.dims[1]; ++y)
+            for (int x = 0; x < g.dims[0]; ++x)
+                if (g.v[((size_t)z * g.dims[1] + y) * g.dims[0] + x] != 0.0f) {
+                    const int c[3] = {x, y, z};
+                    for (int a = 0; a < 3; ++a) {
+                        vmin[a] = std::min(vmin[a], c[a] + g.origin[a]);
+                        vmax[a] = std::max(vmax[a], c[a] + g.origin[a]);
+                    }
+                }
+    double bbmin[3];
+    float bbsize[3];
+    for (int a = 0; a < 3; ++a) {
+        bbmin[a] = g.wo[a] + (double)vmin[a] * g.h;
+        bbsize[a] = (float)((g.wo[a] + (double)vmax[a] * g.h) - bbmin[a]);
+    }
+    const float avg = (bbsize[0] + bbsize[1] + bbsize[2]) / 3.0f;
+    const float min_dist = o->min_dist_mult * avg;
+    const uint32_t batch = o->scatter_count / o->n_estimates;
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int i = 0; i < n_iter; ++i) {
+        std::mt19937 eng(o->seed_base + (uint32_t)(first_iter + i));
+        std::uniform_real_distribution<float> uni(0.0f, 1.0f);
+        std::vector<V3> pc;
+        float m2 = min_dist * min_dist, last = m2;
+        uint32_t pc_size = 0;
+        for (uint32_t n = 0; n < o->scatter_count; ++n) {
+            float np[3];
+            for (int a = 0; a < 3; ++a) np[a] = uni(eng) * bbsize[a] + bbmin[a];
+            if (pc_size > o->target_size) break;
+            if ((n + 1) % batch == 0) {
+                const uint32_t expected =
+                    o->target_size * std::pow((double)n / (double)o->scatter_count, (double)o->growth_power);
+                const double ratio = pc_size / (double)expected;
+                m2 *= ratio;
+            }
+            const V3 pt(np[0], np[1], np[2]);
+            if (g.sample_world(pt) < o->density_cutoff) continue;
+            bool collision = false;
+            for (size_t k = 0; k < pc.size(); ++k)
+                if ((pt - pc[k]).lengthSqr() < m2) { collision = true; break; }
+            if (!collision) {
+                pc.push_back(pt);
+                last = m2;
+                ++pc_size;
+            }
+        }
+        float* dst = points + (size_t)i * o->hard_limit * 3;
+        for (size_t k = 0; k < pc.size() && k < o->hard_limit; ++k) {
+            dst[3 * k] = (float)pc[k].x;
+            dst[3 * k + 1] = (float)pc[k].y;
+            dst[3 * k + 2] = (float)pc[k].z;
+        }
+        counts[i] = (int32_t)pc.size();
+        last_min_dist_sq[i] = last;
+    }
+}
 
 // ---------------------------------------------------------------------------
 // buildGraph (src/LightGraph.h:287-318)

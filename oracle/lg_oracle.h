@@ -8,6 +8,7 @@
  *
  * It restates, in FP64 C++ and in the loop order of the reference
  * (asiroisvigneux/LightGraph), the functions of the hot path:
+ *   LightGraph::scatterPoints      src/LightGraph.h:206-274   lgo_scatter_points
  *   LightGraph::buildGraph         src/LightGraph.h:287-318   lgo_build_graph
  *   LightGraph::raymarchConnection src/LightGraph.h:347-418   lgo_march_edges
  *   LightGraph::floydAlgo          src/LightGraph.h:512-542   lgo_fw_maxtimes
@@ -105,6 +106,18 @@ void lgo_render(const lgo_grid* dens, const lgo_grid* temp, const lg_shader* sh,
  * marg_func h, marg_cdf h+1, marg_int 1. */
 void lgo_env_cdf(const lgo_env* env, float* cond_func, float* cond_cdf, float* cond_int, float* marg_func,
                  float* marg_cdf, float* marg_int);
+
+/* scatterPoints for iterations first_iter .. first_iter + n_iter - 1: points
+ * (n_iter x hard_limit x 3; iteration i's counts[i] points at
+ * i * hard_limit * 3) and the squared minimum distance of each iteration's
+ * last accepted point. Uses the host C++ library's std::mt19937 and
+ * std::uniform_real_distribution<float>, as the reference's RandGen does. */
+void lgo_scatter_points(const lgo_grid* dens, const lg_scatter_opts* o, int first_iter, int n_iter,
+                        float* points, int32_t* counts, float* last_min_dist_sq);
+
+/* n draws of std::mt19937(seed): through std::uniform_real_distribution<float>
+ * (0, 1) (out) and raw (raw); either may be NULL. */
+void lgo_randgen_draws(uint32_t seed, int64_t n, float* out, uint32_t* raw);
 
 /* Number of OpenMP threads the oracle uses. */
 int lgo_threads(void);

@@ -61,6 +61,8 @@ def load() -> C.CDLL:
                                C.c_int, C.c_int, P, P, P, P, P]
     lib.lgo_env_cdf.argtypes = [C.POINTER(OEnv), P, P, P, P, P, P]
     lib.lgo_threads.restype = C.c_int
+    lib.lgo_scatter_points.argtypes = [C.POINTER(OGrid), C.c_void_p, C.c_int, C.c_int, P, P, P]
+    lib.lgo_randgen_draws.argtypes = [C.c_uint32, C.c_int64, P, P]
     _lib = lib
     return lib
 
@@ -184,6 +186,27 @@ class Oracle:
         mi = np.zeros(1, np.float32)
         self.lib.lgo_env_cdf(C.byref(self.env), *[_p(x) for x in (cf, cc, ci, mf, mc, mi)])
         return cf, cc, ci, mf, mc, mi[0]
+
+
+def scatter_points(density, opts, first_iter, n_iter):
+    """lgo_scatter_points: (points n_iter x hard_limit x 3, counts, last squared minimum distance)."""
+    lib = load()
+    vals = np.ascontiguousarray(density.values, np.float32)
+    g = OGrid(density.desc(), vals.ctypes.data)
+    pts = np.zeros((n_iter, opts.hard_limit, 3), np.float32)
+    cnt = np.zeros(n_iter, np.int32)
+    m2 = np.zeros(n_iter, np.float32)
+    lib.lgo_scatter_points(C.byref(g), C.cast(C.pointer(opts), C.c_void_p), first_iter, n_iter, _p(pts), _p(cnt),
+                           _p(m2))
+    return pts, cnt, m2
+
+
+def randgen_draws(seed, n):
+    """std::mt19937(seed) through std::uniform_real_distribution<float>(0, 1): (floats, raw)."""
+    out = np.zeros(n, np.float32)
+    raw = np.zeros(n, np.uint32)
+    load().lgo_randgen_draws(seed, n, _p(out), _p(raw))
+    return out, raw
 
 
 def fw_minplus_f32(S):
