@@ -52,7 +52,61 @@ def parse():
     ap.add_argument("--res", type=int, default=0, help="override the production grid resolution (profiling runs)")
     ap.add_argument("--serving", type=int, default=24, help="requests in the serving measurement (0: skip)")
     ap.add_argument("--rate", type=float, default=50.0, help="Poisson arrival rate of the serving stream (req/s)")
+    ap.add_argument("--ref-iters", type=int, default=500,
+                    help="LightGraph iterations of the reference-scale pipeline measurement (0: skip)")
     return ap.parse_args()
+
+
+def run_reference_scale(iterations: int, local: int, cpu: bool):
+    """The reference's own pipeline at its own scale (its explosion scene's
+    -iter 500): dart throwing of every iteration's points on the GPU, graph
+    build, edge march, batched Floyd-Warshall, vertex light, diffusion, one
+    splat of all points and the render, timed stage by stage (one warm-up
+    pass, then one timed pass)."""
+    import time
+    import torch
+    from lightgraph_gb300 import Context, scenes
+    from lightgraph_gb300.lightgraph import scatter_opts
+    sc = scenes.reference_scale(iterations)
+    ctx = Context(local)
+    scenes.load_into(ctx, sc)
+    opts = scatter_opts()
+    ms = {}
+    for rep in range(2):
+        t = {}
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        cnt = ctx.scatter_graphs(0, iterations, sc.max_connect, opts)
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        ctx.solve_graphs(want=False)
+        torch.cuda.synchronize()
+        t2 = time.perf_counter()
+        ctx.splat(0.0)
+        torch.cuda.synchronize()
+        t3 = time.perf_counter()
+        ctx.lib.lg_render(ctx.h, __import__("ctypes").byref(sc.opts.camera_c()), None, None, None, None)
+        torch.cuda.synchronize()
+        t4 = time.perf_counter()
+        ms = {"scatter_points_and_graph_build": (t1 - t0) * 1e3, "lightgraph_solve": (t2 - t1) * 1e3,
+              "splat": (t3 - t2) * 1e3, "render": (t4 - t3) * 1e3, "frame": (t4 - t0) * 1e3}
+    out = {"workload": f"{iterations} LightGraph iterations from dart throwing (1M candidates each, "
+                       f"~750 points kept), production 512^3 cumulus, dir + 3-sample env light, "
+                       f"{sc.opts.width}x{sc.opts.height} at {sc.opts.samples} spp",
+           "points": int(cnt.sum()), "points_per_iteration": [int(cnt.min()), int(cnt.max())],
+           "ms": {k: round(v, 3) for k, v in ms.items()},
+           "timing": "host wall clock around each stage with a device synchronize, second of two passes"}
+    if cpu:
+        from oracle import pyoracle as po
+        n_cpu = 16
+        t0 = time.perf_counter()
+        po.scatter_points(sc.density, opts, 0, n_cpu)
+        dt = (time.perf_counter() - t0) * 1e3
+        out["cpu_scatter_points"] = {"ms_per_frame": dt * iterations / n_cpu,
+                                     "sample": f"{n_cpu} iterations scaled x{iterations / n_cpu:g}",
+                                     "cores": int(po.load().lgo_threads()), "kind": "port"}
+    ctx.close()
+    return out
 
 
 def run_serving(n: int, rate: float):
@@ -427,6 +481,8 @@ def run_ours(args):
     }
     if rank == 0 and args.serving > 0:
         line["serving"] = run_serving(args.serving, args.rate)
+    if rank == 0 and world == 1 and args.ref_iters > 0 and not args.small:
+        line["reference_scale"] = run_reference_scale(args.ref_iters, local, not args.no_cpu_baseline)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         fw_rounds, stride = (128, 64) if not args.small else (256, 16)
         v, det, sample, threads = cpu_sample(sc, fw_rounds, stride)

@@ -12,10 +12,12 @@
 //
 // Here one CTA runs one iteration and reproduces that sequence exactly. It
 // takes the candidates a block of 208 at a time (208 x 3 = 624 draws: one
-// MT19937 state block, renewed by the CTA's threads in four dependent phases):
-//   1. every thread of a candidate computes its position and its density with
-//      the reference's sampler arithmetic (float voxel values, double weights,
-//      a float result per interpolation step);
+// MT19937 state block, renewed by the CTA's threads in four dependent phases
+// of at most 227 words):
+//   1. every thread of a candidate computes its position and its density in
+//      FP32, re-tested with the reference's sampler arithmetic (float voxel
+//      values, double weights, a float result per interpolation step) when
+//      the FP32 value is within its error bound of the cutoff;
 //   2. between two radius updates, every density-passing candidate is tested
 //      in parallel (a warp per candidate, lanes over the accepted points)
 //      against the points accepted before the segment;
@@ -33,7 +35,7 @@ namespace lg {
 
 namespace {
 
-constexpr int kDartThreads = 640;  // >= 624 (one thread per MT word)
+constexpr int kDartThreads = 512;  // >= 227 (the widest twist phase); 4 CTAs per SM
 constexpr int kDartBlock = 208;    // candidates per MT block (3 draws each)
 constexpr int kDartWarps = kDartThreads / 32;
 
@@ -58,6 +60,44 @@ __device__ float sample_exact(const DevGrid& g, double px, double py, double pz)
     return lerp(x0, x1, u);
 }
 
+// The density test without FP64 in the common case: an FP32 sample, and the
+// exact sample_exact when the FP32 value lies within its error bound of the
+// cutoff or the FP32 position lies within twice its error of a cell face
+// (where the exact position may sit in the neighbouring cell). Inside one
+// cell the trilinear sample moves by at most 3 * (max tap - min tap) per voxel
+// of position error index_err (FP32 rounding of wo, of 1 / h and of the
+// subtraction and product); the seven FP32 interpolations add under 2^-19 of
+// the largest tap.
+__device__ __forceinline__ bool density_passes(const DevGrid& g, const float p[3], const DartParams& prm) {
+    const float ix = (p[0] - prm.wo_f[0]) * prm.inv_h_f, iy = (p[1] - prm.wo_f[1]) * prm.inv_h_f,
+                iz = (p[2] - prm.wo_f[2]) * prm.inv_h_f;
+    const float fx = floorf(ix), fy = floorf(iy), fz = floorf(iz);
+    const float u = ix - fx, w = iy - fy, t = iz - fz;
+    float v[8];
+    const uint32_t rec = cell_record(g, (int)fx, (int)fy, (int)fz);
+    if (g.dtype == 1) ld_cell<1>(g.data, rec, v);
+    else if (g.dtype == 2) ld_cell<2>(g.data, rec, v);
+    else ld_cell<0>(g.data, rec, v);
+    float lo = v[0], hi = v[0];
+#pragma unroll
+    for (int k = 1; k < 8; ++k) { lo = fminf(lo, v[k]); hi = fmaxf(hi, v[k]); }
+    auto lerp = [](float a, float b, float wt) { return fmaf(b - a, wt, a); };
+    const float x0 = lerp(lerp(v[0], v[4], t), lerp(v[2], v[6], t), w);
+    const float x1 = lerp(lerp(v[1], v[5], t), lerp(v[3], v[7], t), w);
+    const float val = lerp(x0, x1, u);
+    const float e2 = 2.f * prm.index_err;
+    const bool near_face = u < e2 || u > 1.f - e2 || w < e2 || w > 1.f - e2 || t < e2 || t > 1.f - e2;
+    const float bound = 3.f * (hi - lo) * prm.index_err + fmaxf(fabsf(hi), fabsf(lo)) * 2e-6f + 1e-30f;
+    if (!near_face) {
+        if (val < prm.cutoff - bound) return false;
+        if (val > prm.cutoff + bound) return true;
+    }
+    const double dx = ((double)p[0] - prm.wo[0]) / prm.h;
+    const double dy = ((double)p[1] - prm.wo[1]) / prm.h;
+    const double dz = ((double)p[2] - prm.wo[2]) / prm.h;
+    return !(sample_exact(g, dx, dy, dz) < prm.cutoff);
+}
+
 // |a - b|^2 < m2 as the reference decides it (double arithmetic on float
 // coordinates), with an FP32 fast path outside a 2^-18 relative band.
 __device__ __forceinline__ bool closer(const float* a, const float* b, float m2) {
@@ -72,7 +112,7 @@ __device__ __forceinline__ bool closer(const float* a, const float* b, float m2)
     return e2 < (double)m2;
 }
 
-__global__ void __launch_bounds__(kDartThreads, 1) k_dart(DevGrid g, DartParams prm, const uint32_t* __restrict__ expected,
+__global__ void __launch_bounds__(kDartThreads, 4) k_dart(DevGrid g, DartParams prm, const uint32_t* __restrict__ expected,
                                                           float* __restrict__ out_pts, int32_t* __restrict__ out_count,
                                                           float* __restrict__ out_last_m2) {
     __shared__ uint32_t mt_a[kMtN], mt_b[kMtN];
@@ -105,11 +145,17 @@ __global__ void __launch_bounds__(kDartThreads, 1) k_dart(DevGrid g, DartParams 
         // i < 227 and new[i-227] after, i = 623 taking new[0] as its next
         if (tid < 227) nxt[tid] = mt_twist_word(cur[tid], cur[tid + 1], cur[tid + kMtM]);
         __syncthreads();
-        if (tid >= 227 && tid < 454) nxt[tid] = mt_twist_word(cur[tid], cur[tid + 1], nxt[tid - 227]);
+        if (tid < 227) {
+            const int i = 227 + tid;
+            nxt[i] = mt_twist_word(cur[i], cur[i + 1], nxt[i - 227]);
+        }
         __syncthreads();
-        if (tid >= 454 && tid < 623) nxt[tid] = mt_twist_word(cur[tid], cur[tid + 1], nxt[tid - 227]);
+        if (tid < 169) {
+            const int i = 454 + tid;
+            nxt[i] = mt_twist_word(cur[i], cur[i + 1], nxt[i - 227]);
+        }
         __syncthreads();
-        if (tid == 623) nxt[623] = mt_twist_word(cur[623], nxt[0], nxt[396]);
+        if (tid == 0) nxt[623] = mt_twist_word(cur[623], nxt[0], nxt[396]);
         __syncthreads();
         {
             uint32_t* t = cur;
@@ -129,10 +175,7 @@ __global__ void __launch_bounds__(kDartThreads, 1) k_dart(DevGrid g, DartParams 
                     p[a] = __double2float_rn(__dadd_rn((double)__fmul_rn(u, prm.bbsize[a]), prm.bbmin[a]));
                     cand[tid][a] = p[a];
                 }
-                const double ix = ((double)p[0] - prm.wo[0]) / prm.h;
-                const double iy = ((double)p[1] - prm.wo[1]) / prm.h;
-                const double iz = ((double)p[2] - prm.wo[2]) / prm.h;
-                ok = !(sample_exact(g, ix, iy, iz) < prm.cutoff);
+                ok = density_passes(g, p, prm);
             }
             dens_ok[tid] = ok;
         }
@@ -142,8 +185,11 @@ __global__ void __launch_bounds__(kDartThreads, 1) k_dart(DevGrid g, DartParams 
         int j0 = 0;
         const int jend = (int)min((uint32_t)kDartBlock, prm.scatter_count - base);
         while (j0 < jend && !s_done) {
-            int j1 = j0 + 1;
-            while (j1 < jend && (base + (uint32_t)j1 + 1u) % prm.batch != 0u) ++j1;
+            // next boundary after j0: the smallest n > base + j0 with
+            // (n + 1) % batch == 0
+            const uint32_t m = base + (uint32_t)j0 + 1u;
+            const uint64_t nb = ((uint64_t)(m + 1u) + prm.batch - 1u) / prm.batch * prm.batch - 1u;
+            const int j1 = (int)min((uint64_t)jend, nb - base);
             // the update belongs to candidate j0 when it is a boundary
             if (tid == 0 && (base + (uint32_t)j0 + 1u) % prm.batch == 0u) {
                 const double ratio = (double)s_pc / (double)expected[(base + j0) / prm.batch];

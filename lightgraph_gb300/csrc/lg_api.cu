@@ -690,6 +690,19 @@ lg_status Ctx::scatter_points(const lg_scatter_opts& o, int first_iter, int n_it
         prm.wo[a] = gs.desc.world_origin[a];
     }
     prm.h = gs.desc.voxel_size;
+    // FP32 fast path of the density test: index = (p - wo) * (1 / h). Its
+    // error in voxels: the rounding of wo (|wo - wo_f| / h) plus three
+    // roundings of at most 2^-24 relative (the subtraction, 1 / h, the
+    // product) on indices below max_index, doubled for margin
+    double max_index = 0.0, wo_err = 0.0;
+    for (int a = 0; a < 3; ++a) {
+        prm.wo_f[a] = (float)gs.desc.world_origin[a];
+        for (double e : {bbmin[a], bbmax[a]})
+            max_index = std::max(max_index, std::fabs((e - gs.desc.world_origin[a]) / gs.desc.voxel_size) + 2.0);
+        wo_err = std::max(wo_err, std::fabs(gs.desc.world_origin[a] - (double)prm.wo_f[a]) / gs.desc.voxel_size);
+    }
+    prm.inv_h_f = (float)(1.0 / gs.desc.voxel_size);
+    prm.index_err = (float)(2.0 * (wo_err + 3.0 * max_index * 5.9604644775390625e-8) + 1e-7);
     const size_t npts = (size_t)n_iter * o.hard_limit * 3;
     CK(d_dart_pts.reserve(sizeof(float) * npts), "dart alloc");
     CK(d_dart_cnt.reserve(sizeof(int32_t) * n_iter), "dart alloc");

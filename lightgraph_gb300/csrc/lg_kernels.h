@@ -177,6 +177,8 @@ struct DartParams {
     double bbmin[3];  // active-voxel bbox, world space
     float bbsize[3];
     double wo[3], h;  // the grid's world origin and voxel size
+    float wo_f[3], inv_h_f;  // the same in FP32 (fast path)
+    float index_err;         // bound of the FP32 index-position error (voxels)
 };
 // expected: the expected sizes at the scatter_count / batch radius updates;
 // out_pts: n_iter x hard_limit x 3 floats; out_last_m2: the squared minimum

@@ -116,6 +116,38 @@ def production(n_points: int = 4096, width: int = 1024, height: int = 1024, spp:
                  info={"res": res, "voxel": voxel, "active_voxels": int((dens > 0).sum())})
 
 
+def reference_scale(iterations: int = 500, width: int = 960, height: int = 540, spp: int = 3, res: int = 512,
+                    seed: int = 0) -> Scene:
+    """The reference's own workload shape (its explosion scene script): 500
+    LightGraph iterations whose points come from dart throwing (~750 each, one
+    splat of ~375k points), a distant light plus a 3-sample environment light,
+    3 spp at the reference's default 960x540, ptsPerKernel 2, shadow step 2,
+    cutoff 0.0025, on the production cumulus. The points are produced on the
+    GPU (lg_scatter_graphs), so `points` is empty."""
+    voxel = 1.28 / res
+    dens = volume(_capi.LGS_VOLUME_CUMULUS, res, 6, 1)
+    temp = volume(_capi.LGS_VOLUME_TEMPERATURE, res, 6, 2, 1500.0, mask=dens)
+    sh = Shader()
+    k = 20.0 * voxel
+    sh.setScattering((0.9 * k * 1.0, 0.9 * k * 1.25, 0.9 * k * 1.5))
+    sh.setAbsorption(0.1 * k)
+    sh.setVolumeColor(1.0)
+    sh.setDensityScale(0.5)
+    sh.setScatterScale(3.0 * 0.9 * k / 1.5)
+    sh.setScatterDensityScale(1.0)
+    sh.setScatterDensityMin(0.025)
+    sh.setScatterDensityMaskPower(1.0)
+    sh.setEmissionScale(3.0)
+    sh.setEmissionColorRamp(ColorRamp.parse(
+        "0.0,0.33,0.66,1.0/0,0,0:1.0,0.076,0.0:1.0,0.322,0.0:1.0,0.45,0.15/600/1500"))
+    opts = SceneSettings(width=width, height=height, samples=spp, camTranslate=(0.0, 0.0, 2.2), iter=iterations,
+                         seed=seed, cutoff=0.0025, step=(1.0, 2.0), ptsPerKernel=2)
+    lights = [Light.parse("dir:45:1,0.89,0.79:0.7:-48.8,-311.86,0"), Light.parse("env:0:1,1,1:0.35:3:sky")]
+    return Scene("reference_scale", _grid(dens, voxel), _grid(temp, voxel), sh, lights, envmap(), opts, [], [],
+                 info={"res": res, "voxel": voxel, "active_voxels": int((dens > 0).sum()),
+                       "iterations": iterations})
+
+
 def with_envmap(scene: Scene, samples: int = 3) -> Scene:
     env = envmap()
     scene.lights = list(scene.lights) + [Light.parse(f"env:0:1,1,1:0.35:{samples}:sky")]
