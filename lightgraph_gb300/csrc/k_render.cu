@@ -89,7 +89,7 @@ struct PixelSample {
 // counts the shading samples; kWrite = true accumulates the scatter and
 // emission AOVs and writes the shadow tasks at offsets[ps].
 template <bool kWrite, int DT>
-__global__ void __launch_bounds__(128, 4) k_primary(DevScene sc, DevCamera cam, DevScatterGrid sg,
+__global__ void __launch_bounds__(128, 6) k_primary(DevScene sc, DevCamera cam, DevScatterGrid sg,
                                                  int32_t* __restrict__ counts, const int32_t* __restrict__ offsets,
                                                  ShadowTask* __restrict__ tasks, int64_t task_cap,
                                                  PixelSample* __restrict__ out, unsigned long long* __restrict__ ctr) {

@@ -70,7 +70,9 @@ LG_HD Stream make_stream(uint64_t seed, uint64_t stream_id) {
 }
 
 // Draw number `key` of stream s.
-LG_HD float draw(Stream s, uint32_t key) { return u01(hash32(s.a ^ hash32(s.b + key))); }
+// The key is spread by an odd multiplier (a bijection) before the one hash,
+// so consecutive keys of a stream give independent-looking draws.
+LG_HD float draw(Stream s, uint32_t key) { return u01(hash32(s.a ^ (s.b + key * 0x9E3779B9u))); }
 
 // Sub-stream of a shadow ray: keyed by the primary iteration n, light k and
 // light sample ls (render), or by light k and sample ls with n = 0 (vertices).
@@ -85,6 +87,6 @@ LG_HD uint32_t shadow_key(Stream s, uint32_t n, uint32_t k, uint32_t ls) {
     return shadow_key_from(s.a, shadow_iter_word(s, n), k, ls);
 }
 
-LG_HD float draw_sub(uint32_t sub, uint32_t key) { return u01(hash32(sub ^ hash32(key))); }
+LG_HD float draw_sub(uint32_t sub, uint32_t key) { return u01(hash32(sub ^ (key * 0x9E3779B9u))); }
 
 }  // namespace lg

@@ -63,11 +63,11 @@ Stream make_stream(uint64_t seed, uint64_t id) {
     const uint64_t k = mix64(seed ^ mix64(id));
     return Stream{(uint32_t)k, (uint32_t)(k >> 32)};
 }
-float draw(Stream s, uint32_t key) { return u01(hash32(s.a ^ hash32(s.b + key))); }
+float draw(Stream s, uint32_t key) { return u01(hash32(s.a ^ (s.b + key * 0x9E3779B9u))); }
 uint32_t shadow_key(Stream s, uint32_t n, uint32_t k, uint32_t ls) {
     return hash32(s.a ^ hash32(s.b ^ (0x30000000u | (n & 0x0FFFFFFFu))) + k * 0x9E3779B9u + ls * 0x85EBCA6Bu);
 }
-float draw_sub(uint32_t sub, uint32_t key) { return u01(hash32(sub ^ hash32(key))); }
+float draw_sub(uint32_t sub, uint32_t key) { return u01(hash32(sub ^ (key * 0x9E3779B9u))); }
 constexpr uint64_t kDomainPixel = 0x01ull << 56, kDomainVertex = 0x02ull << 56;
 constexpr uint32_t kTagJitterX = 0x00000000u, kTagJitterY = 0x00000001u, kTagPrimarySpan = 0x10000000u,
                    kTagPrimaryStep = 0x20000000u, kTagShadowSpan = 0x40000000u, kTagShadowStep = 0x50000000u,
