@@ -292,6 +292,14 @@ lg_status lg_get_scatter_grid(lg_ctx* ctx, int32_t dims[3], int32_t origin[3],
 /* Vertex light / diffuse radiance of all loaded points (sum(N_g) x 3). */
 lg_status lg_get_vertex_data(lg_ctx* ctx, float* light_out, float* diffuse_out);
 
+/* LightGraph::outputDebugGeo (src/LightGraph.h:604-696), the -geoDump flag:
+ * for every loaded graph g writes dir/stem_{pc,edge,marching,light,diffuse}_NNNN.txt
+ * with NNNN = first_iter + g: point positions, edges (i < j, row-major order),
+ * the solved and column-normalised RGB path weights of those edges, and the
+ * direct and diffused vertex radiance, one comma-separated line each
+ * (6 significant digits). Needs lg_solve_graphs first; creates dir. */
+lg_status lg_geo_dump(lg_ctx* ctx, const char* dir, const char* stem, int first_iter);
+
 /* ------------------------------------------------------------------------- */
 /* Stage 3: render (VolumeRender::render / operator(), src/Renderer.h:496-693) */
 /* ------------------------------------------------------------------------- */

@@ -119,6 +119,7 @@ SIGNATURES = {
     "lg_point_voxel_size": (D, [I64, P, C.c_int]),
     "lg_get_scatter_grid": (I32, [P, P, P, P]),
     "lg_get_vertex_data": (I32, [P, P, P]),
+    "lg_geo_dump": (I32, [P, C.c_char_p, C.c_char_p, C.c_int]),
     "lg_render": (I32, [P, C.POINTER(CameraC), P, P, P, P]),
     "lg_render_frame": (I32, [P, C.c_int, P, P, P, C.c_int, D, C.POINTER(CameraC), P, P, P, P]),
     "lg_frame_device": (I32, [P, C.c_int, D, C.POINTER(CameraC)]),

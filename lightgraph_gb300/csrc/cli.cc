@@ -5,7 +5,8 @@
 // OpenVDB is not available, so the volume comes from -synthetic
 // {sphere,cumulus}:<res> (seeded fBm, see lightgraph_scene.h) or from -rawIn
 // <file>:<res>:<voxelSize> (a dense res^3 float32 array, x fastest). Points are
-// injected: -points <file> (float32 x,y,z triples) or uniform interior samples
+// thrown by the reference's dart throwing on the GPU (default), or injected:
+// -points <file> (float32 x,y,z triples) or uniform interior samples
 // (-numPoints, -seed). Output is an uncompressed multi-layer EXR with the
 // reference's 13 channels (src/Image.h:47-62).
 #include <algorithm>
@@ -41,9 +42,12 @@ void print_help() {
         "-light                  : dir:yRot:r,g,b:intensity:rx,ry,rz | point:yRot:r,g,b:intensity:x,y,z |\n"
         "                          env:yRot:r,g,b:intensity:samples:sky (synthetic sky map)\n"
         "-iter                   : number of LightGraphs\n"
-        "-numPoints              : points per LightGraph (default 750)\n"
-        "-connectRadius          : connection radius in world units (default 1.7 x spacing)\n"
+        "-numPoints              : uniform interior points per LightGraph instead of dart throwing\n"
+        "-connectRadius          : connection radius in world units for -numPoints/-points\n"
+        "                          (default 1.7 x spacing)\n"
         "-points                 : float32 x,y,z file (one graph per -iter slice)\n"
+        "                          (default: the reference's dart throwing, on the GPU)\n"
+        "-geoDump                : write the LightGraph geometry to geoDump/ as ASCII files\n"
         "-seed                   : seed of the points and of the render random streams\n"
         "-scatterGridResFactor -ptsPerKernel -densityScale -densityMax -shadowDensityScale\n"
         "-scatterDensityScale -scatterDensityMin -absorption -scattering -volumeColor\n"
@@ -137,7 +141,8 @@ int main(int argc, char** argv) {
     std::vector<lg_light> lights;
     std::string exr_out = "lightgraph.exr", synthetic = "sphere:128", raw_in, points_file;
     double absorption[3] = {0.1, 0.1, 0.1}, scattering[3] = {1.5, 1.5, 1.5}, color[3] = {1, 1, 1};
-    int num_points = 750, dtype = LG_DTYPE_F32;
+    int num_points = 0, dtype = LG_DTYPE_F32;
+    bool geo_dump = false;
     double connect_radius = -1.0;
     bool verbose = false, need_env = false;
     for (int i = 1; i < argc; ++i) {
@@ -149,7 +154,7 @@ int main(int argc, char** argv) {
         double v3[3];
         if (a == "-h" || a == "-help" || a == "--help") { print_help(); return 0; }
         else if (a == "-v") verbose = true;
-        else if (a == "-geoDump") std::cout << "-geoDump: not written by this build\n";
+        else if (a == "-geoDump") geo_dump = true;
         else if (a == "-vdbIn") { std::cerr << "-vdbIn needs OpenVDB, which this build does not link; use -synthetic or -rawIn\n"; return 1; }
         else if (a == "-synthetic") synthetic = next();
         else if (a == "-rawIn") raw_in = next();
@@ -240,7 +245,17 @@ int main(int argc, char** argv) {
     // points: one graph per iteration
     std::vector<float> pts;
     std::vector<int64_t> offs(1, 0);
-    if (!points_file.empty()) {
+    const bool dart = points_file.empty() && num_points <= 0;
+    if (dart) {
+        // LightGraph::scatterPoints for every iteration, then buildGraph
+        lg_scatter_opts so;
+        lg_scatter_opts_default(&so);
+        std::vector<int32_t> counts(opts.iter);
+        const double t0 = now_s();
+        check(lg_scatter_graphs(ctx, &so, 0, opts.iter, 12, counts.data()), "dart throwing");
+        for (int g = 0; g < opts.iter; ++g) offs.push_back(offs.back() + counts[g]);
+        if (verbose) std::cout << "Point Cloud Creation: " << (now_s() - t0) << " sec" << std::endl;
+    } else if (!points_file.empty()) {
         std::ifstream f(points_file, std::ios::binary | std::ios::ate);
         const size_t n = (size_t)f.tellg() / 12;
         f.seekg(0);
@@ -256,8 +271,8 @@ int main(int argc, char** argv) {
             offs.push_back(offs.back() + got);
         }
     }
-    std::vector<float> r2(opts.iter);
-    for (int g = 0; g < opts.iter; ++g) {
+    std::vector<float> r2(dart ? 0 : opts.iter);
+    for (int g = 0; g < (dart ? 0 : opts.iter); ++g) {
         double r = connect_radius;
         if (r <= 0) {
             // 1.7 x the mean spacing of the graph's points (CONNECT_SEARCH_RADIUS_MULT)
@@ -268,8 +283,19 @@ int main(int argc, char** argv) {
         r2[g] = (float)r * (float)r;
     }
     const double t0 = now_s();
-    check(lg_build_graphs(ctx, opts.iter, pts.data(), offs.data(), r2.data(), 12, nullptr, nullptr), "build graphs");
+    if (!dart)
+        check(lg_build_graphs(ctx, opts.iter, pts.data(), offs.data(), r2.data(), 12, nullptr, nullptr),
+              "build graphs");
     check(lg_solve_graphs(ctx, nullptr), "solve graphs");
+    if (geo_dump) {
+        // file stem of the volume (the reference uses the .vdb file's stem)
+        std::string stem = raw_in.empty() ? synthetic : raw_in.substr(0, raw_in.find(':'));
+        stem = stem.substr(stem.find_last_of('/') + 1);
+        stem = stem.substr(0, stem.find('.'));
+        for (char& c : stem)
+            if (c == ':') c = '_';
+        check(lg_geo_dump(ctx, "geoDump", stem.c_str(), 0), "geo dump");
+    }
     const double t1 = now_s();
     std::cout << "LightGraphs Calculation: " << (t1 - t0) << " sec" << std::endl;
     if (verbose) std::cout << "Point Cloud size: " << offs.back() << std::endl;

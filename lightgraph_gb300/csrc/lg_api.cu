@@ -11,6 +11,8 @@
 #include <string>
 #include <vector>
 
+#include <sys/stat.h>
+
 #include "lg_ctx.h"
 #include "lg_mt.h"
 
@@ -1056,6 +1058,92 @@ extern "C" lg_status lg_get_vertex_data(lg_ctx* handle, float* light_out, float*
                            ctx->st), "D download");
     }
     CK(cudaStreamSynchronize(ctx->st), "sync");
+    return LG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// geometry dump (LightGraph::outputDebugGeo, src/LightGraph.h:604-696)
+// ---------------------------------------------------------------------------
+
+extern "C" lg_status lg_geo_dump(lg_ctx* handle, const char* dir, const char* stem, int first_iter) {
+    Ctx* ctx = reinterpret_cast<Ctx*>(handle);
+    GUARD(ctx);
+    if (!dir || !stem || first_iter < 0) return ctx->fail(LG_ERR_INVALID, "null directory or stem");
+    if (!ctx->paths_solved || !ctx->light_done || !ctx->diffuse_done)
+        return ctx->fail(LG_ERR_STATE, "the graphs are not solved (lg_solve_graphs first)");
+    const int G = ctx->n_graphs;
+    const int64_t P = ctx->n_points;
+    std::vector<float> L(3 * std::max<int64_t>(P, 1)), D(3 * std::max<int64_t>(P, 1));
+    std::vector<float> S((size_t)std::max<int64_t>(ctx->s_floats, 1));
+    std::vector<int2> edges((size_t)std::max<int64_t>(ctx->edge_slots, 1));
+    std::vector<int32_t> ecnt(G);
+    CK(cudaMemcpyAsync(L.data(), ctx->d_L.p, sizeof(float) * 3 * P, cudaMemcpyDeviceToHost, ctx->st), "L download");
+    CK(cudaMemcpyAsync(D.data(), ctx->d_D.p, sizeof(float) * 3 * P, cudaMemcpyDeviceToHost, ctx->st), "D download");
+    CK(cudaMemcpyAsync(S.data(), ctx->d_S.p, sizeof(float) * ctx->s_floats, cudaMemcpyDeviceToHost, ctx->st),
+       "S download");
+    CK(cudaMemcpyAsync(edges.data(), ctx->d_edges.p, sizeof(int2) * ctx->edge_slots, cudaMemcpyDeviceToHost, ctx->st),
+       "edge download");
+    CK(cudaMemcpyAsync(ecnt.data(), ctx->d_edge_cnt.p, sizeof(int32_t) * G, cudaMemcpyDeviceToHost, ctx->st),
+       "edge count download");
+    CK(cudaStreamSynchronize(ctx->st), "sync");
+    // create the directory if it does not exist (boost::filesystem::create_directory)
+    ::mkdir(dir, 0755);
+    const double* ext = ctx->shader.extinction;
+    char name[4096];
+    auto open = [&](const char* kind, int it) -> FILE* {
+        std::snprintf(name, sizeof name, "%s/%s_%s_%04i.txt", dir, stem, kind, it);
+        return std::fopen(name, "w");
+    };
+    // ostream's default formatting of a double: 6 significant digits
+    auto v3 = [](FILE* f, double a, double b, double c) { std::fprintf(f, "%.6g,%.6g,%.6g\n", a, b, c); };
+    for (int g = 0; g < G; ++g) {
+        const GraphInfo& gi = ctx->h_graphs[g];
+        const int n = gi.n, it = first_iter + g;
+        const float* pts = ctx->h_pts.data() + 3 * gi.pt_off;
+        FILE* f = open("pc", it);
+        if (!f) return ctx->fail(LG_ERR_INVALID, "cannot write %s", name);
+        for (int i = 0; i < n; ++i) v3(f, pts[3 * i], pts[3 * i + 1], pts[3 * i + 2]);
+        std::fclose(f);
+        // the graph's edges in (i, j) row-major order
+        std::vector<std::pair<int, int>> e;
+        for (int k = 0; k < ecnt[g]; ++k) {
+            const int2 p = edges[gi.e_off + k];
+            e.push_back({std::min(p.x, p.y), std::max(p.x, p.y)});
+        }
+        std::sort(e.begin(), e.end());
+        if (!(f = open("edge", it))) return ctx->fail(LG_ERR_INVALID, "cannot write %s", name);
+        for (auto& p : e) std::fprintf(f, "%d,%d\n", p.first, p.second);
+        std::fclose(f);
+        // the path matrix as diffuseLight leaves it: T_c = exp(ext_c * S) after
+        // the solve (diagonal 1), each column divided by max(column sum, 1)
+        const float* Sg = S.data() + gi.s_off;
+        std::vector<double> colsum(3 * (size_t)n, 0.0);
+        for (int i = 0; i < n; ++i)
+            for (int j = 0; j < n; ++j) {
+                const double sij = Sg[(size_t)i * gi.ld + j];
+                for (int c = 0; c < 3; ++c) colsum[3 * (size_t)j + c] += std::exp(ext[c] * sij);
+            }
+        if (!(f = open("marching", it))) return ctx->fail(LG_ERR_INVALID, "cannot write %s", name);
+        for (auto& p : e) {
+            const double sij = Sg[(size_t)p.first * gi.ld + p.second];
+            double t[3];
+            for (int c = 0; c < 3; ++c) t[c] = std::exp(ext[c] * sij) / std::max(colsum[3 * (size_t)p.second + c], 1.0);
+            v3(f, t[0], t[1], t[2]);
+        }
+        std::fclose(f);
+        if (!(f = open("light", it))) return ctx->fail(LG_ERR_INVALID, "cannot write %s", name);
+        for (int i = 0; i < n; ++i) {
+            const float* l = L.data() + 3 * (gi.pt_off + i);
+            v3(f, l[0], l[1], l[2]);
+        }
+        std::fclose(f);
+        if (!(f = open("diffuse", it))) return ctx->fail(LG_ERR_INVALID, "cannot write %s", name);
+        for (int i = 0; i < n; ++i) {
+            const float* d = D.data() + 3 * (gi.pt_off + i);
+            v3(f, d[0], d[1], d[2]);
+        }
+        std::fclose(f);
+    }
     return LG_OK;
 }
 
