@@ -365,6 +365,23 @@ lg_status lg_set_fw_schedule(lg_ctx* ctx, int schedule);
 lg_status lg_fw_schedule(lg_ctx* ctx, int* schedule, double* tuned_ms, int n);
 
 /* ------------------------------------------------------------------------- */
+/* Image files without the OpenEXR library                                   */
+/* ------------------------------------------------------------------------- */
+
+/* Writes an uncompressed scanline OpenEXR file of n_channels FLOAT channels
+ * (names[k], planes[k] = w*h floats, row 0 at the top), as the renderer's
+ * saveEXR writes its AOV layers (src/Image.h:47-62). */
+lg_status lg_write_exr(const char* path, int w, int h, int n_channels, const char* const* names,
+                       const float* const* planes);
+
+/* Reads an environment map the way readExr does through Imf::RgbaInputFile
+ * (src/Sampling.h:175-189): the data window's R, G, B, A as half-precision
+ * values (missing colours 0, missing alpha 1), row 0 at the top, into
+ * rgba (w*h*4 floats; NULL queries the size). Only uncompressed scanline
+ * files are readable here (LG_ERR_INVALID otherwise). */
+lg_status lg_read_exr_rgba(const char* path, int32_t* width, int32_t* height, float* rgba);
+
+/* ------------------------------------------------------------------------- */
 /* Kernel-level entry points (device pointers, caller's stream)              */
 /* ------------------------------------------------------------------------- */
 

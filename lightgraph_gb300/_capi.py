@@ -120,6 +120,8 @@ SIGNATURES = {
     "lg_get_scatter_grid": (I32, [P, P, P, P]),
     "lg_get_vertex_data": (I32, [P, P, P]),
     "lg_geo_dump": (I32, [P, C.c_char_p, C.c_char_p, C.c_int]),
+    "lg_write_exr": (I32, [C.c_char_p, C.c_int, C.c_int, C.c_int, P, P]),
+    "lg_read_exr_rgba": (I32, [C.c_char_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32), P]),
     "lg_render": (I32, [P, C.POINTER(CameraC), P, P, P, P]),
     "lg_render_frame": (I32, [P, C.c_int, P, P, P, C.c_int, D, C.POINTER(CameraC), P, P, P, P]),
     "lg_frame_device": (I32, [P, C.c_int, D, C.POINTER(CameraC)]),

@@ -30,7 +30,7 @@ ORACLE_NAME = "liblg_oracle.so"
 
 CU_SOURCES = ["lg_api.cu", "k_graph.cu", "k_march.cu", "k_fw.cu", "k_diffuse.cu", "k_splat.cu",
               "k_render.cu", "k_grid.cu", "k_dart.cu", "lg_server.cu", "lg_noalloc.cu"]
-CC_SOURCES = ["scene.cc", "lg_parse.cc"]
+CC_SOURCES = ["scene.cc", "lg_parse.cc", "lg_exr.cc"]
 CLI_SOURCE = "cli.cc"
 ORACLE_SOURCES = ["lg_oracle.cc"]
 

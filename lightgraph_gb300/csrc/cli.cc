@@ -40,7 +40,8 @@ void print_help() {
         "-primaryStep -shadowStep: voxels per sample\n"
         "-cutoff                 : float\n"
         "-light                  : dir:yRot:r,g,b:intensity:rx,ry,rz | point:yRot:r,g,b:intensity:x,y,z |\n"
-        "                          env:yRot:r,g,b:intensity:samples:sky (synthetic sky map)\n"
+        "                          env:yRot:r,g,b:intensity:samples:sky (synthetic sky map) or a path\n"
+        "                          to an uncompressed EXR env map\n"
         "-iter                   : number of LightGraphs\n"
         "-numPoints              : uniform interior points per LightGraph instead of dart throwing\n"
         "-connectRadius          : connection radius in world units for -numPoints/-points\n"
@@ -65,66 +66,6 @@ bool vec3(const char* s, double out[3]) {
 
 // Minimal OpenEXR writer: scanline, NO_COMPRESSION, FLOAT channels in
 // alphabetical order, one line per block.
-bool write_exr(const std::string& path, int w, int h, const std::vector<std::pair<std::string, const float*>>& ch_in) {
-    std::vector<std::pair<std::string, const float*>> ch = ch_in;
-    std::sort(ch.begin(), ch.end(), [](auto& a, auto& b) { return a.first < b.first; });
-    std::vector<char> hdr;
-    auto put = [&](const void* p, size_t n) { hdr.insert(hdr.end(), (const char*)p, (const char*)p + n); };
-    auto put_i32 = [&](int32_t v) { put(&v, 4); };
-    auto put_str = [&](const std::string& s) { put(s.c_str(), s.size() + 1); };
-    auto attr = [&](const std::string& name, const std::string& type, const std::vector<char>& val) {
-        put_str(name);
-        put_str(type);
-        put_i32((int32_t)val.size());
-        put(val.data(), val.size());
-    };
-    const int32_t magic = 20000630, version = 2;
-    put_i32(magic);
-    put_i32(version);
-    std::vector<char> chl;
-    for (auto& c : ch) {
-        chl.insert(chl.end(), c.first.begin(), c.first.end());
-        chl.push_back(0);
-        const int32_t pix_type = 2, sx = 1, sy = 1;  // FLOAT
-        const uint8_t plinear = 0, res[3] = {0, 0, 0};
-        chl.insert(chl.end(), (const char*)&pix_type, (const char*)&pix_type + 4);
-        chl.push_back((char)plinear);
-        chl.insert(chl.end(), (const char*)res, (const char*)res + 3);
-        chl.insert(chl.end(), (const char*)&sx, (const char*)&sx + 4);
-        chl.insert(chl.end(), (const char*)&sy, (const char*)&sy + 4);
-    }
-    chl.push_back(0);
-    attr("channels", "chlist", chl);
-    attr("compression", "compression", std::vector<char>{0});
-    const int32_t box[4] = {0, 0, w - 1, h - 1};
-    std::vector<char> bx((const char*)box, (const char*)box + 16);
-    attr("dataWindow", "box2i", bx);
-    attr("displayWindow", "box2i", bx);
-    attr("lineOrder", "lineOrder", std::vector<char>{0});
-    const float par = 1.0f, swc[2] = {0.f, 0.f}, sww = 1.0f;
-    attr("pixelAspectRatio", "float", std::vector<char>((const char*)&par, (const char*)&par + 4));
-    attr("screenWindowCenter", "v2f", std::vector<char>((const char*)swc, (const char*)swc + 8));
-    attr("screenWindowWidth", "float", std::vector<char>((const char*)&sww, (const char*)&sww + 4));
-    hdr.push_back(0);
-    std::ofstream f(path, std::ios::binary);
-    if (!f) return false;
-    f.write(hdr.data(), hdr.size());
-    const uint64_t line_bytes = 8 + (uint64_t)w * 4 * ch.size();
-    uint64_t off = hdr.size() + 8ull * h;
-    for (int y = 0; y < h; ++y) {
-        f.write((const char*)&off, 8);
-        off += line_bytes;
-    }
-    std::vector<float> row(w);
-    for (int y = 0; y < h; ++y) {
-        const int32_t yy = y, sz = (int32_t)(w * 4 * ch.size());
-        f.write((const char*)&yy, 4);
-        f.write((const char*)&sz, 4);
-        for (auto& c : ch) f.write((const char*)(c.second + (int64_t)y * w), 4 * w);
-    }
-    return (bool)f;
-}
-
 double now_s() {
     return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
 }
@@ -145,6 +86,7 @@ int main(int argc, char** argv) {
     bool geo_dump = false;
     double connect_radius = -1.0;
     bool verbose = false, need_env = false;
+    std::string env_file;
     for (int i = 1; i < argc; ++i) {
         const std::string a = argv[i];
         auto next = [&]() -> const char* {
@@ -173,7 +115,13 @@ int main(int argc, char** argv) {
             lg_light L;
             const char* spec = next();
             if (lg_parse_light(spec, &L) != LG_OK) { std::cout << spec << " is not a valid light!\n"; continue; }
-            need_env |= L.type == LG_LIGHT_ENV;
+            if (L.type == LG_LIGHT_ENV) {
+                need_env = true;
+                // env:yRot:color:intensity:samples:file -- "sky" is the synthetic map
+                const std::string sp(spec);
+                const std::string file = sp.substr(sp.find_last_of(':') + 1);
+                if (file != "sky") env_file = file;
+            }
             lights.push_back(L);
         }
         else if (a == "-iter") opts.iter = std::atoi(next());
@@ -233,8 +181,22 @@ int main(int argc, char** argv) {
     gd.voxel_size = voxel;
     check(lg_upload_grid(ctx, LG_GRID_DENSITY, &gd, dens.data(), dtype), "density upload");
     std::vector<float> env;
-    const int ew = 512, eh = 256;
-    if (need_env) {
+    int ew = 512, eh = 256;
+    if (need_env && !env_file.empty()) {
+        // an uncompressed EXR env map, read as readExr does (half RGBA)
+        int32_t w = 0, h = 0;
+        if (lg_read_exr_rgba(env_file.c_str(), &w, &h, nullptr) != LG_OK) {
+            std::cerr << "cannot read the env map " << env_file << " (uncompressed scanline EXR only)\n";
+            return 1;
+        }
+        std::vector<float> rgba((size_t)w * h * 4);
+        lg_read_exr_rgba(env_file.c_str(), &w, &h, rgba.data());
+        ew = w;
+        eh = h;
+        env.resize((size_t)w * h * 3);
+        for (size_t p = 0; p < (size_t)w * h; ++p)
+            for (int c = 0; c < 3; ++c) env[3 * p + c] = rgba[4 * p + c];
+    } else if (need_env) {
         env.resize((size_t)ew * eh * 3);
         lgs_envmap(ew, eh, 30.0, 60.0, 2.0, 50.0, env.data());
     }
@@ -319,9 +281,12 @@ int main(int argc, char** argv) {
     }
     const char* names[13] = {"R", "G", "B", "A", "direct.R", "direct.G", "direct.B", "scatter.R", "scatter.G",
                              "scatter.B", "emission.R", "emission.G", "emission.B"};
-    std::vector<std::pair<std::string, const float*>> ch;
-    for (int k = 0; k < 13; ++k) ch.push_back({names[k], planes[k].data()});
-    if (!write_exr(exr_out, cam.width, cam.height, ch)) { std::cerr << "cannot write " << exr_out << "\n"; return 1; }
+    const float* plane_ptrs[13];
+    for (int k = 0; k < 13; ++k) plane_ptrs[k] = planes[k].data();
+    if (lg_write_exr(exr_out.c_str(), cam.width, cam.height, 13, names, plane_ptrs) != LG_OK) {
+        std::cerr << "cannot write " << exr_out << "\n";
+        return 1;
+    }
     std::cout << "Writting to Disk: " << exr_out << "\n\n";
     lg_destroy(ctx);
     return 0;
