@@ -91,7 +91,11 @@ struct PanelSmem {
 //      at k' costs Dg*[k][k'] + T[k'][j], so one min-plus product (no per-k
 //      barrier) replaces the 64 sequential panel steps.
 template <bool kL2>
-__device__ __forceinline__ void fw_panel_tile(float* __restrict__ d, int n, int ld, int kb, int b, PanelSmem& sm) {
+// closed_diag: the diagonal block of round kb is already closed in d (the
+// persistent schedule closes it once, in its own item), so row and column
+// panel tiles load it instead of closing it again.
+__device__ __forceinline__ void fw_panel_tile(float* __restrict__ d, int n, int ld, int kb, int b, PanelSmem& sm,
+                                              bool closed_diag = false) {
     const int nt = (n + kKB - 1) / kKB;
     const int tid = threadIdx.x, ty = tid >> 4, tx = tid & 15;
     const int K0 = kb * kKB;
@@ -114,6 +118,13 @@ __device__ __forceinline__ void fw_panel_tile(float* __restrict__ d, int n, int 
             sm.T[r][c] = kind == 1 ? ld_or_inf<kL2>(d, n, ld, K0 + r, O0 + c) : ld_or_inf<kL2>(d, n, ld, O0 + r, K0 + c);
         }
     }
+    if (kind != 0 && closed_diag) {
+#pragma unroll
+        for (int r = 0; r < 4; ++r)
+#pragma unroll
+            for (int c = 0; c < 4; ++c) sm.Dg[ty + 16 * r][tx + 16 * c] = g[r][c];
+        __syncthreads();
+    } else {
     // publish row 0 and column 0 (owners: ty == 0 row, tx == 0 column)
 #pragma unroll
     for (int c = 0; c < 4; ++c)
@@ -171,6 +182,7 @@ __device__ __forceinline__ void fw_panel_tile(float* __restrict__ d, int n, int 
 #pragma unroll
         for (int c = 0; c < 4; ++c) sm.Dg[ty + 16 * r][tx + 16 * c] = g[r][c];
     __syncthreads();
+    }
     // 2. one min-plus product against the closed diagonal tile
     float acc[4][4];
 #pragma unroll
@@ -392,7 +404,9 @@ cudaError_t fw_solve(float* d, int n, int ld, cudaStream_t st) {
 // done (round r writes each block once, by its panel tile when the block is
 // in row or column block r, else by the update tile holding it). An item of
 // round r waits for exactly the blocks it reads:
-//   panel  (r, X)    : blocks (r, r) and X at version >= r;
+//   panel  (r, X)    : X at version >= r, and block (r, r) at version >= r
+//                      for the diagonal item (which closes it) or >= r + 1
+//                      for the row and column items (which read it closed);
 //   update (r, tile) : its A and B panel blocks (column / row block r) at
 //                      version >= r + 1 and its own blocks outside row and
 //                      column block r at version >= r.
@@ -463,7 +477,9 @@ __global__ void __launch_bounds__(256, 2) k_fw_persistent(float* __restrict__ ba
                     bi = col ? other : r;
                     bj = col ? r : other;
                 }
-                ok = wait_version(ver + r * nt + r, (uint32_t)r, err) &&
+                // the diagonal item waits for its block's round r - 1; row
+                // and column panels for the diagonal closed in round r
+                ok = wait_version(ver + r * nt + r, (uint32_t)r + (w.w > 0 ? 1u : 0u), err) &&
                      wait_version(ver + bi * nt + bj, (uint32_t)r, err);
             } else {
                 const int ti = w.w / g.nu, tj = w.w % g.nu;
@@ -485,7 +501,7 @@ __global__ void __launch_bounds__(256, 2) k_fw_persistent(float* __restrict__ ba
         if (s_abort) break;
         float* d = base + g.off;
         if (w.z == 0) {
-            fw_panel_tile<true>(d, g.n, g.ld, r, w.w, psm);
+            fw_panel_tile<true>(d, g.n, g.ld, r, w.w, psm, /*closed_diag=*/true);
         } else {
             fw_update_tile<true>(d, g.n, g.ld, r, w.w / g.nu, w.w % g.nu, As, Bs);
         }
