@@ -52,6 +52,7 @@ def parse():
     ap.add_argument("--res", type=int, default=0, help="override the production grid resolution (profiling runs)")
     ap.add_argument("--serving", type=int, default=24, help="requests in the serving measurement (0: skip)")
     ap.add_argument("--rate", type=float, default=50.0, help="Poisson arrival rate of the serving stream (req/s)")
+    ap.add_argument("--batched", type=int, default=1, help="run the 64-graph batched measurement (0: skip)")
     ap.add_argument("--ref-iters", type=int, default=500,
                     help="LightGraph iterations of the reference-scale pipeline measurement (0: skip)")
     return ap.parse_args()
@@ -105,6 +106,56 @@ def run_reference_scale(iterations: int, local: int, cpu: bool):
         out["cpu_scatter_points"] = {"ms_per_frame": dt * iterations / n_cpu,
                                      "sample": f"{n_cpu} iterations scaled x{iterations / n_cpu:g}",
                                      "cores": int(po.load().lgo_threads()), "kind": "port"}
+    ctx.close()
+    return out
+
+
+def run_batched_graphs(local: int):
+    """Many graphs of uneven size in one solve: 64 graphs, N log-uniform in
+    [256, 4096], each solve's Floyd-Warshall in one persistent launch (or per
+    round, whichever the autotuner picks), timed with CUDA events over the
+    whole LightGraph stage (graph build, edge march, Floyd-Warshall, vertex
+    light, diffusion) plus the splat, after one warm-up pass."""
+    import ctypes as C
+    import torch
+    from lightgraph_gb300 import Context, scenes
+    sc = scenes.batched_graphs()
+    ctx = Context(local)
+    scenes.load_into(ctx, sc)
+    lib = ctx.lib
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    ctx.build_graphs(sc.points, sc.radius_sq, sc.max_connect)
+    ctx.solve_graphs(want=False)
+    ctx.splat(0.0)
+    torch.cuda.synchronize()
+    lib.lg_set_profiling(ctx.h, 1)
+    reps = 3
+    buf = (C.c_double * len(STAGES))()
+    stage = np.zeros(len(STAGES))
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(reps):
+        lib.lg_frame_device(ctx.h, sc.max_connect, C.c_double(0.0), C.byref(sc.opts.camera_c()))
+        if lib.lg_stage_times(ctx.h, buf, len(STAGES)) == 0:
+            stage += np.array(buf[:])
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    lib.lg_set_profiling(ctx.h, 0)
+    stage /= reps
+    sched, tuned = ctx.fw_schedule()
+    lds = [(len(p) + 127) // 128 * 128 for p in sc.points]
+    flops = sum(2.0 * ld ** 3 for ld in lds)
+    fw_ms = float(stage[2])
+    out = {"workload": "64 LightGraphs, N log-uniform in [256, 4096] (seed 3), one 256^3 cumulus, radius 0.15, "
+                       "256^2 at 1 spp", "points": int(sum(len(p) for p in sc.points)),
+           "sizes": [int(min(len(p) for p in sc.points)), int(max(len(p) for p in sc.points))],
+           "frame_ms": ev0.elapsed_time(ev1) / reps,
+           "stages_ms": {k: round(float(v), 4) for k, v in zip(STAGES, stage)},
+           "fw": {"schedule": {0: "per-round launches", 1: "persistent 1 CTA/SM",
+                               2: "persistent 2 CTA/SM"}.get(sched, str(sched)),
+                  "autotuner_ms": [round(x, 4) for x in tuned], "tflops": flops / (fw_ms * 1e-3) / 1e12,
+                  "frac_of_nominal_fp32": flops / (fw_ms * 1e-3) / 1e12 / NOMINAL_FP32_TFLOPS},
+           "timing": "CUDA events on the frame stream, frames through lg_frame_device (graph build to render)"}
     ctx.close()
     return out
 
@@ -483,6 +534,8 @@ def run_ours(args):
         line["serving"] = run_serving(args.serving, args.rate)
     if rank == 0 and world == 1 and args.ref_iters > 0 and not args.small:
         line["reference_scale"] = run_reference_scale(args.ref_iters, local, not args.no_cpu_baseline)
+    if rank == 0 and world == 1 and args.batched and not args.small:
+        line["batched_graphs"] = run_batched_graphs(local)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         fw_rounds, stride = (128, 64) if not args.small else (256, 16)
         v, det, sample, threads = cpu_sample(sc, fw_rounds, stride)

@@ -148,6 +148,26 @@ def reference_scale(iterations: int = 500, width: int = 960, height: int = 540, 
                        "iterations": iterations})
 
 
+def batched_graphs(n_graphs: int = 64, n_min: int = 256, n_max: int = 4096, seed: int = 3, res: int = 256,
+                   radius: float = 0.15) -> Scene:
+    """Many LightGraphs of uneven size solved together: n_graphs point sets
+    with N log-uniform in [n_min, n_max] (seeded), all in one 256^3 fBm
+    cumulus (one density grid per context), connect radius 0.15."""
+    voxel = 1.28 / res
+    dens = volume(_capi.LGS_VOLUME_CUMULUS, res, 6, 1)
+    rng = np.random.default_rng(seed)
+    sizes = np.exp(rng.uniform(np.log(n_min), np.log(n_max), n_graphs)).astype(int)
+    pts = [points(dens, voxel, int(n), seed=3000 + seed * 1000 + g) for g, n in enumerate(sizes)]
+    sh = Shader()
+    k = 20.0 * voxel
+    sh.setScattering((0.9 * k, 0.9 * k * 1.1, 0.9 * k * 1.25))
+    sh.setAbsorption(0.1 * k)
+    opts = SceneSettings(width=256, height=256, samples=1, camTranslate=(0.0, 0.0, 2.2), iter=n_graphs, seed=seed)
+    lights = [Light.parse("dir:0:1,0.89,0.79:1.2:-40,30,0")]
+    return Scene("batched_graphs", _grid(dens, voxel), None, sh, lights, None, opts, pts, [radius] * n_graphs,
+                 info={"res": res, "voxel": voxel, "sizes": [int(len(p)) for p in pts]})
+
+
 def with_envmap(scene: Scene, samples: int = 3) -> Scene:
     env = envmap()
     scene.lights = list(scene.lights) + [Light.parse(f"env:0:1,1,1:0.35:{samples}:sky")]
