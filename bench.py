@@ -161,9 +161,11 @@ def run_batched_graphs(local: int):
 
 
 def run_serving(n: int, rate: float):
-    """The mixed request stream (4 resident volumes 64^3..512^3, 512..8192
-    points, 128^2..1024^2 at 1-4 spp, 1-3 lights, Poisson arrivals, seed 4)
-    served one request at a time and with continuous batching (4 slots)."""
+    """The mixed request stream (4 volumes 64^3..512^3, 512..8192 points,
+    128^2..1024^2 at 1-4 spp, 1-3 lights, Poisson arrivals, seed 4): served
+    by the server (volumes resident) one request at a time and with
+    continuous batching (8 slots), and through the plain drop-in path (each
+    request uploads its volume and renders alone)."""
     from lightgraph_gb300 import serve
     out = {"stream": f"{n} requests, Poisson {rate} req/s, seed 4, volumes 64^3-512^3, 512-8192 points, "
                      "128^2-1024^2 at 1-4 spp, 1-3 lights"}
@@ -188,6 +190,10 @@ def run_serving(n: int, rate: float):
             stats, _ = serve.run_stream(srv, stream, want_images=False, realtime=realtime)
             out[label] = stats
         srv.close()
+    # the plain drop-in path: each request uploads its volume and renders alone
+    out["standalone_capacity"] = serve.run_standalone(vs, serve.request_stream(vs, n, rate, seed=4))
+    out["capacity_batched_over_standalone"] = (out["batched_capacity"]["renders_per_s"] /
+                                               out["standalone_capacity"]["renders_per_s"])
     out["batched_over_plain_renders_per_s"] = out["batched"]["renders_per_s"] / out["plain"]["renders_per_s"]
     out["capacity_batched_over_plain"] = (out["batched_capacity"]["renders_per_s"] /
                                           out["plain_capacity"]["renders_per_s"])

@@ -199,3 +199,31 @@ def run_stream(server: Server, stream, want_images: bool = False, realtime: bool
              "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
              "mean_ms": float(lat.mean()), "queue_p50_ms": float(np.percentile(que, 50))}
     return stats, imgs
+
+
+def run_standalone(vs: VolumeSet, stream, device: int = 0):
+    """The plain drop-in path, one request at a time, as the reference runs one
+    render per invocation: upload the request's volume, then lg_render_frame
+    with the request's points and lights (host buffers in, the four films
+    out). One context is reused, so no CUDA context is created per request.
+    All requests are taken at once (throughput when the queue never drains)."""
+    from .lightgraph import Context
+    ctx = Context(device)
+    t0 = time.perf_counter()
+    lat = []
+    for _, req in stream:
+        t = time.perf_counter()
+        ctx.upload_density(vs.grids[vs.ids.index(req.volume) if vs.ids else req.volume])
+        ctx.set_shader(req.shader)
+        ctx.set_settings(req.opts)
+        ctx.set_lights(req.lights)
+        r2 = [np.float32(r) * np.float32(r) for r in req.radius]
+        ctx.render_frame(req.points, r2, req.opts, req.max_connect, req.point_voxel_size)
+        lat.append((time.perf_counter() - t) * 1e3)
+    wall = time.perf_counter() - t0
+    ctx.close()
+    lat = np.array(lat)
+    return {"requests": len(stream), "wall_s": wall, "renders_per_s": len(stream) / wall,
+            "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+            "mean_ms": float(lat.mean())}
+
