@@ -11,11 +11,15 @@
 //   (exclusive scan of the counts)
 //   k_primary<true>  : march again, accumulate the scatter and emission AOVs
 //                      and write one shadow task per shading sample
-//                      (position, pTrans * (1 - dT), loop iteration);
-//   k_shadow         : one thread per task marches its shadow rays (all light
-//                      samples); consecutive threads are consecutive samples of
-//                      one primary ray, so their shadow rays are coherent;
-//   k_resolve        : per pixel, sums the tasks in order and writes the films.
+//                      (position, pTrans * (1 - dT), stream words);
+//   k_ray_bins       : order each light's shadow rays by a light-space key
+//                      (counting sort: count, scan, scatter), so the rays in
+//                      flight are neighbouring, parallel rays;
+//   k_shadow         : one thread per (light, ordered pair of tasks) marches
+//                      that light's shadow rays (all its samples) and writes
+//                      the light's contribution to the task's slot;
+//   k_resolve        : per pixel, sums the tasks and lights in order and
+//                      writes the films.
 // Shadow rays accumulate a scalar optical depth (every channel of the
 // reference's product of exponentials is exp(-a_c * tau)) and stop when tau
 // passes the dropout depth. Random numbers come from counter-based streams
