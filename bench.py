@@ -37,6 +37,10 @@ sys.path.insert(0, ROOT)
 
 STAGES = ["build_graph", "edge_march", "floyd_warshall", "vertex_light", "diffuse", "splat", "render"]
 NOMINAL_FP32_TFLOPS = 152 * 128 * 2 * 2.070 / 1000  # GB300: SMs x FP32 lanes x 2 (FMA) x 2.07 GHz
+FW_SCHEDULES = {0: "per-round launches", 1: "persistent 1 CTA/SM", 2: "persistent 2 CTA/SM",
+                3: "symmetric persistent 1 CTA/SM", 4: "symmetric persistent 2 CTA/SM"}
+FW_KERNELS = {0: "k_fw_update+k_fw_panels", 1: "k_fw_persistent", 2: "k_fw_persistent",
+              3: "k_fw_persistent_sym+k_fw_mirror", 4: "k_fw_persistent_sym+k_fw_mirror"}
 
 
 def parse():
@@ -151,8 +155,7 @@ def run_batched_graphs(local: int):
            "sizes": [int(min(len(p) for p in sc.points)), int(max(len(p) for p in sc.points))],
            "frame_ms": ev0.elapsed_time(ev1) / reps,
            "stages_ms": {k: round(float(v), 4) for k, v in zip(STAGES, stage)},
-           "fw": {"schedule": {0: "per-round launches", 1: "persistent 1 CTA/SM",
-                               2: "persistent 2 CTA/SM"}.get(sched, str(sched)),
+           "fw": {"schedule": FW_SCHEDULES.get(sched, str(sched)),
                   "autotuner_ms": [round(x, 4) for x in tuned], "tflops": flops / (fw_ms * 1e-3) / 1e12,
                   "frac_of_nominal_fp32": flops / (fw_ms * 1e-3) / 1e12 / NOMINAL_FP32_TFLOPS},
            "timing": "CUDA events on the frame stream, frames through lg_frame_device (graph build to render)"}
@@ -527,13 +530,12 @@ def run_ours(args):
                             "shadow": wave_ms[3], "resolve": wave_ms[4]},
         "render_stage": {"ms": float(stage_ms[6]), "algorithmic_bytes": render_bytes, "achieved_gbs": render_gbs,
                          "frac": render_gbs / peaks.get("hbm_gbs")},
-        "fw_roofline": {"kernel": "k_fw_update+k_fw_panels" if fw_sched == 0 else "k_fw_persistent",
+        "fw_roofline": {"kernel": FW_KERNELS.get(fw_sched, "?"),
                         "bound": "fp32_alu", "n": int(ld),
                         "achieved": fw_tflops, "unit": "TFLOP/s", "peak": NOMINAL_FP32_TFLOPS,
                         "peak_kind": "nominal (152 SMs x 128 lanes x 2 x 2.07 GHz)",
                         "frac": fw_tflops / NOMINAL_FP32_TFLOPS,
-                        "schedule": {0: "per-round launches", 1: "persistent 1 CTA/SM",
-                                     2: "persistent 2 CTA/SM"}.get(fw_sched, str(fw_sched)),
+                        "schedule": FW_SCHEDULES.get(fw_sched, str(fw_sched)),
                         "autotuner_ms": [round(x, 4) for x in fw_tuned]},
     }
     if rank == 0 and args.serving > 0:

@@ -363,6 +363,14 @@ lg_status lg_set_fw_schedule(lg_ctx* ctx, int schedule);
 /* The schedule in use and the autotuner's timings (ms) of schedules 0, 1, 2.
  * Returns LG_ERR_TIMEOUT if a persistent solve reported a stalled queue. */
 lg_status lg_fw_schedule(lg_ctx* ctx, int* schedule, double* tuned_ms, int n);
+/* Host-only check of the persistent schedules' work queue for graphs of the
+ * given point counts (no device work). Builds the queue the solve would use
+ * (sym != 0: the symmetric solve of schedules 3 and 4) and replays it in
+ * order with the kernels' dependency waits and version updates. LG_OK when
+ * every item's waits are met by earlier items (the launch cannot deadlock)
+ * and every block is written exactly once per round; LG_ERR_STATE otherwise.
+ * *n_items (optional) receives the queue length. */
+lg_status lg_fw_queue_check(int n_graphs, const int32_t* sizes, int sym, int64_t* n_items);
 
 /* ------------------------------------------------------------------------- */
 /* Image files without the OpenEXR library                                   */

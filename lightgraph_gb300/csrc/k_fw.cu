@@ -33,6 +33,7 @@
 //                      always come earlier in the queue, so the schedule
 //                      cannot deadlock whatever the residency.
 #include <algorithm>
+#include <vector>
 
 #include "lg_kernels.h"
 
@@ -41,6 +42,7 @@ namespace lg {
 constexpr int kKB = 64;      // k-block
 constexpr int kTile = 128;   // update tile (rows and cols)
 constexpr int kApad = 2;     // float2 padding per k-pair row of the A stage
+constexpr int kPanelSlots = 3;  // column-panel slots of the symmetric solve (round r uses r % 3)
 
 __device__ __forceinline__ float min3f(float a, float b, float c) {
     float r;
@@ -72,28 +74,150 @@ __device__ __forceinline__ float ld_or_inf(const float* d, int n, int ld, int i,
     return (i < n && j < n) ? ldm<kL2>(d + (int64_t)i * ld + j) : kInf;
 }
 
+constexpr int kPS = kKB + 2;  // row stride of the panel stage (even: k-pairs are 8-byte loads)
+
 struct PanelSmem {
-    float Dg[kKB][kKB + 1];
-    float T[kKB][kKB + 1];
-    float rowk[2][kKB];  // row k / column k of the diagonal tile, double buffered
-    float colk[2][kKB];
+    float Dg[kKB][kPS];
+    float T[kKB][kPS];
 };
+
+__device__ __forceinline__ int outside16(int o, int S0) { return o < S0 ? o : o + 16; }
+
+// Closes the 64 x 64 diagonal tile D (shared memory, 256 threads) by blocked
+// FW with 16 x 16 sub-blocks s = 0..3:
+//   1. warp 0 closes sub-block (s, s) in registers: 16 steps, lane (i, half)
+//      holds 8 elements of row i and fetches row k and column k by warp
+//      shuffles (they do not change in step k because D_kk >= 0);
+//   2. the sub-block's row and column panels become min(P, Dss* (x) P) and
+//      min(P, P (x) Dss*) (computed from the old panels, written after a
+//      barrier);
+//   3. the other 48 x 48 elements take min(D, column panel (x) row panel) in
+//      place (neither panel changes in this phase).
+// 16 barriers in all instead of one per step. The products take k in pairs,
+// one add.rn.f32x2 and one 3-input min per two k.
+__device__ __forceinline__ void close_diag_blocked(float (*D)[kPS]) {
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int p = tid >> 4, q = tid & 15;
+    for (int S0 = 0; S0 < kKB; S0 += 16) {
+        if (warp == 0) {
+            const int i = lane >> 1, j0 = (lane & 1) * 8;
+            float v[8];
+#pragma unroll
+            for (int jj = 0; jj < 8; ++jj) v[jj] = D[S0 + i][S0 + j0 + jj];
+#pragma unroll
+            for (int k = 0; k < 16; ++k) {
+                const float dik = __shfl_sync(0xffffffffu, v[k & 7], 2 * i + (k >> 3));
+                float dkj[8];
+#pragma unroll
+                for (int jj = 0; jj < 8; ++jj) dkj[jj] = __shfl_sync(0xffffffffu, v[jj], 2 * k + (lane & 1));
+#pragma unroll
+                for (int jj = 0; jj < 8; ++jj) v[jj] = fminf(v[jj], dik + dkj[jj]);
+            }
+#pragma unroll
+            for (int jj = 0; jj < 8; ++jj) D[S0 + i][S0 + j0 + jj] = v[jj];
+        }
+        __syncthreads();
+        // 2. row panel elements (S0 + p, out(q + 16m)), column panel elements
+        //    (out(p + 16m), S0 + q)
+        float rp[3], cp[3];
+#pragma unroll
+        for (int m = 0; m < 3; ++m) {
+            rp[m] = D[S0 + p][outside16(q + 16 * m, S0)];
+            cp[m] = D[outside16(p + 16 * m, S0)][S0 + q];
+        }
+#pragma unroll
+        for (int kp = 0; kp < 8; ++kp) {
+            const int k = S0 + 2 * kp;
+            const float2 dp = *reinterpret_cast<const float2*>(&D[S0 + p][k]);
+            const float2 dq = make_float2(D[k][S0 + q], D[k + 1][S0 + q]);
+#pragma unroll
+            for (int m = 0; m < 3; ++m) {
+                const int j = outside16(q + 16 * m, S0), i = outside16(p + 16 * m, S0);
+                const float2 sr = __fadd2_rn(dp, make_float2(D[k][j], D[k + 1][j]));
+                rp[m] = min3f(rp[m], sr.x, sr.y);
+                const float2 sc = __fadd2_rn(*reinterpret_cast<const float2*>(&D[i][k]), dq);
+                cp[m] = min3f(cp[m], sc.x, sc.y);
+            }
+        }
+        __syncthreads();
+#pragma unroll
+        for (int m = 0; m < 3; ++m) {
+            D[S0 + p][outside16(q + 16 * m, S0)] = rp[m];
+            D[outside16(p + 16 * m, S0)][S0 + q] = cp[m];
+        }
+        __syncthreads();
+        // 3. elements (out(p + 16m), out(q + 16m'))
+        float acc[3][3];
+#pragma unroll
+        for (int m = 0; m < 3; ++m)
+#pragma unroll
+            for (int mm = 0; mm < 3; ++mm) acc[m][mm] = D[outside16(p + 16 * m, S0)][outside16(q + 16 * mm, S0)];
+#pragma unroll
+        for (int kp = 0; kp < 8; ++kp) {
+            const int k = S0 + 2 * kp;
+            float2 a[3], b[3];
+#pragma unroll
+            for (int m = 0; m < 3; ++m) {
+                a[m] = *reinterpret_cast<const float2*>(&D[outside16(p + 16 * m, S0)][k]);
+                const int j = outside16(q + 16 * m, S0);
+                b[m] = make_float2(D[k][j], D[k + 1][j]);
+            }
+#pragma unroll
+            for (int m = 0; m < 3; ++m)
+#pragma unroll
+                for (int mm = 0; mm < 3; ++mm) {
+                    const float2 sm2 = __fadd2_rn(a[m], b[mm]);
+                    acc[m][mm] = min3f(acc[m][mm], sm2.x, sm2.y);
+                }
+        }
+#pragma unroll
+        for (int m = 0; m < 3; ++m)
+#pragma unroll
+            for (int mm = 0; mm < 3; ++mm) D[outside16(p + 16 * m, S0)][outside16(q + 16 * mm, S0)] = acc[m][mm];
+        __syncthreads();
+    }
+}
+
+// One min-plus product of a panel tile against the closed diagonal tile Dg*
+// (thread (ty, tx) owns the 4 x 4 elements (ty + 16r, tx + 16c)):
+//   row panel    : acc = min(T, Dg* (x) T)
+//   column panel : acc = min(T, T (x) Dg*)
+// Every path that leaves the k-block for the last time at k' costs
+// Dg*[k][k'] + T[k'][j], so one product replaces the 64 sequential panel
+// steps. k is taken in pairs (add.rn.f32x2 + 3-input min); the minimum of the
+// same sums is exact whatever the grouping.
+__device__ __forceinline__ void panel_product(const PanelSmem& sm, bool row_panel, int ty, int tx,
+                                              float (&acc)[4][4]) {
+#pragma unroll
+    for (int r = 0; r < 4; ++r)
+#pragma unroll
+        for (int c = 0; c < 4; ++c) acc[r][c] = sm.T[ty + 16 * r][tx + 16 * c];
+    const float (*L)[kPS] = row_panel ? sm.Dg : sm.T;  // left factor (rows)
+    const float (*R)[kPS] = row_panel ? sm.T : sm.Dg;  // right factor (columns)
+#pragma unroll 4
+    for (int kp = 0; kp < kKB / 2; ++kp) {
+        float2 a[4], bb[4];
+#pragma unroll
+        for (int r = 0; r < 4; ++r) a[r] = *reinterpret_cast<const float2*>(&L[ty + 16 * r][2 * kp]);
+#pragma unroll
+        for (int c = 0; c < 4; ++c) bb[c] = make_float2(R[2 * kp][tx + 16 * c], R[2 * kp + 1][tx + 16 * c]);
+#pragma unroll
+        for (int r = 0; r < 4; ++r)
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+                const float2 sv = __fadd2_rn(a[r], bb[c]);
+                acc[r][c] = min3f(acc[r][c], sv.x, sv.y);
+            }
+    }
+}
 
 // Panel tile b of round kb: 0 = diagonal, 1..nt-1 = row panel, nt..2nt-2 =
 // column panel (the diagonal's index skipped). 256 threads, each owning the
-// 4x4 elements (ty + 16r, tx + 16c).
-//   1. The diagonal tile Dg is closed by 64 FW steps held in registers; step k
-//      only needs row k and column k, which do not change in step k, so their
-//      owners publish them to shared memory (double buffered, one barrier per
-//      step).
-//   2. With Dg* closed, the row panel is min(T, Dg* (x) T) and the column panel
-//      min(T, T (x) Dg*): every path that leaves the k-block for the last time
-//      at k' costs Dg*[k][k'] + T[k'][j], so one min-plus product (no per-k
-//      barrier) replaces the 64 sequential panel steps.
+// 4x4 elements (ty + 16r, tx + 16c) of the panel product. The diagonal tile
+// is closed in shared memory (close_diag_blocked) unless closed_diag says
+// it is already closed in d (the persistent schedule closes it once, in its
+// own item).
 template <bool kL2>
-// closed_diag: the diagonal block of round kb is already closed in d (the
-// persistent schedule closes it once, in its own item), so row and column
-// panel tiles load it instead of closing it again.
 __device__ __forceinline__ void fw_panel_tile(float* __restrict__ d, int n, int ld, int kb, int b, PanelSmem& sm,
                                               bool closed_diag = false) {
     const int nt = (n + kKB - 1) / kKB;
@@ -107,115 +231,23 @@ __device__ __forceinline__ void fw_panel_tile(float* __restrict__ d, int n, int 
         other = q < kb ? q : q + 1;
     }
     const int O0 = other * kKB;
-    float g[4][4];
-#pragma unroll
-    for (int r = 0; r < 4; ++r)
-#pragma unroll
-        for (int c = 0; c < 4; ++c) g[r][c] = ld_or_inf<kL2>(d, n, ld, K0 + ty + 16 * r, K0 + tx + 16 * c);
-    if (kind != 0) {
+    for (int e = tid; e < kKB * kKB; e += 256) {
+        const int r = e >> 6, c = e & 63;
+        sm.Dg[r][c] = ld_or_inf<kL2>(d, n, ld, K0 + r, K0 + c);
+        if (kind != 0)
+            sm.T[r][c] = kind == 1 ? ld_or_inf<kL2>(d, n, ld, K0 + r, O0 + c) : ld_or_inf<kL2>(d, n, ld, O0 + r, K0 + c);
+    }
+    __syncthreads();
+    if (kind == 0 || !closed_diag) close_diag_blocked(sm.Dg);
+    if (kind == 0) {
         for (int e = tid; e < kKB * kKB; e += 256) {
             const int r = e >> 6, c = e & 63;
-            sm.T[r][c] = kind == 1 ? ld_or_inf<kL2>(d, n, ld, K0 + r, O0 + c) : ld_or_inf<kL2>(d, n, ld, O0 + r, K0 + c);
+            if (K0 + r < n && K0 + c < n) d[(int64_t)(K0 + r) * ld + K0 + c] = sm.Dg[r][c];
         }
-    }
-    if (kind != 0 && closed_diag) {
-#pragma unroll
-        for (int r = 0; r < 4; ++r)
-#pragma unroll
-            for (int c = 0; c < 4; ++c) sm.Dg[ty + 16 * r][tx + 16 * c] = g[r][c];
-        __syncthreads();
-    } else {
-    // publish row 0 and column 0 (owners: ty == 0 row, tx == 0 column)
-#pragma unroll
-    for (int c = 0; c < 4; ++c)
-        if (ty == 0) sm.rowk[0][tx + 16 * c] = g[0][c];
-#pragma unroll
-    for (int r = 0; r < 4; ++r)
-        if (tx == 0) sm.colk[0][ty + 16 * r] = g[r][0];
-    __syncthreads();
-    // 1. close the diagonal tile in registers
-    for (int k = 0; k < kKB; ++k) {
-        const int buf = k & 1;
-        float rk[4], ck[4];
-#pragma unroll
-        for (int c = 0; c < 4; ++c) rk[c] = sm.rowk[buf][tx + 16 * c];
-#pragma unroll
-        for (int r = 0; r < 4; ++r) ck[r] = sm.colk[buf][ty + 16 * r];
-#pragma unroll
-        for (int r = 0; r < 4; ++r)
-#pragma unroll
-            for (int c = 0; c < 4; ++c) g[r][c] = fminf(g[r][c], ck[r] + rk[c]);
-        const int k1 = k + 1;
-        if (k1 < kKB) {
-            // owners of row k+1 and column k+1 publish them for the next step
-            if ((k1 & 15) == ty) {
-#pragma unroll
-                for (int r = 0; r < 4; ++r)
-                    if (ty + 16 * r == k1) {
-#pragma unroll
-                        for (int c = 0; c < 4; ++c) sm.rowk[buf ^ 1][tx + 16 * c] = g[r][c];
-                    }
-            }
-            if ((k1 & 15) == tx) {
-#pragma unroll
-                for (int c = 0; c < 4; ++c)
-                    if (tx + 16 * c == k1) {
-#pragma unroll
-                        for (int r = 0; r < 4; ++r) sm.colk[buf ^ 1][ty + 16 * r] = g[r][c];
-                    }
-            }
-        }
-        __syncthreads();
-    }
-    if (kind == 0) {
-#pragma unroll
-        for (int r = 0; r < 4; ++r)
-#pragma unroll
-            for (int c = 0; c < 4; ++c) {
-                const int gi = K0 + ty + 16 * r, gj = K0 + tx + 16 * c;
-                if (gi < n && gj < n) d[(int64_t)gi * ld + gj] = g[r][c];
-            }
         return;
     }
-#pragma unroll
-    for (int r = 0; r < 4; ++r)
-#pragma unroll
-        for (int c = 0; c < 4; ++c) sm.Dg[ty + 16 * r][tx + 16 * c] = g[r][c];
-    __syncthreads();
-    }
-    // 2. one min-plus product against the closed diagonal tile
     float acc[4][4];
-#pragma unroll
-    for (int r = 0; r < 4; ++r)
-#pragma unroll
-        for (int c = 0; c < 4; ++c) acc[r][c] = sm.T[ty + 16 * r][tx + 16 * c];
-    if (kind == 1) {
-#pragma unroll 4
-        for (int k = 0; k < kKB; ++k) {
-            float a[4], bb[4];
-#pragma unroll
-            for (int r = 0; r < 4; ++r) a[r] = sm.Dg[ty + 16 * r][k];
-#pragma unroll
-            for (int c = 0; c < 4; ++c) bb[c] = sm.T[k][tx + 16 * c];
-#pragma unroll
-            for (int r = 0; r < 4; ++r)
-#pragma unroll
-                for (int c = 0; c < 4; ++c) acc[r][c] = fminf(acc[r][c], a[r] + bb[c]);
-        }
-    } else {
-#pragma unroll 4
-        for (int k = 0; k < kKB; ++k) {
-            float a[4], bb[4];
-#pragma unroll
-            for (int r = 0; r < 4; ++r) a[r] = sm.T[ty + 16 * r][k];
-#pragma unroll
-            for (int c = 0; c < 4; ++c) bb[c] = sm.Dg[k][tx + 16 * c];
-#pragma unroll
-            for (int r = 0; r < 4; ++r)
-#pragma unroll
-                for (int c = 0; c < 4; ++c) acc[r][c] = fminf(acc[r][c], a[r] + bb[c]);
-        }
-    }
+    panel_product(sm, kind == 1, ty, tx, acc);
 #pragma unroll
     for (int r = 0; r < 4; ++r)
 #pragma unroll
@@ -531,7 +563,7 @@ __global__ void __launch_bounds__(256, 2) k_fw_persistent(float* __restrict__ ba
     }
 }
 
-size_t fw_batched_items(const FwGraph* graphs, int n_graphs, int4* items) {
+size_t fw_batched_items(const FwGraph* graphs, int n_graphs, int4* items, bool sym) {
     int max_nt = 0;
     for (int g = 0; g < n_graphs; ++g) max_nt = std::max(max_nt, graphs[g].nt);
     size_t k = 0;
@@ -539,36 +571,160 @@ size_t fw_batched_items(const FwGraph* graphs, int n_graphs, int4* items) {
         if (items) items[k] = make_int4(g, r, kind, t);
         ++k;
     };
+    // the general solve has a diagonal, row and column panel tiles per round;
+    // the symmetric one the diagonal and the column panel only
     auto panels = [&](int r) {
         for (int g = 0; g < n_graphs; ++g)
             if (r < graphs[g].nt)
-                for (int b = 0; b < 2 * graphs[g].nt - 1; ++b) emit(g, r, 0, b);
+                for (int b = 0; b < (sym ? graphs[g].nt : 2 * graphs[g].nt - 1); ++b) emit(g, r, 0, b);
     };
-    // prio: the update tiles of round r holding row or column block r + 1
-    auto updates = [&](int r, bool prio) {
+    // prio: the update tiles of round r holding row or column block r + ahead
+    auto updates = [&](int r, bool prio, int ahead) {
         for (int g = 0; g < n_graphs; ++g) {
             const FwGraph& G = graphs[g];
             if (r >= G.nt || G.nt < 2) continue;
-            const int tn = (r + 1) / 2;
+            const int tn = (r + ahead) / 2;
             for (int t = 0; t < G.nu * G.nu; ++t) {
                 const int ti = t / G.nu, tj = t % G.nu;
-                const bool p = r + 1 < G.nt && (ti == tn || tj == tn);
+                if (sym && ti > tj) continue;
+                const bool p = r + ahead < G.nt && (ti == tn || tj == tn);
                 if (p == prio) emit(g, r, 1, t);
             }
         }
     };
+    // symmetric solve: the strip blocks of round r (row / column block r + 1,
+    // the diagonal block first) as their own items
+    auto strips = [&](int r) {
+        for (int g = 0; g < n_graphs; ++g) {
+            const int nt = graphs[g].nt;
+            if (r + 1 >= nt) continue;
+            emit(g, r, 2, r + 1);
+            for (int X = 0; X < nt; ++X)
+                if (X != r && X != r + 1) emit(g, r, 2, X);
+        }
+    };
     panels(0);
     for (int r = 0; r < max_nt; ++r) {
-        updates(r, true);
-        panels(r + 1);
-        updates(r, false);
+        if (sym) {
+            // strip blocks, then the next round's panels, then the tiles that
+            // hold the next round's strip blocks, then the rest
+            strips(r);
+            panels(r + 1);
+            updates(r, true, 2);
+            updates(r, false, 2);
+        } else {
+            updates(r, true, 1);
+            panels(r + 1);
+            updates(r, false, 1);
+        }
     }
     return k;
 }
 
+// Host replay of a queue with the waits and version updates of
+// k_fw_persistent (sym = false) or k_fw_persistent_sym (sym = true), one item
+// at a time in queue order. Returns 0 when every wait of every item is
+// already met at its turn (so the persistent launch cannot deadlock, whatever
+// the residency), every block is written exactly once per round, and every
+// block ends at version nt; otherwise the 1-based index of the first item
+// that breaks one of these.
+size_t fw_queue_replay(const FwGraph* graphs, int n_graphs, const int4* items, size_t n_items, bool sym) {
+    std::vector<std::vector<uint32_t>> ver(n_graphs), done(n_graphs);
+    for (int g = 0; g < n_graphs; ++g) {
+        ver[g].assign((size_t)graphs[g].nt * graphs[g].nt, 0u);
+        done[g].assign(graphs[g].nt, 0u);
+    }
+    auto up = [](int a, int b, int nt) { return a < b ? a * nt + b : b * nt + a; };
+    for (size_t it = 0; it < n_items; ++it) {
+        const int4 w = items[it];
+        const FwGraph& G = graphs[w.x];
+        const int r = w.y, nt = G.nt;
+        std::vector<uint32_t>& v = ver[w.x];
+        bool ok = true;
+        std::vector<int> writes;
+        auto need = [&](int idx, uint32_t target) { ok = ok && v[idx] >= target; };
+        if (!sym) {
+            if (w.z == 0) {
+                int bi = r, bj = r;
+                if (w.w > 0) {
+                    int q = w.w - 1;
+                    const bool col = q >= nt - 1;
+                    if (col) q -= nt - 1;
+                    const int other = q < r ? q : q + 1;
+                    bi = col ? other : r;
+                    bj = col ? r : other;
+                }
+                need(r * nt + r, (uint32_t)r + (w.w > 0 ? 1u : 0u));
+                need(bi * nt + bj, (uint32_t)r);
+                writes.push_back(bi * nt + bj);
+            } else {
+                const int ti = w.w / G.nu, tj = w.w % G.nu;
+                for (int a = 0; a < 2; ++a) {
+                    const int bi = 2 * ti + a, bj = 2 * tj + a;
+                    if (bi < nt) need(bi * nt + r, (uint32_t)r + 1u);
+                    if (bj < nt) need(r * nt + bj, (uint32_t)r + 1u);
+                }
+                for (int a = 0; a < 2; ++a)
+                    for (int c = 0; c < 2; ++c) {
+                        const int bi = 2 * ti + a, bj = 2 * tj + c;
+                        if (bi < nt && bj < nt && bi != r && bj != r) {
+                            need(bi * nt + bj, (uint32_t)r);
+                            writes.push_back(bi * nt + bj);
+                        }
+                    }
+            }
+        } else {
+            const uint32_t n_upd = (uint32_t)(G.nu * (G.nu + 1) / 2 + G.nt - 1);
+            if (w.z == 0) {
+                int X = r;
+                if (w.w > 0) {
+                    const int q = w.w - 1;
+                    X = q < r ? q : q + 1;
+                }
+                if (r >= kPanelSlots) ok = ok && done[w.x][r - kPanelSlots] >= n_upd;
+                need(r * nt + r, (uint32_t)r + (w.w > 0 ? 1u : 0u));
+                if (w.w > 0) need(up(X, r, nt), (uint32_t)r);
+                writes.push_back(up(X, r, nt));
+            } else if (w.z == 2) {
+                const int X = w.w;
+                need(up(X, r, nt), (uint32_t)r + 1u);
+                need(up(r + 1, r, nt), (uint32_t)r + 1u);
+                need(up(X, r + 1, nt), (uint32_t)r);
+                writes.push_back(up(X, r + 1, nt));
+                ++done[w.x][r];
+            } else {
+                const int ti = w.w / G.nu, tj = w.w % G.nu;
+                if (ti > tj) ok = false;
+                for (int k = 0; k < 4; ++k) need(up(2 * (k < 2 ? ti : tj) + (k & 1), r, nt), (uint32_t)r + 1u);
+                for (int a = 0; a < 2; ++a)
+                    for (int c = 0; c < 2; ++c) {
+                        const int bi = 2 * ti + a, bj = 2 * tj + c;
+                        if (bi <= bj && bi != r && bj != r && bi != r + 1 && bj != r + 1) {
+                            need(bi * nt + bj, (uint32_t)r);
+                            writes.push_back(bi * nt + bj);
+                        }
+                    }
+                ++done[w.x][r];
+            }
+        }
+        for (int b : writes) {
+            if (v[b] != (uint32_t)r) ok = false;  // exactly one write per block and round
+            ++v[b];
+        }
+        if (!ok) return it + 1;
+    }
+    for (int g = 0; g < n_graphs; ++g) {
+        const int nt = graphs[g].nt;
+        for (int a = 0; a < nt; ++a)
+            for (int b = 0; b < nt; ++b)
+                if ((!sym || a <= b) && ver[g][(size_t)a * nt + b] != (uint32_t)nt) return n_items + 1;
+    }
+    return 0;
+}
+
 size_t fw_sync_words(const FwGraph* graphs, int n_graphs) {
     size_t w = 2;
-    for (int g = 0; g < n_graphs; ++g) w += (size_t)graphs[g].nt * graphs[g].nt;
+    for (int g = 0; g < n_graphs; ++g) w += (size_t)graphs[g].nt * graphs[g].nt + graphs[g].nt;
     return w;
 }
 
@@ -593,6 +749,421 @@ int fw_persistent_ctas_per_sm() {
     int blocks = 0;
     cudaFuncSetAttribute(k_fw_persistent, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kUpdateSmem);
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, k_fw_persistent, 256, kUpdateSmem) != cudaSuccess)
+        return 1;
+    return std::max(blocks, 1);
+}
+
+// ---------------------------------------------------------------------------
+// symmetric persistent solve
+// ---------------------------------------------------------------------------
+// LightGraph's path matrices are symmetric (every edge is stored both ways,
+// src/LightGraph.h:405-406), and the recurrence keeps them exactly symmetric
+// in FP32: S_ik + S_kj and S_jk + S_ki are the same IEEE sum, so S_ij and S_ji
+// see bit-identical candidates in every round. This solve therefore keeps only
+// the 64 x 64 blocks on and above the diagonal up to date (block (a, b) with
+// a > b is read as the transpose of block (b, a)) and mirrors them below the
+// diagonal at the end: half the update tiles of the general solve, with
+// results identical to it.
+//
+// Round r:
+//   diagonal item : closes block (r, r);
+//   panel item X  : block (X, r) = min(T, T (x) Dg*) with T = S[X-block][r-block]
+//                   (stored as block (r, X) transposed when X > r);
+//   strip item X  : block (X, r + 1), the blocks round r + 1's diagonal and
+//                   panel items read, updated on their own right after the
+//                   panels (64 x 64 items instead of whole update tiles on
+//                   the round-to-round critical path);
+//   update tile   : (ti <= tj), C = S[I][J] on and above the diagonal outside
+//                   row / column blocks r and r + 1,
+//                   C = min(C, A (x) B) with A = S[I][r-block] and, by symmetry,
+//                   B = S[r-block][J] = (S[J][r-block])^T.
+// Both operands are rows of the round's column panel S[*][r-block]. The panel
+// items write that panel, in the k-pair form the update tiles consume, to one
+// of three slots (round r uses slot r % 3):
+//   slot[ti][kp][i] = {S[128 ti + i][64 r + 2 kp], S[128 ti + i][64 r + 2 kp + 1]}
+// so an update tile stages each operand with one contiguous 32 KB copy and
+// never reads the column blocks that round r + 1 rewrites. A panel item of
+// round r reuses slot r % 3 only after all update tiles and strip items of
+// round r - 3 are done (per-round counters after the block versions).
+// Queue order per round: strips(r), panels(r + 1), the update tiles of round
+// r holding row / column block r + 2 (the next strips' blocks), the rest.
+
+
+size_t fw_panel_words(const FwGraph& g) { return (size_t)kPanelSlots * g.nu * 32 * kTile; }
+
+__device__ __forceinline__ int up_block(int a, int b, int nt) { return a < b ? a * nt + b : b * nt + a; }
+
+// Diagonal (b = 0) or column panel item b >= 1 of round kb (block X = the
+// b-th block other than kb). 256 threads; the result goes back to its block
+// above the diagonal and into the round's panel slot Pr.
+__device__ __noinline__ void fw_panel_tile_sym(float* __restrict__ d, int ld, int kb, int b,
+                                                  float2* __restrict__ Pr, PanelSmem& sm) {
+    const int tid = threadIdx.x, ty = tid >> 4, tx = tid & 15;
+    const int K0 = kb * kKB;
+    int X = kb;
+    if (b > 0) {
+        const int q = b - 1;
+        X = q < kb ? q : q + 1;
+    }
+    const int X0 = X * kKB;
+    if (b == 0) {
+        for (int e = tid; e < kKB * kKB; e += 256) {
+            const int r = e >> 6, c = e & 63;
+            sm.T[r][c] = __ldcg(d + (int64_t)(K0 + r) * ld + K0 + c);
+        }
+        __syncthreads();
+        close_diag_blocked(sm.T);
+    } else {
+        for (int e = tid; e < kKB * kKB; e += 256) {
+            const int r = e >> 6, c = e & 63;
+            if (X < kb) sm.T[r][c] = __ldcg(d + (int64_t)(X0 + r) * ld + K0 + c);
+            else sm.T[c][r] = __ldcg(d + (int64_t)(K0 + r) * ld + X0 + c);
+            sm.Dg[r][c] = __ldcg(d + (int64_t)(K0 + r) * ld + K0 + c);
+        }
+        __syncthreads();
+        float acc[4][4];
+        panel_product(sm, false, ty, tx, acc);
+        __syncthreads();
+#pragma unroll
+        for (int r = 0; r < 4; ++r)
+#pragma unroll
+            for (int c = 0; c < 4; ++c) sm.T[ty + 16 * r][tx + 16 * c] = acc[r][c];
+        __syncthreads();
+    }
+    // the block above the diagonal (transposed when X > kb)
+    for (int e = tid; e < kKB * kKB; e += 256) {
+        const int r = e >> 6, c = e & 63;
+        if (X <= kb) d[(int64_t)(X0 + r) * ld + K0 + c] = sm.T[r][c];
+        else d[(int64_t)(K0 + r) * ld + X0 + c] = sm.T[c][r];
+    }
+    // the rows of block X in the panel slot
+    float2* dst = Pr + (size_t)(X >> 1) * 32 * kTile + (X & 1) * kKB;
+    for (int e = tid; e < 32 * kKB; e += 256) {
+        const int kp = e >> 6, i = e & 63;
+        dst[kp * kTile + i] = *reinterpret_cast<const float2*>(&sm.T[i][2 * kp]);
+    }
+}
+
+// Strip block (a, b), a <= b, of round kb: one of the 64 x 64 blocks in row
+// or column block kb + 1, which round kb + 1's diagonal and panel items read.
+// It runs as its own item right after round kb's panels, so that the next
+// round does not wait for whole update tiles:
+//   C = min(C, A (x) B^T), A / B = the panel-slot rows of block a / b.
+// 256 threads, each owning the 4 x 4 elements (ty + 16r, tx + 16c), k in
+// pairs (add.rn.f32x2 + 3-input min) as in the update tiles.
+__device__ __forceinline__ void fw_strip_tile_sym(float* __restrict__ d, int ld, int a, int b,
+                                                  const float2* __restrict__ Pr, float2* __restrict__ As,
+                                                  float2* __restrict__ Bs) {
+    const int tid = threadIdx.x, ty = tid >> 4, tx = tid & 15;
+    const float4* pa = reinterpret_cast<const float4*>(Pr + (size_t)(a >> 1) * 32 * kTile + (a & 1) * kKB);
+    const float4* pb = reinterpret_cast<const float4*>(Pr + (size_t)(b >> 1) * 32 * kTile + (b & 1) * kKB);
+    // As[kp][i] = {S[64a + i][k], S[64a + i][k + 1]}: 32 k-pairs x 32 float4
+#pragma unroll
+    for (int m = 0; m < 4; ++m) {
+        const int e = tid + 256 * m, kp = e >> 5, i2 = e & 31;
+        reinterpret_cast<float4*>(As)[e] = __ldcg(pa + kp * (kTile / 2) + i2);
+        reinterpret_cast<float4*>(Bs)[e] = __ldcg(pb + kp * (kTile / 2) + i2);
+    }
+    float acc[4][4];
+#pragma unroll
+    for (int r = 0; r < 4; ++r)
+#pragma unroll
+        for (int c = 0; c < 4; ++c) acc[r][c] = __ldcg(d + (int64_t)(a * kKB + ty + 16 * r) * ld + b * kKB + tx + 16 * c);
+    __syncthreads();
+#pragma unroll 4
+    for (int kp = 0; kp < 32; ++kp) {
+        float2 av[4], bv[4];
+#pragma unroll
+        for (int r = 0; r < 4; ++r) av[r] = As[kp * kKB + ty + 16 * r];
+#pragma unroll
+        for (int c = 0; c < 4; ++c) bv[c] = Bs[kp * kKB + tx + 16 * c];
+#pragma unroll
+        for (int r = 0; r < 4; ++r)
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+                const float2 sv = __fadd2_rn(av[r], bv[c]);
+                acc[r][c] = min3f(acc[r][c], sv.x, sv.y);
+            }
+    }
+#pragma unroll
+    for (int r = 0; r < 4; ++r)
+#pragma unroll
+        for (int c = 0; c < 4; ++c) d[(int64_t)(a * kKB + ty + 16 * r) * ld + b * kKB + tx + 16 * c] = acc[r][c];
+}
+
+// Update tile (ti, tj), ti <= tj, of round kb: the inner loop of
+// fw_update_tile with both operands copied from the panel slot Pr. Blocks
+// that other items of the round own (row / column block kb: panel items;
+// row / column block kb + 1: strip items) and, in a diagonal tile, the block
+// below the diagonal are neither loaded nor stored.
+__device__ __forceinline__ void fw_update_tile_sym(float* __restrict__ d, int ld, int kb, int ti, int tj,
+                                                   const float2* __restrict__ Pr, float2* __restrict__ As,
+                                                   float2* __restrict__ Bs) {
+    const int I0 = ti * kTile, J0 = tj * kTile;
+    const int tid = threadIdx.x;
+    {
+        const float4* pa = reinterpret_cast<const float4*>(Pr + (size_t)ti * 32 * kTile);
+        const float4* pb = reinterpret_cast<const float4*>(Pr + (size_t)tj * 32 * kTile);
+        float4* sa = reinterpret_cast<float4*>(As);
+        float4* sb = reinterpret_cast<float4*>(Bs);
+        float4 va[8], vb[8];
+#pragma unroll
+        for (int m = 0; m < 8; ++m) va[m] = __ldcg(pa + tid + 256 * m);
+#pragma unroll
+        for (int m = 0; m < 8; ++m) vb[m] = __ldcg(pb + tid + 256 * m);
+#pragma unroll
+        for (int m = 0; m < 8; ++m) sa[tid + 256 * m] = va[m];
+#pragma unroll
+        for (int m = 0; m < 8; ++m) sb[tid + 256 * m] = vb[m];
+    }
+    const int warp = tid >> 5, lane = tid & 31;
+    const int wy = warp >> 1, wx = warp & 1, ty = lane >> 3, tx = lane & 7;
+    const int rbase = wy * 32 + ty * 2;  // rows rbase + 8q + {0,1}
+    const int cbase = wx * 64 + tx * 2;  // cols cbase + 16p + {0,1}
+    float acc[8][8];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+#pragma unroll
+        for (int s = 0; s < 2; ++s) {
+            const int gi = I0 + rbase + 8 * q + s;
+            const int bi = gi >> 6;
+#pragma unroll
+            for (int p = 0; p < 4; ++p) {
+                const int gj = J0 + cbase + 16 * p;
+                const int bj = gj >> 6;
+                float2 v = make_float2(kInf, kInf);
+                if (bi <= bj && bi != kb && bj != kb && bi != kb + 1 && bj != kb + 1)
+                    v = __ldcg(reinterpret_cast<const float2*>(d + (int64_t)gi * ld + gj));
+                acc[2 * q + s][2 * p] = v.x;
+                acc[2 * q + s][2 * p + 1] = v.y;
+            }
+        }
+    }
+    __syncthreads();
+
+#pragma unroll 1
+    for (int kp = 0; kp < 32; ++kp) {
+        float2 a[8], b[8];
+        const float4* ap = reinterpret_cast<const float4*>(As + kp * kTile + rbase);
+        const float4* bp = reinterpret_cast<const float4*>(Bs + kp * kTile + cbase);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const float4 va = ap[4 * q];   // rows rbase + 8q, +1
+            a[2 * q] = make_float2(va.x, va.y);
+            a[2 * q + 1] = make_float2(va.z, va.w);
+            const float4 vb = bp[8 * q];   // cols cbase + 16q, +1
+            b[2 * q] = make_float2(vb.x, vb.y);
+            b[2 * q + 1] = make_float2(vb.z, vb.w);
+        }
+#pragma unroll
+        for (int r = 0; r < 8; ++r) {
+#pragma unroll
+            for (int c = 0; c < 8; ++c) {
+                const float2 s = __fadd2_rn(a[r], b[c]);
+                acc[r][c] = min3f(acc[r][c], s.x, s.y);
+            }
+        }
+    }
+
+    // store the blocks this tile owns
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+#pragma unroll
+        for (int s = 0; s < 2; ++s) {
+            const int gi = I0 + rbase + 8 * q + s;
+            const int bi = gi >> 6;
+            if (bi == kb || bi == kb + 1) continue;
+#pragma unroll
+            for (int p = 0; p < 4; ++p) {
+                const int gj = J0 + cbase + 16 * p;
+                const int bj = gj >> 6;
+                if (bj == kb || bj == kb + 1 || bi > bj) continue;
+                *reinterpret_cast<float2*>(d + (int64_t)gi * ld + gj) =
+                    make_float2(acc[2 * q + s][2 * p], acc[2 * q + s][2 * p + 1]);
+            }
+        }
+    }
+}
+
+constexpr size_t kUpdateSymSmem = sizeof(float2) * 2 * 32 * kTile;
+static_assert(sizeof(PanelSmem) <= kUpdateSymSmem, "panel items reuse the update stage");
+
+// The persistent loop of the symmetric solve: the queue, the bounded waits
+// and the error flag work as in k_fw_persistent. Waits of an item of round r:
+//   diagonal      : block (r, r) at version >= r;
+//   panel X       : block (r, r) at >= r + 1 (closed) and block (X, r) at >= r;
+//   strip X       : the column-panel blocks (X, r) and (r + 1, r) at >= r + 1,
+//                   its block (X, r + 1) at >= r;
+//   update tile   : the column-panel blocks of its four block rows / columns
+//                   at >= r + 1, the blocks it owns at >= r;
+//   panel items of round r >= 3 also wait for every update tile and strip
+//   item of round r - 3 (the last readers of their panel slot).
+// Every dependency is an item earlier in the queue, so it cannot deadlock.
+// One queue item of the symmetric solve, decoded (by thread 0, before the
+// item for its waits and again after it for its version updates, so that
+// nothing of it stays live in registers across the tile).
+struct SymItem {
+    uint32_t* ver;   // the graph's block versions
+    uint32_t* done;  // the graph's finished update tiles per round
+    int r, nt, kind, b, X, ti, tj;  // kind 0 panel (b, block X), 1 update tile (ti, tj), 2 strip block X
+    uint32_t n_upd;
+};
+
+__device__ __forceinline__ SymItem decode_sym(const int4* items, const FwGraph* gs, uint32_t* sync, int it) {
+    const int4 w = items[it];
+    const FwGraph g = gs[w.x];
+    SymItem m;
+    m.ver = sync + 2 + g.vofs;
+    m.done = m.ver + g.nt * g.nt;
+    m.r = w.y;
+    m.nt = g.nt;
+    m.kind = w.z;
+    m.b = w.w;
+    m.X = m.r;
+    if (w.z == 0 && w.w > 0) {
+        const int q = w.w - 1;
+        m.X = q < m.r ? q : q + 1;
+    }
+    if (w.z == 2) m.X = w.w;
+    m.ti = w.w / g.nu;
+    m.tj = w.w % g.nu;
+    // update tiles and strip blocks of a round that has strip blocks (every
+    // round a panel item waits for: r - 3 with r < nt)
+    m.n_upd = (uint32_t)(g.nu * (g.nu + 1) / 2 + g.nt - 1);
+    return m;
+}
+
+__global__ void __launch_bounds__(256, 2) k_fw_persistent_sym(float* __restrict__ base, const FwGraph* __restrict__ gs,
+                                                              const int4* __restrict__ items, int n_items,
+                                                              uint32_t* __restrict__ sync, float2* __restrict__ panels) {
+    extern __shared__ float4 fw_smem[];
+    float2* As = reinterpret_cast<float2*>(fw_smem);
+    float2* Bs = As + 32 * kTile;
+    PanelSmem& psm = *reinterpret_cast<PanelSmem*>(fw_smem);
+    __shared__ int s_item;
+    __shared__ int s_abort;
+    uint32_t* head = sync;
+    uint32_t* err = sync + 1;
+    for (;;) {
+        if (threadIdx.x == 0) {
+            const int it = (int)atomicAdd(head, 1u);
+            s_item = it;
+            s_abort = ld_acquire(err) != 0;
+            if (it < n_items && !s_abort) {
+                const SymItem m = decode_sym(items, gs, sync, it);
+                const int r = m.r, nt = m.nt;
+                bool ok = true;
+                if (m.kind == 0) {
+                    if (r >= kPanelSlots) ok = wait_version(m.done + (r - kPanelSlots), m.n_upd, err);
+                    ok = ok && wait_version(m.ver + r * nt + r, (uint32_t)r + (m.b > 0 ? 1u : 0u), err);
+                    if (ok && m.b > 0) ok = wait_version(m.ver + up_block(m.X, r, nt), (uint32_t)r, err);
+                } else if (m.kind == 2) {
+                    ok = wait_version(m.ver + up_block(m.X, r, nt), (uint32_t)r + 1u, err) &&
+                         wait_version(m.ver + up_block(r + 1, r, nt), (uint32_t)r + 1u, err) &&
+                         wait_version(m.ver + up_block(m.X, r + 1, nt), (uint32_t)r, err);
+                } else {
+#pragma unroll
+                    for (int k = 0; k < 4; ++k) {
+                        const int ob = 2 * (k < 2 ? m.ti : m.tj) + (k & 1);  // operand block rows
+                        ok = ok && wait_version(m.ver + up_block(ob, r, nt), (uint32_t)r + 1u, err);
+                    }
+                    for (int a = 0; a < 2 && ok; ++a)
+                        for (int c = 0; c < 2 && ok; ++c) {
+                            const int bi = 2 * m.ti + a, bj = 2 * m.tj + c;
+                            if (bi <= bj && bi != r && bj != r && bi != r + 1 && bj != r + 1)
+                                ok = wait_version(m.ver + bi * nt + bj, (uint32_t)r, err);
+                        }
+                }
+                if (!ok) s_abort = 1;
+            }
+        }
+        __syncthreads();
+        const int it = s_item;
+        if (it >= n_items || s_abort) break;
+        const int4 w = items[it];
+        const FwGraph g = gs[w.x];
+        float* d = base + g.off;
+        float2* Pr = panels + g.pofs + (size_t)(w.y % kPanelSlots) * g.nu * 32 * kTile;
+        if (w.z == 0) {
+            fw_panel_tile_sym(d, g.ld, w.y, w.w, Pr, psm);
+        } else if (w.z == 2) {
+            fw_strip_tile_sym(d, g.ld, min(w.w, w.y + 1), max(w.w, w.y + 1), Pr, As, Bs);
+        } else {
+            fw_update_tile_sym(d, g.ld, w.y, w.w / g.nu, w.w % g.nu, Pr, As, Bs);
+        }
+        __threadfence();
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            const SymItem m = decode_sym(items, gs, sync, it);
+            const int r = m.r, nt = m.nt;
+            if (m.kind == 0) {
+                atomicAdd(m.ver + up_block(m.X, r, nt), 1u);
+            } else if (m.kind == 2) {
+                atomicAdd(m.ver + up_block(m.X, r + 1, nt), 1u);
+                atomicAdd(m.done + r, 1u);
+            } else {
+                for (int a = 0; a < 2; ++a)
+                    for (int c = 0; c < 2; ++c) {
+                        const int bi = 2 * m.ti + a, bj = 2 * m.tj + c;
+                        if (bi <= bj && bi != r && bj != r && bi != r + 1 && bj != r + 1)
+                            atomicAdd(m.ver + bi * nt + bj, 1u);
+                    }
+                atomicAdd(m.done + r, 1u);
+            }
+        }
+    }
+}
+
+// Copies every block above the diagonal to its mirror below it (one 64 x 64
+// block per CTA and step, through shared memory so both sides are coalesced).
+__global__ void __launch_bounds__(256) k_fw_mirror(float* __restrict__ base, const FwGraph* __restrict__ gs) {
+    __shared__ float tile[kKB][kKB + 1];
+    const FwGraph g = gs[blockIdx.y];
+    const int nt = g.nt;
+    float* d = base + g.off;
+    for (int t = blockIdx.x; t < nt * nt; t += gridDim.x) {
+        const int bi = t / nt, bj = t % nt;
+        if (bi >= bj) continue;
+        for (int e = threadIdx.x; e < kKB * kKB; e += 256) {
+            const int r = e >> 6, c = e & 63;
+            tile[r][c] = d[(int64_t)(bi * kKB + r) * g.ld + bj * kKB + c];
+        }
+        __syncthreads();
+        for (int e = threadIdx.x; e < kKB * kKB; e += 256) {
+            const int r = e >> 6, c = e & 63;
+            d[(int64_t)(bj * kKB + r) * g.ld + bi * kKB + c] = tile[c][r];
+        }
+        __syncthreads();
+    }
+}
+
+cudaError_t fw_solve_batched_sym(float* base, const FwGraph* graphs, int n_graphs, int max_nt, const int4* items,
+                                 int n_items, uint32_t* sync, size_t sync_words, float2* panels, int ctas,
+                                 cudaStream_t st) {
+    static bool attr_set = false;
+    if (!attr_set) {
+        cudaError_t e = cudaFuncSetAttribute(k_fw_persistent_sym, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)kUpdateSymSmem);
+        if (e != cudaSuccess) return e;
+        attr_set = true;
+    }
+    cudaError_t e = cudaMemsetAsync(sync, 0, sizeof(uint32_t) * sync_words, st);
+    if (e != cudaSuccess) return e;
+    if (n_items == 0) return cudaSuccess;
+    k_fw_persistent_sym<<<ctas, 256, kUpdateSymSmem, st>>>(base, graphs, items, n_items, sync, panels);
+    ++g_launch_counter;
+    if (max_nt > 1) {
+        k_fw_mirror<<<dim3(std::min(max_nt * max_nt, 4096), n_graphs), 256, 0, st>>>(base, graphs);
+        ++g_launch_counter;
+    }
+    return cudaGetLastError();
+}
+
+int fw_persistent_sym_ctas_per_sm() {
+    int blocks = 0;
+    cudaFuncSetAttribute(k_fw_persistent_sym, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kUpdateSymSmem);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, k_fw_persistent_sym, 256, kUpdateSymSmem) !=
+        cudaSuccess)
         return 1;
     return std::max(blocks, 1);
 }

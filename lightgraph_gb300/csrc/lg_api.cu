@@ -835,7 +835,10 @@ lg_status Ctx::march_edges() {
 }
 
 // Schedules of the path solve: 0 = two launches per round per graph
-// (fw_solve), k >= 1 = one persistent launch for all graphs with k CTAs per SM.
+// (fw_solve); 1, 2 = one persistent launch for all graphs with 1 or 2 CTAs per
+// SM; 3, 4 = the symmetric persistent solve (the tiles on and above the
+// diagonal, then a mirror pass) with 1 or 2 CTAs per SM. The graph matrices
+// are symmetric by construction (k_march.cu stores every edge both ways).
 static lg_status run_fw_schedule(Ctx* ctx, float* base, int choice) {
     if (choice == 0) {
         for (const GraphInfo& g : ctx->h_graphs) {
@@ -846,6 +849,13 @@ static lg_status run_fw_schedule(Ctx* ctx, float* base, int choice) {
     }
     int sms = 0;
     CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device), "device query");
+    if (choice >= 3) {
+        CK(fw_solve_batched_sym(base, ctx->d_fwg.as<FwGraph>(), ctx->n_graphs, ctx->fw_max_nt,
+                                ctx->d_fw_items_sym.as<int4>(), ctx->fw_items_sym_n, ctx->d_fw_sync.as<uint32_t>(),
+                                ctx->fw_sync_n, ctx->d_fw_panels.as<float2>(), (choice - 2) * sms, ctx->st),
+           "symmetric batched floyd-warshall");
+        return LG_OK;
+    }
     CK(fw_solve_batched(base, ctx->d_fwg.as<FwGraph>(), ctx->d_fw_items.as<int4>(), ctx->fw_items_n,
                         ctx->d_fw_sync.as<uint32_t>(), ctx->fw_sync_n, choice * sms, ctx->st),
        "batched floyd-warshall");
@@ -856,7 +866,8 @@ lg_status Ctx::solve_paths_batched(int choice) {
     Ctx* ctx = this;
     if (!fw_queue_valid) {
         std::vector<FwGraph> fg(n_graphs);
-        int64_t vofs = 0;
+        int64_t vofs = 0, pofs = 0;
+        fw_max_nt = 0;
         for (int g = 0; g < n_graphs; ++g) {
             const GraphInfo& gi = h_graphs[g];
             fg[g].off = gi.s_off;
@@ -865,20 +876,31 @@ lg_status Ctx::solve_paths_batched(int choice) {
             fg[g].nt = gi.n == 0 ? 0 : gi.ld / 64;
             fg[g].nu = gi.n == 0 ? 0 : gi.ld / 128;
             fg[g].vofs = vofs;
-            vofs += (int64_t)fg[g].nt * fg[g].nt;
+            fg[g].pofs = pofs;
+            vofs += (int64_t)fg[g].nt * fg[g].nt + fg[g].nt;
+            pofs += (int64_t)fw_panel_words(fg[g]);
+            fw_max_nt = std::max(fw_max_nt, fg[g].nt);
         }
         const size_t n_items = fw_batched_items(fg.data(), n_graphs, nullptr);
         std::vector<int4> items(std::max<size_t>(n_items, 1));
         fw_batched_items(fg.data(), n_graphs, items.data());
+        const size_t n_items_sym = fw_batched_items(fg.data(), n_graphs, nullptr, true);
+        std::vector<int4> items_sym(std::max<size_t>(n_items_sym, 1));
+        fw_batched_items(fg.data(), n_graphs, items_sym.data(), true);
         fw_sync_n = fw_sync_words(fg.data(), n_graphs);
         CK(d_fwg.reserve(sizeof(FwGraph) * n_graphs), "fw queue alloc");
         CK(d_fw_items.reserve(sizeof(int4) * items.size()), "fw queue alloc");
+        CK(d_fw_items_sym.reserve(sizeof(int4) * items_sym.size()), "fw queue alloc");
         CK(d_fw_sync.reserve(sizeof(uint32_t) * fw_sync_n), "fw queue alloc");
+        CK(d_fw_panels.reserve(sizeof(float2) * std::max<int64_t>(pofs, 1)), "fw panel alloc");
         CK(cudaMemcpyAsync(d_fwg.p, fg.data(), sizeof(FwGraph) * n_graphs, cudaMemcpyHostToDevice, st), "fw queue upload");
         CK(cudaMemcpyAsync(d_fw_items.p, items.data(), sizeof(int4) * items.size(), cudaMemcpyHostToDevice, st),
            "fw queue upload");
+        CK(cudaMemcpyAsync(d_fw_items_sym.p, items_sym.data(), sizeof(int4) * items_sym.size(),
+                           cudaMemcpyHostToDevice, st), "fw queue upload");
         CK(cudaStreamSynchronize(st), "fw queue sync");
         fw_items_n = (int)n_items;
+        fw_items_sym_n = (int)n_items_sym;
         fw_queue_valid = true;
     }
     (void)choice;
@@ -894,15 +916,17 @@ lg_status Ctx::tune_fw() {
         if (kv.first == key) { fw_choice = kv.second; return LG_OK; }
     lg_status s = solve_paths_batched(1);
     if (s != LG_OK) return s;
-    const int per_sm = fw_persistent_ctas_per_sm();
     std::vector<int> cands = {0, 1};
-    if (per_sm >= 2) cands.push_back(2);
+    if (fw_persistent_ctas_per_sm() >= 2) cands.push_back(2);
+    cands.push_back(3);
+    if (fw_persistent_sym_ctas_per_sm() >= 2) cands.push_back(4);
     CK(d_fw_tune.reserve(sizeof(float) * std::max<int64_t>(s_floats, 1)), "fw tune alloc");
     cudaEvent_t e0, e1;
     CK(cudaEventCreate(&e0), "event");
     CK(cudaEventCreate(&e1), "event");
     int best = 0;
     float best_ms = 1e30f;
+    for (double& t : fw_tune_ms) t = 0.0;
     for (size_t c = 0; c < cands.size(); ++c) {
         CK(cudaMemcpyAsync(d_fw_tune.p, d_S.p, sizeof(float) * s_floats, cudaMemcpyDeviceToDevice, st), "fw tune copy");
         CK(cudaEventRecord(e0, st), "event");
@@ -912,16 +936,21 @@ lg_status Ctx::tune_fw() {
         CK(cudaEventSynchronize(e1), "event sync");
         float ms = 0.f;
         CK(cudaEventElapsedTime(&ms, e0, e1), "event time");
-        if (c < 4) fw_tune_ms[c] = ms;
+        if (cands[c] > 0) {
+            // a persistent launch reports a stalled queue through its error flag
+            uint32_t flags[2] = {0, 0};
+            CK(cudaMemcpy(flags, d_fw_sync.p, sizeof flags, cudaMemcpyDeviceToHost), "fw flag read");
+            if (flags[1] != 0) {
+                s = fail(LG_ERR_TIMEOUT, "batched floyd-warshall: a dependency wait timed out");
+                break;
+            }
+        }
+        fw_tune_ms[cands[c]] = ms;
         if (ms < best_ms) { best_ms = ms; best = cands[c]; }
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     if (s != LG_OK) return s;
-    // a persistent launch reports a stalled queue through its error flag
-    uint32_t flags[2] = {0, 0};
-    CK(cudaMemcpy(flags, d_fw_sync.p, sizeof flags, cudaMemcpyDeviceToHost), "fw flag read");
-    if (flags[1] != 0) return fail(LG_ERR_TIMEOUT, "batched floyd-warshall: a dependency wait timed out");
     fw_tuned.push_back({key, best});
     fw_choice = best;
     return LG_OK;
@@ -1526,7 +1555,7 @@ extern "C" lg_status lg_set_graph_mode(lg_ctx* handle, int on) {
 extern "C" lg_status lg_set_fw_schedule(lg_ctx* handle, int schedule) {
     Ctx* ctx = reinterpret_cast<Ctx*>(handle);
     GUARD(ctx);
-    if (schedule < -1 || schedule > 2) return ctx->fail(LG_ERR_INVALID, "schedule must be -1, 0, 1 or 2");
+    if (schedule < -1 || schedule > 4) return ctx->fail(LG_ERR_INVALID, "schedule must be -1, 0, 1, 2, 3 or 4");
     if (schedule == -1) {
         ctx->fw_choice = -1;
         for (auto& kv : ctx->fw_tuned)
@@ -1542,7 +1571,7 @@ extern "C" lg_status lg_fw_schedule(lg_ctx* handle, int* schedule, double* tuned
     Ctx* ctx = reinterpret_cast<Ctx*>(handle);
     GUARD(ctx);
     if (schedule) *schedule = ctx->fw_choice;
-    for (int k = 0; tuned_ms && k < n && k < 4; ++k) tuned_ms[k] = ctx->fw_tune_ms[k];
+    for (int k = 0; tuned_ms && k < n && k < 5; ++k) tuned_ms[k] = ctx->fw_tune_ms[k];
     if (ctx->fw_choice > 0 && ctx->d_fw_sync.bytes >= 8) {
         uint32_t flags[2] = {0, 0};
         CK(cudaMemcpyAsync(flags, ctx->d_fw_sync.p, sizeof flags, cudaMemcpyDeviceToHost, ctx->st), "flag read");
@@ -1550,6 +1579,30 @@ extern "C" lg_status lg_fw_schedule(lg_ctx* handle, int* schedule, double* tuned
         if (flags[1] != 0) return ctx->fail(LG_ERR_TIMEOUT, "batched floyd-warshall: a dependency wait timed out");
     }
     return LG_OK;
+}
+
+extern "C" lg_status lg_fw_queue_check(int n_graphs, const int32_t* sizes, int sym, int64_t* n_items) {
+    if (n_graphs < 0 || (n_graphs > 0 && !sizes)) return LG_ERR_INVALID;
+    std::vector<FwGraph> fg(n_graphs);
+    int64_t vofs = 0, pofs = 0;
+    for (int g = 0; g < n_graphs; ++g) {
+        if (sizes[g] < 0) return LG_ERR_INVALID;
+        const int ld = (sizes[g] + 127) / 128 * 128;
+        fg[g].off = 0;
+        fg[g].n = ld;
+        fg[g].ld = ld;
+        fg[g].nt = sizes[g] == 0 ? 0 : ld / 64;
+        fg[g].nu = sizes[g] == 0 ? 0 : ld / 128;
+        fg[g].vofs = vofs;
+        fg[g].pofs = pofs;
+        vofs += (int64_t)fg[g].nt * fg[g].nt + fg[g].nt;
+        pofs += (int64_t)fw_panel_words(fg[g]);
+    }
+    const size_t n = fw_batched_items(fg.data(), n_graphs, nullptr, sym != 0);
+    std::vector<int4> items(std::max<size_t>(n, 1));
+    fw_batched_items(fg.data(), n_graphs, items.data(), sym != 0);
+    if (n_items) *n_items = (int64_t)n;
+    return fw_queue_replay(fg.data(), n_graphs, items.data(), n, sym != 0) == 0 ? LG_OK : LG_ERR_STATE;
 }
 
 extern "C" uint64_t lg_frame_launches(const lg_ctx* handle) {

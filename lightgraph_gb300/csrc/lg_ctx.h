@@ -99,14 +99,17 @@ struct Ctx {
 
     // batched Floyd-Warshall: work queue, counters and the autotuned schedule
     DevBuf d_fwg, d_fw_items, d_fw_sync, d_fw_tune;
+    DevBuf d_fw_items_sym, d_fw_panels;  // symmetric solve: its queue and column-panel slots
     int fw_items_n = 0;
+    int fw_items_sym_n = 0;
+    int fw_max_nt = 0;
     size_t fw_sync_n = 2;  // uint32 words of d_fw_sync
     bool fw_queue_valid = false;
     // schedule per (graph count, largest n): 0 = per-graph launches,
     // k > 0 = persistent with k CTAs per SM
     std::vector<std::pair<std::pair<int, int>, int>> fw_tuned;
     int fw_choice = -1;
-    double fw_tune_ms[4] = {0, 0, 0, 0};
+    double fw_tune_ms[5] = {0, 0, 0, 0, 0};
 
     // frame replay through a captured CUDA graph
     bool graph_mode = false;

@@ -47,16 +47,32 @@ struct FwGraph {
     int32_t n, ld;
     int32_t nt;    // k-blocks of 64
     int32_t nu;    // update tiles of 128 per side
-    int64_t vofs;  // first of the graph's nt^2 block version counters
+    int64_t vofs;  // first of the graph's nt^2 block version counters and nt round counters
+    int64_t pofs;  // first float2 of the graph's column-panel slots (symmetric solve)
 };
-// Writes the work queue (if items != null) and returns its length.
-size_t fw_batched_items(const FwGraph* graphs, int n_graphs, int4* items);
-// uint32 words of the batched solve's sync buffer: 2 + sum of nt^2.
+// Writes the work queue (if items != null) and returns its length. sym: the
+// queue of the symmetric solve (tiles on and above the diagonal only).
+size_t fw_batched_items(const FwGraph* graphs, int n_graphs, int4* items, bool sym = false);
+// Host replay of a queue with the kernels' waits and version updates in
+// queue order: 0 if it cannot deadlock and writes every block once per round,
+// else the 1-based index of the first offending item (n_items + 1: a block
+// missed a round).
+size_t fw_queue_replay(const FwGraph* graphs, int n_graphs, const int4* items, size_t n_items, bool sym);
+// uint32 words of the batched solve's sync buffer: 2 + sum of nt^2 + nt.
 size_t fw_sync_words(const FwGraph* graphs, int n_graphs);
+// float2 words of one graph's column-panel slots (symmetric solve).
+size_t fw_panel_words(const FwGraph& g);
 // sync: fw_sync_words uint32 (cleared here). ctas: persistent CTAs.
 cudaError_t fw_solve_batched(float* base, const FwGraph* graphs, const int4* items, int n_items, uint32_t* sync,
                              size_t sync_words, int ctas, cudaStream_t st);
+// The same solve for symmetric matrices (every S_ij == S_ji, as LightGraph's
+// path matrices are): computes the tiles on and above the diagonal and then
+// mirrors them below it. panels: sum of fw_panel_words float2.
+cudaError_t fw_solve_batched_sym(float* base, const FwGraph* graphs, int n_graphs, int max_nt, const int4* items,
+                                 int n_items, uint32_t* sync, size_t sync_words, float2* panels, int ctas,
+                                 cudaStream_t st);
 int fw_persistent_ctas_per_sm();
+int fw_persistent_sym_ctas_per_sm();
 cudaError_t launch_set_diag(float* S, const GraphInfo* graphs, int n_graphs, int max_n,
                             cudaStream_t st);
 

@@ -410,13 +410,14 @@ class Context:
         self._ck(self.lib.lg_frame_device(self.h, max_connect, point_voxel_size, C.byref(cam)))
 
     def set_fw_schedule(self, schedule: int) -> None:
-        """-1 autotuned, 0 per-graph launches, 1/2 persistent (CTAs per SM)."""
+        """-1 autotuned, 0 per-graph launches, 1/2 persistent (CTAs per SM),
+        3/4 symmetric persistent (CTAs per SM)."""
         self._ck(self.lib.lg_set_fw_schedule(self.h, schedule))
 
     def fw_schedule(self):
         s = C.c_int()
-        ms = (C.c_double * 3)()
-        self._ck(self.lib.lg_fw_schedule(self.h, C.byref(s), ms, 3))
+        ms = (C.c_double * 5)()
+        self._ck(self.lib.lg_fw_schedule(self.h, C.byref(s), ms, 5))
         return s.value, list(ms)
 
     def set_graph_mode(self, on: bool) -> None:

@@ -103,3 +103,27 @@ def test_scene_generator_is_deterministic():
     p = scenes.points(a, 0.04, 100, seed=5)
     q = scenes.points(a, 0.04, 100, seed=5)
     assert np.array_equal(p, q) and len(p) == 100
+
+
+@pytest.mark.parametrize("sym", [0, 1])
+@pytest.mark.parametrize("sizes", [[1], [64], [128], [200], [700], [4096], [0, 300, 33, 700, 129, 1000],
+                                   [256, 4096, 512, 1300]])
+def test_fw_queue_cannot_deadlock(sizes, sym):
+    """The persistent solves' work queues, replayed on the host in order with
+    the kernels' dependency waits: every wait is met by earlier items (so no
+    residency can deadlock the launch) and every 64 x 64 block is written
+    exactly once per round."""
+    lib = _capi.load()
+    arr = np.asarray(sizes, np.int32)
+    n = C.c_int64()
+    assert lib.lg_fw_queue_check(len(arr), arr.ctypes.data, sym, C.byref(n)) == _capi.LG_OK
+    nts = [(s + 127) // 128 * 2 for s in sizes if s > 0]
+    nus = [nt // 2 for nt in nts]
+    if sym:
+        # per round: nt panel items, nt - 1 strip blocks (all but the last
+        # round), the tiles on and above the diagonal (rounds with nt >= 2)
+        want = sum(nt * nt + (nt - 1) * (nt - 1) + (nt * nu * (nu + 1) // 2 if nt >= 2 else 0)
+                   for nt, nu in zip(nts, nus))
+    else:
+        want = sum(nt * (2 * nt - 1) + (nt * nu * nu if nt >= 2 else 0) for nt, nu in zip(nts, nus))
+    assert n.value == want

@@ -35,25 +35,31 @@ def solve_with(ctx, sc, schedule):
 
 
 def test_schedules_bit_identical_and_match_oracle(gpu_ctx, uneven_graphs):
+    """Every schedule, the symmetric ones (3, 4) included, gives the same bits;
+    the graphs up to 700 points run 12 rounds, so the symmetric solve reuses
+    each of its three column-panel slots several times."""
     sc = uneven_graphs
     S0, d0, u0, _ = solve_with(gpu_ctx, sc, 0)
-    _, d1, u1, _ = solve_with(gpu_ctx, sc, 1)
-    _, d2, u2, _ = solve_with(gpu_ctx, sc, 2)
-    assert (u0, u1, u2) == (0, 1, 2)
+    assert u0 == 0
+    for schedule in (1, 2, 3, 4):
+        _, ds, us, _ = solve_with(gpu_ctx, sc, schedule)
+        assert us == schedule
+        for g in range(len(sc.points)):
+            assert np.array_equal(d0[g], ds[g]), (schedule, g)
     for g in range(len(sc.points)):
-        assert np.array_equal(d0[g], d1[g]), g
-        assert np.array_equal(d0[g], d2[g]), g
+        assert np.array_equal(S0[g], S0[g].T), g  # the solve's symmetric input
+        assert np.array_equal(d0[g], d0[g].T), g
         ref = po.fw_minplus_f32(S0[g])
         np.fill_diagonal(ref, 0.0)
         fin = np.isfinite(ref)
-        assert np.array_equal(np.isfinite(d1[g]), fin)
-        assert np.allclose(d1[g][fin], ref[fin], rtol=1e-6, atol=0), g
+        assert np.array_equal(np.isfinite(d0[g]), fin)
+        assert np.allclose(d0[g][fin], ref[fin], rtol=1e-6, atol=0), g
 
 
 def test_autotuner_picks_a_schedule(gpu_ctx, uneven_graphs):
     S, d, used, ms = solve_with(gpu_ctx, uneven_graphs, -1)
-    assert used in (0, 1, 2)
-    assert ms[0] > 0 and ms[1] > 0
+    assert used in (0, 1, 2, 3, 4)
+    assert ms[0] > 0 and ms[1] > 0 and ms[3] > 0
     _, d0, _, _ = solve_with(gpu_ctx, uneven_graphs, 0)
     for g in range(len(d)):
         assert np.array_equal(d[g], d0[g])
@@ -64,7 +70,7 @@ def test_many_graphs_full_frame(gpu_ctx, uneven_graphs):
     is identical whichever Floyd-Warshall schedule runs."""
     sc = uneven_graphs
     out = []
-    for schedule in (0, 1):
+    for schedule in (0, 1, 3):
         scenes.load_into(gpu_ctx, sc)
         gpu_ctx.build_graphs(sc.points, sc.radius_sq, sc.max_connect)
         gpu_ctx.set_fw_schedule(schedule)
@@ -72,6 +78,7 @@ def test_many_graphs_full_frame(gpu_ctx, uneven_graphs):
         out.append(gpu_ctx.films(sc.opts))
     for k in ["rgba", "direct", "scatter", "emission"]:
         assert np.array_equal(getattr(out[0], k), getattr(out[1], k))
+        assert np.array_equal(getattr(out[0], k), getattr(out[2], k))
     assert np.isfinite(out[0].rgba).all()
 
 
