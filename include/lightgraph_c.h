@@ -365,7 +365,8 @@ lg_status lg_set_fw_schedule(lg_ctx* ctx, int schedule);
 lg_status lg_fw_schedule(lg_ctx* ctx, int* schedule, double* tuned_ms, int n);
 /* Host-only check of the persistent schedules' work queue for graphs of the
  * given point counts (no device work). Builds the queue the solve would use
- * (sym != 0: the symmetric solve of schedules 3 and 4) and replays it in
+ * (sym != 0: the symmetric solve of schedules 3 and 4, in its structural
+ * and its list-scheduled order for 152 and 304 CTAs) and replays it in
  * order with the kernels' dependency waits and version updates. LG_OK when
  * every item's waits are met by earlier items (the launch cannot deadlock)
  * and every block is written exactly once per round; LG_ERR_STATE otherwise.

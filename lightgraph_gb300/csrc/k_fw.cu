@@ -33,6 +33,8 @@
 //                      always come earlier in the queue, so the schedule
 //                      cannot deadlock whatever the residency.
 #include <algorithm>
+#include <functional>
+#include <queue>
 #include <vector>
 
 #include "lg_kernels.h"
@@ -573,10 +575,13 @@ size_t fw_batched_items(const FwGraph* graphs, int n_graphs, int4* items, bool s
     };
     // the general solve has a diagonal, row and column panel tiles per round;
     // the symmetric one the diagonal and the column panel only
+    // (the symmetric solve closes the diagonal blocks of rounds >= 1 in the
+    // strip item that finishes them)
     auto panels = [&](int r) {
         for (int g = 0; g < n_graphs; ++g)
             if (r < graphs[g].nt)
-                for (int b = 0; b < (sym ? graphs[g].nt : 2 * graphs[g].nt - 1); ++b) emit(g, r, 0, b);
+                for (int b = sym && r > 0 ? 1 : 0; b < (sym ? graphs[g].nt : 2 * graphs[g].nt - 1); ++b)
+                    emit(g, r, 0, b);
     };
     // prio: the update tiles of round r holding row or column block r + ahead
     auto updates = [&](int r, bool prio, int ahead) {
@@ -619,6 +624,162 @@ size_t fw_batched_items(const FwGraph* graphs, int n_graphs, int4* items, bool s
         }
     }
     return k;
+}
+
+// List-scheduled order of the symmetric queue. The persistent kernel hands
+// items out in queue order; an item claimed before its dependencies are done
+// holds its CTA idle, and one claimed long after they are done delays
+// everything that waits on it. This reorders the queue by simulating
+// `workers` CTAs on the item dependency graph (durations in units of one
+// update tile, the ratios measured on GB300 at 2 CTAs per SM): a free CTA
+// takes the ready item with the longest remaining dependency chain (ties: the
+// structural order), and the simulated claim order becomes the queue. Every item is taken after its dependencies in the
+// simulation, so the order stays a dependency order (deadlock-free, checked by
+// fw_queue_replay).
+void fw_order_sym(const FwGraph* graphs, int n_graphs, int4* items, size_t n_items, int workers) {
+    if (n_items == 0 || workers < 1) return;
+    const int N = (int)n_items;
+    // item lookup: (graph, round, kind, index) -> position in the input
+    std::vector<int64_t> pan_off(n_graphs), str_off(n_graphs), upd_off(n_graphs), v_off(n_graphs);
+    int64_t tot = 0;
+    for (int g = 0; g < n_graphs; ++g) {
+        const int nt = graphs[g].nt, nu = graphs[g].nu;
+        pan_off[g] = tot; tot += (int64_t)nt * nt;               // [r][b]
+        str_off[g] = tot; tot += (int64_t)nt * nt;               // [r][X]
+        upd_off[g] = tot; tot += (int64_t)nt * nu * nu;          // [r][t]
+    }
+    std::vector<int> pos(tot, -1);
+    for (int i = 0; i < N; ++i) {
+        const int4 w = items[i];
+        const FwGraph& G = graphs[w.x];
+        int64_t k;
+        if (w.z == 0) k = pan_off[w.x] + (int64_t)w.y * G.nt + w.w;
+        else if (w.z == 2) k = str_off[w.x] + (int64_t)w.y * G.nt + w.w;
+        else k = upd_off[w.x] + ((int64_t)w.y * G.nu * G.nu + w.w);
+        pos[k] = i;
+    }
+    // virtual nodes V(g, q): every update tile and strip item of round q done
+    // (the panel slot reuse of round q + 3); numbered after the items
+    int64_t nv = 0;
+    for (int g = 0; g < n_graphs; ++g) { v_off[g] = N + nv; nv += graphs[g].nt; }
+    const int M = N + (int)nv;
+    auto panel = [&](int g, int r, int X) {  // the item writing block (X, r) in round r
+        if (X == r && r > 0) return pos[str_off[g] + (int64_t)(r - 1) * graphs[g].nt + r];  // fused closure
+        const int b = X == r ? 0 : (X < r ? X : X - 1) + 1;
+        return pos[pan_off[g] + (int64_t)r * graphs[g].nt + b];
+    };
+    auto writer = [&](int g, int q, int a, int b) {  // the item writing block (a, b), a <= b, in round q
+        const FwGraph& G = graphs[g];
+        if (a == q || b == q) return panel(g, q, a == q ? b : a);
+        if (a == q + 1 || b == q + 1) return pos[str_off[g] + (int64_t)q * G.nt + (a == q + 1 ? b : a)];
+        return pos[upd_off[g] + ((int64_t)q * G.nu * G.nu + (a / 2) * G.nu + b / 2)];
+    };
+    std::vector<std::vector<int>> succ(M);
+    std::vector<int> indeg(M, 0);
+    std::vector<float> dur(M, 0.f);
+    auto edge = [&](int from, int to) {
+        if (from < 0) return;
+        succ[from].push_back(to);
+        ++indeg[to];
+    };
+    for (int i = 0; i < N; ++i) {
+        const int4 w = items[i];
+        const int g = w.x, r = w.y, nt = graphs[g].nt, nu = graphs[g].nu;
+        std::vector<int> deps;
+        if (w.z == 0) {
+            const int X = w.w == 0 ? r : ((w.w - 1) < r ? (w.w - 1) : w.w);
+            dur[i] = w.w == 0 ? 0.85f : 0.6f;
+            if (w.w > 0) deps.push_back(panel(g, r, r));
+            if (r >= 1) deps.push_back(writer(g, r - 1, std::min(X, r), std::max(X, r)));
+            if (r >= kPanelSlots) deps.push_back((int)v_off[g] + r - kPanelSlots);
+        } else if (w.z == 2) {
+            const int X = w.w;
+            dur[i] = X == r + 1 ? 0.8f : 0.33f;
+            if (X == r + 1 && r + 1 >= kPanelSlots) deps.push_back((int)v_off[g] + r + 1 - kPanelSlots);
+            deps.push_back(panel(g, r, X));
+            deps.push_back(panel(g, r, r + 1));
+            if (r >= 1) deps.push_back(writer(g, r - 1, std::min(X, r + 1), std::max(X, r + 1)));
+            edge(i, (int)v_off[g] + r);
+        } else {
+            const int ti = w.w / nu, tj = w.w % nu;
+            dur[i] = 1.f;
+            for (int k = 0; k < 4; ++k) deps.push_back(panel(g, r, 2 * (k < 2 ? ti : tj) + (k & 1)));
+            for (int a = 0; a < 2; ++a)
+                for (int c = 0; c < 2; ++c) {
+                    const int bi = 2 * ti + a, bj = 2 * tj + c;
+                    if (r >= 1 && bi <= bj && bi != r && bj != r && bi != r + 1 && bj != r + 1)
+                        deps.push_back(writer(g, r - 1, bi, bj));
+                }
+            edge(i, (int)v_off[g] + r);
+        }
+        (void)nt;
+        std::sort(deps.begin(), deps.end());
+        deps.erase(std::unique(deps.begin(), deps.end()), deps.end());
+        for (int d : deps) edge(d, i);
+    }
+    // longest remaining chain (bottom level) by a reverse topological pass
+    std::vector<int> topo;
+    topo.reserve(M);
+    {
+        std::vector<int> deg = indeg;
+        for (int i = 0; i < M; ++i)
+            if (deg[i] == 0) topo.push_back(i);
+        for (size_t h = 0; h < topo.size(); ++h)
+            for (int t : succ[topo[h]])
+                if (--deg[t] == 0) topo.push_back(t);
+        if ((int)topo.size() != M) return;  // not a DAG: keep the structural order
+    }
+    std::vector<float> bl(M, 0.f);
+    for (int h = M - 1; h >= 0; --h) {
+        const int x = topo[h];
+        float m = 0.f;
+        for (int t : succ[x]) m = std::max(m, bl[t]);
+        bl[x] = dur[x] + m;
+    }
+    // simulation: workers take the ready item with the largest bottom level
+    auto cmp_ready = [&](int a, int b) { return bl[a] != bl[b] ? bl[a] < bl[b] : a > b; };
+    std::priority_queue<int, std::vector<int>, decltype(cmp_ready)> ready(cmp_ready);
+    using Ev = std::pair<float, int>;  // (completion time, node)
+    std::priority_queue<Ev, std::vector<Ev>, std::greater<Ev>> events;
+    std::priority_queue<float, std::vector<float>, std::greater<float>> free_at;
+    for (int k = 0; k < workers; ++k) free_at.push(0.f);
+    std::vector<int> deg = indeg;
+    std::vector<int4> out;
+    out.reserve(N);
+    auto complete = [&](int x, float t, auto&& self) -> void {
+        for (int s2 : succ[x])
+            if (--deg[s2] == 0) {
+                if (s2 >= N) self(s2, t, self);  // virtual nodes complete at once
+                else ready.push(s2);
+            }
+    };
+    for (int i = 0; i < M; ++i)
+        if (deg[i] == 0) {
+            if (i >= N) complete(i, 0.f, complete);
+            else ready.push(i);
+        }
+    while ((int)out.size() < N) {
+        float t = free_at.top();
+        free_at.pop();
+        while (!events.empty() && events.top().first <= t) {
+            const Ev e = events.top();
+            events.pop();
+            complete(e.second, e.first, complete);
+        }
+        while (ready.empty()) {
+            if (events.empty()) return;  // cannot happen for a DAG; keep the structural order
+            const Ev e = events.top();
+            events.pop();
+            t = std::max(t, e.first);
+            complete(e.second, e.first, complete);
+        }
+        const int x = ready.top();
+        ready.pop();
+        out.push_back(items[x]);
+        events.push({t + dur[x], x});
+        free_at.push(t + dur[x]);
+    }
+    std::copy(out.begin(), out.end(), items);
 }
 
 // Host replay of a queue with the waits and version updates of
@@ -687,10 +848,18 @@ size_t fw_queue_replay(const FwGraph* graphs, int n_graphs, const int4* items, s
                 writes.push_back(up(X, r, nt));
             } else if (w.z == 2) {
                 const int X = w.w;
+                if (X == r + 1 && r + 1 >= kPanelSlots) ok = ok && done[w.x][r + 1 - kPanelSlots] >= n_upd;
                 need(up(X, r, nt), (uint32_t)r + 1u);
                 need(up(r + 1, r, nt), (uint32_t)r + 1u);
                 need(up(X, r + 1, nt), (uint32_t)r);
                 writes.push_back(up(X, r + 1, nt));
+                if (X == r + 1) {  // and round r + 1's closure of the same block
+                    if (v[up(X, r + 1, nt)] != (uint32_t)r) ok = false;
+                    ++v[up(X, r + 1, nt)];
+                    writes.pop_back();
+                    if (v[up(X, r + 1, nt)] != (uint32_t)r + 1u) ok = false;
+                    ++v[up(X, r + 1, nt)];
+                }
                 ++done[w.x][r];
             } else {
                 const int ti = w.w / G.nu, tj = w.w % G.nu;
@@ -793,9 +962,27 @@ size_t fw_panel_words(const FwGraph& g) { return (size_t)kPanelSlots * g.nu * 32
 
 __device__ __forceinline__ int up_block(int a, int b, int nt) { return a < b ? a * nt + b : b * nt + a; }
 
-// Diagonal (b = 0) or column panel item b >= 1 of round kb (block X = the
-// b-th block other than kb). 256 threads; the result goes back to its block
-// above the diagonal and into the round's panel slot Pr.
+// Closes diagonal block kb held in sm.T, writes it back to d and its rows to
+// the round's panel slot Pr.
+__device__ __noinline__ void close_publish_diag(float* __restrict__ d, int ld, int kb, float2* __restrict__ Pr,
+                                                PanelSmem& sm) {
+    const int tid = threadIdx.x, K0 = kb * kKB;
+    close_diag_blocked(sm.T);
+    for (int e = tid; e < kKB * kKB; e += 256) {
+        const int r = e >> 6, c = e & 63;
+        d[(int64_t)(K0 + r) * ld + K0 + c] = sm.T[r][c];
+    }
+    float2* dst = Pr + (size_t)(kb >> 1) * 32 * kTile + (kb & 1) * kKB;
+    for (int e = tid; e < 32 * kKB; e += 256) {
+        const int kp = e >> 6, i = e & 63;
+        dst[kp * kTile + i] = *reinterpret_cast<const float2*>(&sm.T[i][2 * kp]);
+    }
+}
+
+// Diagonal (b = 0, round 0 only: later diagonal blocks are closed by the
+// strip item that finishes them) or column panel item b >= 1 of round kb
+// (block X = the b-th block other than kb). 256 threads; the result goes back
+// to its block above the diagonal and into the round's panel slot Pr.
 __device__ __noinline__ void fw_panel_tile_sym(float* __restrict__ d, int ld, int kb, int b,
                                                   float2* __restrict__ Pr, PanelSmem& sm) {
     const int tid = threadIdx.x, ty = tid >> 4, tx = tid & 15;
@@ -812,7 +999,8 @@ __device__ __noinline__ void fw_panel_tile_sym(float* __restrict__ d, int ld, in
             sm.T[r][c] = __ldcg(d + (int64_t)(K0 + r) * ld + K0 + c);
         }
         __syncthreads();
-        close_diag_blocked(sm.T);
+        close_publish_diag(d, ld, kb, Pr, sm);
+        return;
     } else {
         for (int e = tid; e < kKB * kKB; e += 256) {
             const int r = e >> 6, c = e & 63;
@@ -849,11 +1037,14 @@ __device__ __noinline__ void fw_panel_tile_sym(float* __restrict__ d, int ld, in
 // It runs as its own item right after round kb's panels, so that the next
 // round does not wait for whole update tiles:
 //   C = min(C, A (x) B^T), A / B = the panel-slot rows of block a / b.
+// The diagonal strip block (kb + 1, kb + 1) is then closed at once as round
+// kb + 1's diagonal item (close_publish_diag, into that round's slot Pnext).
 // 256 threads, each owning the 4 x 4 elements (ty + 16r, tx + 16c), k in
 // pairs (add.rn.f32x2 + 3-input min) as in the update tiles.
 __device__ __forceinline__ void fw_strip_tile_sym(float* __restrict__ d, int ld, int a, int b,
-                                                  const float2* __restrict__ Pr, float2* __restrict__ As,
-                                                  float2* __restrict__ Bs) {
+                                                  const float2* __restrict__ Pr, float2* __restrict__ Pnext,
+                                                  float2* __restrict__ As, float2* __restrict__ Bs,
+                                                  PanelSmem& sm) {
     const int tid = threadIdx.x, ty = tid >> 4, tx = tid & 15;
     const float4* pa = reinterpret_cast<const float4*>(Pr + (size_t)(a >> 1) * 32 * kTile + (a & 1) * kKB);
     const float4* pb = reinterpret_cast<const float4*>(Pr + (size_t)(b >> 1) * 32 * kTile + (b & 1) * kKB);
@@ -884,6 +1075,18 @@ __device__ __forceinline__ void fw_strip_tile_sym(float* __restrict__ d, int ld,
                 const float2 sv = __fadd2_rn(av[r], bv[c]);
                 acc[r][c] = min3f(acc[r][c], sv.x, sv.y);
             }
+    }
+    if (a == b) {
+        // the diagonal block a = kb + 1 is final for round kb: close it for
+        // round a right here (its diagonal item) into the next slot Pnext
+        __syncthreads();
+#pragma unroll
+        for (int r = 0; r < 4; ++r)
+#pragma unroll
+            for (int c = 0; c < 4; ++c) sm.T[ty + 16 * r][tx + 16 * c] = acc[r][c];
+        __syncthreads();
+        close_publish_diag(d, ld, a, Pnext, sm);
+        return;
     }
 #pragma unroll
     for (int r = 0; r < 4; ++r)
@@ -1058,7 +1261,10 @@ __global__ void __launch_bounds__(256, 2) k_fw_persistent_sym(float* __restrict_
                     ok = ok && wait_version(m.ver + r * nt + r, (uint32_t)r + (m.b > 0 ? 1u : 0u), err);
                     if (ok && m.b > 0) ok = wait_version(m.ver + up_block(m.X, r, nt), (uint32_t)r, err);
                 } else if (m.kind == 2) {
-                    ok = wait_version(m.ver + up_block(m.X, r, nt), (uint32_t)r + 1u, err) &&
+                    // the diagonal strip also opens round r + 1's panel slot
+                    if (m.X == r + 1 && r + 1 >= kPanelSlots)
+                        ok = wait_version(m.done + (r + 1 - kPanelSlots), m.n_upd, err);
+                    ok = ok && wait_version(m.ver + up_block(m.X, r, nt), (uint32_t)r + 1u, err) &&
                          wait_version(m.ver + up_block(r + 1, r, nt), (uint32_t)r + 1u, err) &&
                          wait_version(m.ver + up_block(m.X, r + 1, nt), (uint32_t)r, err);
                 } else {
@@ -1087,7 +1293,8 @@ __global__ void __launch_bounds__(256, 2) k_fw_persistent_sym(float* __restrict_
         if (w.z == 0) {
             fw_panel_tile_sym(d, g.ld, w.y, w.w, Pr, psm);
         } else if (w.z == 2) {
-            fw_strip_tile_sym(d, g.ld, min(w.w, w.y + 1), max(w.w, w.y + 1), Pr, As, Bs);
+            float2* Pnext = panels + g.pofs + (size_t)((w.y + 1) % kPanelSlots) * g.nu * 32 * kTile;
+            fw_strip_tile_sym(d, g.ld, min(w.w, w.y + 1), max(w.w, w.y + 1), Pr, Pnext, As, Bs, psm);
         } else {
             fw_update_tile_sym(d, g.ld, w.y, w.w / g.nu, w.w % g.nu, Pr, As, Bs);
         }
@@ -1099,7 +1306,8 @@ __global__ void __launch_bounds__(256, 2) k_fw_persistent_sym(float* __restrict_
             if (m.kind == 0) {
                 atomicAdd(m.ver + up_block(m.X, r, nt), 1u);
             } else if (m.kind == 2) {
-                atomicAdd(m.ver + up_block(m.X, r + 1, nt), 1u);
+                // the diagonal strip block also got its round r + 1 closure
+                atomicAdd(m.ver + up_block(m.X, r + 1, nt), m.X == r + 1 ? 2u : 1u);
                 atomicAdd(m.done + r, 1u);
             } else {
                 for (int a = 0; a < 2; ++a)

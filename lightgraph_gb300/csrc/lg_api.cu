@@ -887,6 +887,11 @@ lg_status Ctx::solve_paths_batched(int choice) {
         const size_t n_items_sym = fw_batched_items(fg.data(), n_graphs, nullptr, true);
         std::vector<int4> items_sym(std::max<size_t>(n_items_sym, 1));
         fw_batched_items(fg.data(), n_graphs, items_sym.data(), true);
+        {
+            int sms = 0;
+            CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device), "device query");
+            fw_order_sym(fg.data(), n_graphs, items_sym.data(), n_items_sym, 2 * sms);
+        }
         fw_sync_n = fw_sync_words(fg.data(), n_graphs);
         CK(d_fwg.reserve(sizeof(FwGraph) * n_graphs), "fw queue alloc");
         CK(d_fw_items.reserve(sizeof(int4) * items.size()), "fw queue alloc");
@@ -1602,7 +1607,16 @@ extern "C" lg_status lg_fw_queue_check(int n_graphs, const int32_t* sizes, int s
     std::vector<int4> items(std::max<size_t>(n, 1));
     fw_batched_items(fg.data(), n_graphs, items.data(), sym != 0);
     if (n_items) *n_items = (int64_t)n;
-    return fw_queue_replay(fg.data(), n_graphs, items.data(), n, sym != 0) == 0 ? LG_OK : LG_ERR_STATE;
+    if (fw_queue_replay(fg.data(), n_graphs, items.data(), n, sym != 0) != 0) return LG_ERR_STATE;
+    if (sym) {
+        // the list-scheduled order the solve runs, for 152 and 304 CTAs
+        for (int workers : {152, 304}) {
+            std::vector<int4> ordered = items;
+            fw_order_sym(fg.data(), n_graphs, ordered.data(), n, workers);
+            if (fw_queue_replay(fg.data(), n_graphs, ordered.data(), n, true) != 0) return LG_ERR_STATE;
+        }
+    }
+    return LG_OK;
 }
 
 extern "C" uint64_t lg_frame_launches(const lg_ctx* handle) {

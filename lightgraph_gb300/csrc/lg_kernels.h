@@ -53,6 +53,10 @@ struct FwGraph {
 // Writes the work queue (if items != null) and returns its length. sym: the
 // queue of the symmetric solve (tiles on and above the diagonal only).
 size_t fw_batched_items(const FwGraph* graphs, int n_graphs, int4* items, bool sym = false);
+// Reorders a symmetric queue (fw_batched_items with sym) by list scheduling
+// its dependency graph on `workers` simulated CTAs; the result is still a
+// dependency order.
+void fw_order_sym(const FwGraph* graphs, int n_graphs, int4* items, size_t n_items, int workers);
 // Host replay of a queue with the kernels' waits and version updates in
 // queue order: 0 if it cannot deadlock and writes every block once per round,
 // else the 1-based index of the first offending item (n_items + 1: a block

@@ -120,9 +120,11 @@ def test_fw_queue_cannot_deadlock(sizes, sym):
     nts = [(s + 127) // 128 * 2 for s in sizes if s > 0]
     nus = [nt // 2 for nt in nts]
     if sym:
-        # per round: nt panel items, nt - 1 strip blocks (all but the last
-        # round), the tiles on and above the diagonal (rounds with nt >= 2)
-        want = sum(nt * nt + (nt - 1) * (nt - 1) + (nt * nu * (nu + 1) // 2 if nt >= 2 else 0)
+        # per round: nt - 1 column panel items (plus the diagonal item in
+        # round 0; later diagonals close inside their strip item), nt - 1
+        # strip blocks (all but the last round), the tiles on and above the
+        # diagonal (rounds with nt >= 2)
+        want = sum(1 + nt * (nt - 1) + (nt - 1) * (nt - 1) + (nt * nu * (nu + 1) // 2 if nt >= 2 else 0)
                    for nt, nu in zip(nts, nus))
     else:
         want = sum(nt * (2 * nt - 1) + (nt * nu * nu if nt >= 2 else 0) for nt, nu in zip(nts, nus))
