@@ -39,6 +39,20 @@ STAGES = ["build_graph", "edge_march", "floyd_warshall", "vertex_light", "diffus
 NOMINAL_FP32_TFLOPS = 152 * 128 * 2 * 2.070 / 1000  # GB300: SMs x FP32 lanes x 2 (FMA) x 2.07 GHz
 FW_SCHEDULES = {0: "per-round launches", 1: "persistent 1 CTA/SM", 2: "persistent 2 CTA/SM",
                 3: "symmetric persistent 1 CTA/SM", 4: "symmetric persistent 2 CTA/SM"}
+def fw_executed_flops(ld, schedule):
+    """FP32 ops (add + min per update) the solve's kernels execute for one
+    ld x ld matrix: the general schedules run every (i, j, k); the symmetric
+    ones the 128-tiles on and above the diagonal, the strip blocks and the
+    panel items of each of the nt = ld / 64 rounds."""
+    if schedule < 3:
+        return 2.0 * ld ** 3
+    nt, nu = ld // 64, ld // 128
+    tiles = nt * nu * (nu + 1) // 2 * 128 * 128 * 64
+    strips = (nt - 1) * (nt - 1) * 64 ** 3
+    panels = (1 + nt * (nt - 1)) * 64 ** 3
+    return 2.0 * (tiles + strips + panels)
+
+
 FW_KERNELS = {0: "k_fw_update+k_fw_panels", 1: "k_fw_persistent", 2: "k_fw_persistent",
               3: "k_fw_persistent_sym+k_fw_mirror", 4: "k_fw_persistent_sym+k_fw_mirror"}
 
@@ -511,6 +525,8 @@ def run_ours(args):
     fw_sched, fw_tuned = ctx.fw_schedule()
     fw_flops = 2.0 * ld ** 3
     fw_tflops = fw_flops / (stage_ms[2] * 1e-3) / 1e12
+    fw_exec = fw_executed_flops(ld, fw_sched)
+    fw_ceiling = ctx.fw_inner_loop_rate()
     line = {
         "metric": "ms/frame", "value": value, "unit": "ms", "n_gpus": world, "steps": args.steps,
         "warmup": max(3, args.warmup), "ms_per_step": ms_per_step, "higher_is_better": False, "scaling": "weak",
@@ -536,7 +552,10 @@ def run_ours(args):
                         "peak_kind": "nominal (152 SMs x 128 lanes x 2 x 2.07 GHz)",
                         "frac": fw_tflops / NOMINAL_FP32_TFLOPS,
                         "schedule": FW_SCHEDULES.get(fw_sched, str(fw_sched)),
-                        "autotuner_ms": [round(x, 4) for x in fw_tuned]},
+                        "autotuner_ms": [round(x, 4) for x in fw_tuned],
+                        "executed_tflops": fw_exec / (stage_ms[2] * 1e-3) / 1e12,
+                        "inner_loop_ceiling_tflops": fw_ceiling,
+                        "executed_frac_of_inner_loop_ceiling": fw_exec / (stage_ms[2] * 1e-3) / 1e12 / fw_ceiling},
     }
     if rank == 0 and args.serving > 0:
         line["serving"] = run_serving(args.serving, args.rate)

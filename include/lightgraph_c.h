@@ -363,6 +363,12 @@ lg_status lg_set_fw_schedule(lg_ctx* ctx, int schedule);
 /* The schedule in use and the autotuner's timings (ms) of schedules 0, 1, 2.
  * Returns LG_ERR_TIMEOUT if a persistent solve reported a stalled queue. */
 lg_status lg_fw_schedule(lg_ctx* ctx, int* schedule, double* tuned_ms, int n);
+/* The ceiling of the Floyd-Warshall update tiles on this GPU: FP32 ops/s
+ * (one add and one min per update, as the roofline counts them) of their
+ * inner loop alone, with its operands held in shared memory (no staging, no
+ * dependency waits, no stores), 2 CTAs per SM. Enqueued on the context's
+ * stream and waited for. */
+lg_status lg_fw_inner_loop_rate(lg_ctx* ctx, double* tflops);
 /* Host-only check of the persistent schedules' work queue for graphs of the
  * given point counts (no device work). Builds the queue the solve would use
  * (sym != 0: the symmetric solve of schedules 3 and 4, in its structural

@@ -1376,6 +1376,94 @@ int fw_persistent_sym_ctas_per_sm() {
     return std::max(blocks, 1);
 }
 
+// ---------------------------------------------------------------------------
+// inner-loop ceiling
+// ---------------------------------------------------------------------------
+// The update tiles' inner loop alone: the same 8 x 8 register tile, the same
+// conflict-free fragment loads and the same add.rn.f32x2 + 3-input min per two
+// k, on operands that stay in shared memory (no staging, no dependency waits,
+// no stores), at 2 CTAs per SM. Its rate is the ceiling of min-plus on the
+// CUDA cores: each update needs one add and one min, and on GB300 each of
+// them takes an FP32 lane cycle whether it is packed (add.rn.f32x2, 3-input
+// min) or not, so the ceiling sits near half of the FMA-counted FP32 peak.
+__global__ void __launch_bounds__(256, 2) k_fw_inner_loop(float* __restrict__ out, int reps) {
+    extern __shared__ float4 fw_smem[];
+    float2* As = reinterpret_cast<float2*>(fw_smem);
+    float2* Bs = As + 32 * kTile;
+    const int tid = threadIdx.x;
+    for (int e = tid; e < 32 * kTile; e += 256) {
+        As[e] = make_float2(1.f + (e % 7), 2.f + (e % 5));
+        Bs[e] = make_float2(1.5f + (e % 3), 0.5f + (e % 11));
+    }
+    __syncthreads();
+    const int warp = tid >> 5, lane = tid & 31;
+    const int rbase = (warp >> 1) * 32 + (lane >> 3) * 2, cbase = (warp & 1) * 64 + (lane & 7) * 2;
+    float acc[8][8];
+#pragma unroll
+    for (int r = 0; r < 8; ++r)
+#pragma unroll
+        for (int c = 0; c < 8; ++c) acc[r][c] = 1e30f + (float)(r + c + tid);
+    for (int rep = 0; rep < reps; ++rep) {
+#pragma unroll 1
+        for (int kp = 0; kp < 32; ++kp) {
+            float2 a[8], b[8];
+            const float4* ap = reinterpret_cast<const float4*>(As + kp * kTile + rbase);
+            const float4* bp = reinterpret_cast<const float4*>(Bs + kp * kTile + cbase);
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const float4 va = ap[4 * q];
+                a[2 * q] = make_float2(va.x, va.y);
+                a[2 * q + 1] = make_float2(va.z, va.w);
+                const float4 vb = bp[8 * q];
+                b[2 * q] = make_float2(vb.x, vb.y);
+                b[2 * q + 1] = make_float2(vb.z, vb.w);
+            }
+#pragma unroll
+            for (int r = 0; r < 8; ++r)
+#pragma unroll
+                for (int c = 0; c < 8; ++c) {
+                    const float2 sv = __fadd2_rn(a[r], b[c]);
+                    acc[r][c] = min3f(acc[r][c], sv.x, sv.y);
+                }
+        }
+    }
+    float sum = 0.f;
+#pragma unroll
+    for (int r = 0; r < 8; ++r)
+#pragma unroll
+        for (int c = 0; c < 8; ++c) sum += acc[r][c];
+    out[blockIdx.x * 256 + tid] = sum;
+}
+
+cudaError_t fw_inner_loop_rate(float* scratch, int sms, double* tflops, cudaStream_t st) {
+    const size_t smem = sizeof(float2) * 2 * 32 * kTile;
+    cudaError_t e = cudaFuncSetAttribute(k_fw_inner_loop, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    const int grid = 2 * sms, reps = 200;
+    cudaEvent_t e0, e1;
+    if ((e = cudaEventCreate(&e0)) != cudaSuccess) return e;
+    if ((e = cudaEventCreate(&e1)) != cudaSuccess) { cudaEventDestroy(e0); return e; }
+    k_fw_inner_loop<<<grid, 256, smem, st>>>(scratch, reps);  // warm-up
+    ++g_launch_counter;
+    cudaEventRecord(e0, st);
+    const int iters = 5;
+    for (int k = 0; k < iters; ++k) {
+        k_fw_inner_loop<<<grid, 256, smem, st>>>(scratch, reps);
+        ++g_launch_counter;
+    }
+    cudaEventRecord(e1, st);
+    e = cudaEventSynchronize(e1);
+    float ms = 0.f;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (e != cudaSuccess) return e;
+    // per thread and k-pair: 64 elements x 2 updates, each one add and one min
+    const double ops = (double)grid * 256 * reps * 32 * 64 * 2 * 2 * iters;
+    *tflops = ops / (ms * 1e-3) / 1e12;
+    return cudaGetLastError();
+}
+
 __global__ void k_set_diag(float* __restrict__ S, const GraphInfo* __restrict__ graphs) {
     const GraphInfo g = graphs[blockIdx.y];
     const int i = blockIdx.x * blockDim.x + threadIdx.x;

@@ -1586,6 +1586,18 @@ extern "C" lg_status lg_fw_schedule(lg_ctx* handle, int* schedule, double* tuned
     return LG_OK;
 }
 
+extern "C" lg_status lg_fw_inner_loop_rate(lg_ctx* handle, double* tflops) {
+    Ctx* ctx = reinterpret_cast<Ctx*>(handle);
+    GUARD(ctx);
+    if (!tflops) return ctx->fail(LG_ERR_INVALID, "tflops is null");
+    int sms = 0;
+    CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device), "device query");
+    DevBuf scratch;
+    CK(scratch.reserve(sizeof(float) * 2 * sms * 256), "scratch alloc");
+    CK(fw_inner_loop_rate(scratch.as<float>(), sms, tflops, ctx->st), "inner loop rate");
+    return LG_OK;
+}
+
 extern "C" lg_status lg_fw_queue_check(int n_graphs, const int32_t* sizes, int sym, int64_t* n_items) {
     if (n_graphs < 0 || (n_graphs > 0 && !sizes)) return LG_ERR_INVALID;
     std::vector<FwGraph> fg(n_graphs);

@@ -76,6 +76,9 @@ cudaError_t fw_solve_batched_sym(float* base, const FwGraph* graphs, int n_graph
                                  int n_items, uint32_t* sync, size_t sync_words, float2* panels, int ctas,
                                  cudaStream_t st);
 int fw_persistent_ctas_per_sm();
+// FP32 ops/s (an add and a min per update) of the update tiles' inner loop
+// alone on shared-memory operands, 2 CTAs per SM. scratch: 2 * sms * 256 floats.
+cudaError_t fw_inner_loop_rate(float* scratch, int sms, double* tflops, cudaStream_t st);
 int fw_persistent_sym_ctas_per_sm();
 cudaError_t launch_set_diag(float* S, const GraphInfo* graphs, int n_graphs, int max_n,
                             cudaStream_t st);

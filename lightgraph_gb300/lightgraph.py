@@ -414,6 +414,13 @@ class Context:
         3/4 symmetric persistent (CTAs per SM)."""
         self._ck(self.lib.lg_set_fw_schedule(self.h, schedule))
 
+    def fw_inner_loop_rate(self) -> float:
+        """FP32 TFLOP/s (add + min per update) of the Floyd-Warshall update
+        tiles' inner loop alone: the min-plus ceiling on this GPU."""
+        v = C.c_double()
+        self._ck(self.lib.lg_fw_inner_loop_rate(self.h, C.byref(v)))
+        return v.value
+
     def fw_schedule(self):
         s = C.c_int()
         ms = (C.c_double * 5)()

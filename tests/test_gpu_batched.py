@@ -97,3 +97,11 @@ def test_graph_replay_matches_direct_launches(gpu_ctx):
             assert np.array_equal(getattr(got, k), getattr(ref, k)), k
     assert gpu_ctx.lib.lg_frame_launches(gpu_ctx.h) > 10
     gpu_ctx.set_graph_mode(False)
+
+
+def test_fw_inner_loop_ceiling(gpu_ctx):
+    """The min-plus inner loop alone runs near half of the FMA-counted FP32
+    peak (an add and a min per update, each an FP32 lane cycle): between 20
+    and 70 TFLOP/s on a GB300 (152 SMs, ~1.9-2.07 GHz)."""
+    t = gpu_ctx.fw_inner_loop_rate()
+    assert 20.0 < t < 70.0, t
