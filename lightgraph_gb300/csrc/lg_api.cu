@@ -932,16 +932,19 @@ lg_status Ctx::tune_fw() {
     int best = 0;
     float best_ms = 1e30f;
     for (double& t : fw_tune_ms) t = 0.0;
-    for (size_t c = 0; c < cands.size(); ++c) {
+    // each candidate runs twice and keeps its faster run: the first launch of
+    // a kernel can carry one-time costs (module load, a profiler's setup)
+    for (size_t c = 0; c < 2 * cands.size() && s == LG_OK; ++c) {
+        const int cand = cands[c % cands.size()];
         CK(cudaMemcpyAsync(d_fw_tune.p, d_S.p, sizeof(float) * s_floats, cudaMemcpyDeviceToDevice, st), "fw tune copy");
         CK(cudaEventRecord(e0, st), "event");
-        s = run_fw_schedule(this, d_fw_tune.as<float>(), cands[c]);
+        s = run_fw_schedule(this, d_fw_tune.as<float>(), cand);
         if (s != LG_OK) break;
         CK(cudaEventRecord(e1, st), "event");
         CK(cudaEventSynchronize(e1), "event sync");
         float ms = 0.f;
         CK(cudaEventElapsedTime(&ms, e0, e1), "event time");
-        if (cands[c] > 0) {
+        if (cand > 0) {
             // a persistent launch reports a stalled queue through its error flag
             uint32_t flags[2] = {0, 0};
             CK(cudaMemcpy(flags, d_fw_sync.p, sizeof flags, cudaMemcpyDeviceToHost), "fw flag read");
@@ -950,8 +953,8 @@ lg_status Ctx::tune_fw() {
                 break;
             }
         }
-        fw_tune_ms[cands[c]] = ms;
-        if (ms < best_ms) { best_ms = ms; best = cands[c]; }
+        if (fw_tune_ms[cand] == 0.0 || ms < fw_tune_ms[cand]) fw_tune_ms[cand] = ms;
+        if (ms < best_ms) { best_ms = ms; best = cand; }
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
