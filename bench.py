@@ -71,6 +71,10 @@ def parse():
     ap.add_argument("--serving", type=int, default=24, help="requests in the serving measurement (0: skip)")
     ap.add_argument("--rate", type=float, default=50.0, help="Poisson arrival rate of the serving stream (req/s)")
     ap.add_argument("--batched", type=int, default=1, help="run the 64-graph batched measurement (0: skip)")
+    ap.add_argument("--fw-schedule", type=int, default=-1,
+                    help="pin the Floyd-Warshall schedule (0-4; -1: autotuned). Profiling runs pin the "
+                         "schedule the autotuner picks without a profiler, whose per-launch overhead "
+                         "distorts the trial timings")
     ap.add_argument("--ref-iters", type=int, default=500,
                     help="LightGraph iterations of the reference-scale pipeline measurement (0: skip)")
     return ap.parse_args()
@@ -440,6 +444,8 @@ def run_ours(args):
     ctx = Context(local)
     scenes.load_into(ctx, sc)
     ctx.build_graphs(sc.points, sc.radius_sq, sc.max_connect)
+    if args.fw_schedule >= 0:
+        ctx.set_fw_schedule(args.fw_schedule)
     lib = ctx.lib
     stream = torch.cuda.ExternalStream(ctx.stream)
 

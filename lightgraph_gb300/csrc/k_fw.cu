@@ -443,7 +443,11 @@ cudaError_t fw_solve(float* d, int n, int ld, cudaStream_t st) {
 //                      for the row and column items (which read it closed);
 //   update (r, tile) : its A and B panel blocks (column / row block r) at
 //                      version >= r + 1 and its own blocks outside row and
-//                      column block r at version >= r.
+//                      column block r at version >= r; a tile holding row or
+//                      column block r - 1 also waits for every update tile of
+//                      round r - 1 (per-round counters after the versions),
+//                      which read those blocks as operands and must not see
+//                      them rewritten.
 // The queue is ordered with a one-round look-ahead: the update tiles of round
 // r that hold row or column block r + 1 come first, then the panel tiles of
 // round r + 1, then the rest of round r's update tiles. Every item's
@@ -517,6 +521,11 @@ __global__ void __launch_bounds__(256, 2) k_fw_persistent(float* __restrict__ ba
                      wait_version(ver + bi * nt + bj, (uint32_t)r, err);
             } else {
                 const int ti = w.w / g.nu, tj = w.w % g.nu;
+                // a tile that rewrites row or column block r - 1 waits until
+                // every update tile of round r - 1 (which read those blocks
+                // as operands) is done
+                if (r >= 1 && (2 * ti == r - 1 || 2 * ti + 1 == r - 1 || 2 * tj == r - 1 || 2 * tj + 1 == r - 1))
+                    ok = wait_version(ver + nt * nt + (r - 1), (uint32_t)(g.nu * g.nu), err);
                 for (int a = 0; a < 2 && ok; ++a) {
                     const int bi = 2 * ti + a, bj = 2 * tj + a;
                     if (bi < nt) ok = wait_version(ver + bi * nt + r, (uint32_t)r + 1u, err);
@@ -560,6 +569,7 @@ __global__ void __launch_bounds__(256, 2) k_fw_persistent(float* __restrict__ ba
                         const int bi = 2 * ti + a, bj = 2 * tj + c;
                         if (bi < nt && bj < nt && bi != r && bj != r) atomicAdd(ver + bi * nt + bj, 1u);
                     }
+                atomicAdd(ver + nt * nt + r, 1u);  // finished update tiles of round r
             }
         }
     }
@@ -820,6 +830,9 @@ size_t fw_queue_replay(const FwGraph* graphs, int n_graphs, const int4* items, s
                 writes.push_back(bi * nt + bj);
             } else {
                 const int ti = w.w / G.nu, tj = w.w % G.nu;
+                if (r >= 1 && (2 * ti == r - 1 || 2 * ti + 1 == r - 1 || 2 * tj == r - 1 || 2 * tj + 1 == r - 1))
+                    ok = ok && done[w.x][r - 1] >= (uint32_t)(G.nu * G.nu);
+                ++done[w.x][r];
                 for (int a = 0; a < 2; ++a) {
                     const int bi = 2 * ti + a, bj = 2 * tj + a;
                     if (bi < nt) need(bi * nt + r, (uint32_t)r + 1u);
