@@ -358,9 +358,12 @@ uint64_t lg_frame_launches(const lg_ctx* ctx);
  * the autotuner, which times every candidate once per (graph count, largest
  * graph) on a scratch copy and keeps the fastest; 0: two launches per round
  * per graph; 1 or 2: one persistent launch for every graph with 1 or 2 CTAs
- * per SM (a work queue with per-graph dependency counters). */
+ * per SM (a work queue with per-graph dependency counters); 3 or 4: the
+ * symmetric persistent solve (for the symmetric matrices the graph stage
+ * builds) with 1 or 2 CTAs per SM. A schedule set here stays in force for
+ * later graph builds until -1 is set again. */
 lg_status lg_set_fw_schedule(lg_ctx* ctx, int schedule);
-/* The schedule in use and the autotuner's timings (ms) of schedules 0, 1, 2.
+/* The schedule in use and the autotuner's timings (ms) of schedules 0..4.
  * Returns LG_ERR_TIMEOUT if a persistent solve reported a stalled queue. */
 lg_status lg_fw_schedule(lg_ctx* ctx, int* schedule, double* tuned_ms, int n);
 /* The ceiling of the Floyd-Warshall update tiles on this GPU: FP32 ops/s

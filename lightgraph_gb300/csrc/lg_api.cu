@@ -597,10 +597,10 @@ lg_status Ctx::load_graphs(int n_graphs, const float* points, const int64_t* off
     CK(cudaStreamSynchronize(st), "graph upload sync");
     point_voxel_size_cache = -1.0;
     graph_valid = false;
-    fw_queue_valid = false;
-    fw_choice = -1;
-    for (auto& kv : fw_tuned)
-        if (kv.first == std::make_pair(n_graphs, max_n)) fw_choice = kv.second;
+    fw_choice = fw_pinned;
+    if (fw_pinned < 0)
+        for (auto& kv : fw_tuned)
+            if (kv.first == std::make_pair(n_graphs, max_n)) fw_choice = kv.second;
     graphs_built = false;
     return LG_OK;
 }
@@ -864,7 +864,19 @@ static lg_status run_fw_schedule(Ctx* ctx, float* base, int choice) {
 
 lg_status Ctx::solve_paths_batched(int choice) {
     Ctx* ctx = this;
+    // the queues depend only on where each matrix lives and its padded size:
+    // a new point set of the same sizes (every frame of lg_render_frame)
+    // keeps them
+    std::vector<int64_t> key;
+    key.reserve(2 * n_graphs + 1);
+    key.push_back(n_graphs);
+    for (const GraphInfo& gi : h_graphs) {
+        key.push_back(gi.s_off);
+        key.push_back(gi.n == 0 ? -1 : gi.ld);
+    }
+    if (fw_queue_valid && key != fw_queue_key) fw_queue_valid = false;
     if (!fw_queue_valid) {
+        fw_queue_key = key;
         std::vector<FwGraph> fg(n_graphs);
         int64_t vofs = 0, pofs = 0;
         fw_max_nt = 0;
@@ -1564,6 +1576,7 @@ extern "C" lg_status lg_set_fw_schedule(lg_ctx* handle, int schedule) {
     Ctx* ctx = reinterpret_cast<Ctx*>(handle);
     GUARD(ctx);
     if (schedule < -1 || schedule > 4) return ctx->fail(LG_ERR_INVALID, "schedule must be -1, 0, 1, 2, 3 or 4");
+    ctx->fw_pinned = schedule;
     if (schedule == -1) {
         ctx->fw_choice = -1;
         for (auto& kv : ctx->fw_tuned)

@@ -105,10 +105,12 @@ struct Ctx {
     int fw_max_nt = 0;
     size_t fw_sync_n = 2;  // uint32 words of d_fw_sync
     bool fw_queue_valid = false;
+    std::vector<int64_t> fw_queue_key;  // (graph count, then offset and padded size per graph)
     // schedule per (graph count, largest n): 0 = per-graph launches,
     // k > 0 = persistent with k CTAs per SM
     std::vector<std::pair<std::pair<int, int>, int>> fw_tuned;
     int fw_choice = -1;
+    int fw_pinned = -1;  // lg_set_fw_schedule's choice, kept across graph builds (-1: autotuned)
     double fw_tune_ms[5] = {0, 0, 0, 0, 0};
 
     // frame replay through a captured CUDA graph
