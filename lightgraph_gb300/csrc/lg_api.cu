@@ -876,6 +876,7 @@ lg_status Ctx::solve_paths_batched(int choice) {
     }
     if (fw_queue_valid && key != fw_queue_key) fw_queue_valid = false;
     if (!fw_queue_valid) {
+        // graph descriptors, sync words and panel slots (both solves)
         fw_queue_key = key;
         std::vector<FwGraph> fg(n_graphs);
         int64_t vofs = 0, pofs = 0;
@@ -893,34 +894,54 @@ lg_status Ctx::solve_paths_batched(int choice) {
             pofs += (int64_t)fw_panel_words(fg[g]);
             fw_max_nt = std::max(fw_max_nt, fg[g].nt);
         }
-        const size_t n_items = fw_batched_items(fg.data(), n_graphs, nullptr);
-        std::vector<int4> items(std::max<size_t>(n_items, 1));
-        fw_batched_items(fg.data(), n_graphs, items.data());
-        const size_t n_items_sym = fw_batched_items(fg.data(), n_graphs, nullptr, true);
-        std::vector<int4> items_sym(std::max<size_t>(n_items_sym, 1));
-        fw_batched_items(fg.data(), n_graphs, items_sym.data(), true);
-        {
-            int sms = 0;
-            CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device), "device query");
-            fw_order_sym(fg.data(), n_graphs, items_sym.data(), n_items_sym, 2 * sms);
-        }
         fw_sync_n = fw_sync_words(fg.data(), n_graphs);
         CK(d_fwg.reserve(sizeof(FwGraph) * n_graphs), "fw queue alloc");
-        CK(d_fw_items.reserve(sizeof(int4) * items.size()), "fw queue alloc");
-        CK(d_fw_items_sym.reserve(sizeof(int4) * items_sym.size()), "fw queue alloc");
         CK(d_fw_sync.reserve(sizeof(uint32_t) * fw_sync_n), "fw queue alloc");
         CK(d_fw_panels.reserve(sizeof(float2) * std::max<int64_t>(pofs, 1)), "fw panel alloc");
         CK(cudaMemcpyAsync(d_fwg.p, fg.data(), sizeof(FwGraph) * n_graphs, cudaMemcpyHostToDevice, st), "fw queue upload");
+        CK(cudaStreamSynchronize(st), "fw queue sync");
+        h_fwg = std::move(fg);
+        fw_queue_valid = true;
+        fw_general_built = false;
+        fw_sym_built = false;
+    }
+    if ((choice == 1 || choice == 2) && !fw_general_built) {
+        const size_t n_items = fw_batched_items(h_fwg.data(), n_graphs, nullptr);
+        std::vector<int4> items(std::max<size_t>(n_items, 1));
+        fw_batched_items(h_fwg.data(), n_graphs, items.data());
+        CK(d_fw_items.reserve(sizeof(int4) * items.size()), "fw queue alloc");
         CK(cudaMemcpyAsync(d_fw_items.p, items.data(), sizeof(int4) * items.size(), cudaMemcpyHostToDevice, st),
            "fw queue upload");
-        CK(cudaMemcpyAsync(d_fw_items_sym.p, items_sym.data(), sizeof(int4) * items_sym.size(),
-                           cudaMemcpyHostToDevice, st), "fw queue upload");
         CK(cudaStreamSynchronize(st), "fw queue sync");
         fw_items_n = (int)n_items;
-        fw_items_sym_n = (int)n_items_sym;
-        fw_queue_valid = true;
+        fw_general_built = true;
     }
-    (void)choice;
+    if (choice >= 3 && !fw_sym_built) {
+        const size_t n_items_sym = fw_batched_items(h_fwg.data(), n_graphs, nullptr, true);
+        h_fw_items_sym.assign(std::max<size_t>(n_items_sym, 1), make_int4(0, 0, 0, 0));
+        fw_batched_items(h_fwg.data(), n_graphs, h_fw_items_sym.data(), true);
+        CK(d_fw_items_sym.reserve(sizeof(int4) * h_fw_items_sym.size()), "fw queue alloc");
+        CK(cudaMemcpyAsync(d_fw_items_sym.p, h_fw_items_sym.data(), sizeof(int4) * h_fw_items_sym.size(),
+                           cudaMemcpyHostToDevice, st), "fw queue upload");
+        CK(cudaStreamSynchronize(st), "fw queue sync");
+        fw_items_sym_n = (int)n_items_sym;
+        fw_sym_built = true;
+        fw_queue_uses = 0;
+        fw_sym_ordered = false;
+    } else if (choice >= 3 && !fw_sym_ordered && !capturing && (fw_order_next || ++fw_queue_uses >= 2)) {
+        // the same graph sizes solved again (frames of a fixed scene), or a
+        // frame about to be captured for replay: the list-scheduled order of
+        // the symmetric queue pays for its host time (tens of ms at 4096
+        // points) there, so it is computed now rather than for every one-off
+        // size
+        int sms = 0;
+        CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device), "device query");
+        fw_order_sym(h_fwg.data(), n_graphs, h_fw_items_sym.data(), (size_t)fw_items_sym_n, 2 * sms);
+        CK(cudaMemcpyAsync(d_fw_items_sym.p, h_fw_items_sym.data(), sizeof(int4) * fw_items_sym_n,
+                           cudaMemcpyHostToDevice, st), "fw queue upload");
+        CK(cudaStreamSynchronize(st), "fw queue sync");
+        fw_sym_ordered = true;
+    }
     return LG_OK;
 }
 
@@ -931,12 +952,14 @@ lg_status Ctx::tune_fw() {
     const std::pair<int, int> key(n_graphs, max_n);
     for (auto& kv : fw_tuned)
         if (kv.first == key) { fw_choice = kv.second; return LG_OK; }
-    lg_status s = solve_paths_batched(1);
+    lg_status s = solve_paths_batched(2);
+    if (s == LG_OK) s = solve_paths_batched(4);
     if (s != LG_OK) return s;
-    std::vector<int> cands = {0, 1};
-    if (fw_persistent_ctas_per_sm() >= 2) cands.push_back(2);
-    cands.push_back(3);
-    if (fw_persistent_sym_ctas_per_sm() >= 2) cands.push_back(4);
+    // schedule 0 and the persistent solves at the highest residency (the
+    // 1-CTA/SM ones only where 2 do not fit: they never win otherwise)
+    std::vector<int> cands = {0};
+    cands.push_back(fw_persistent_ctas_per_sm() >= 2 ? 2 : 1);
+    cands.push_back(fw_persistent_sym_ctas_per_sm() >= 2 ? 4 : 3);
     CK(d_fw_tune.reserve(sizeof(float) * std::max<int64_t>(s_floats, 1)), "fw tune alloc");
     cudaEvent_t e0, e1;
     CK(cudaEventCreate(&e0), "event");
@@ -944,10 +967,17 @@ lg_status Ctx::tune_fw() {
     int best = 0;
     float best_ms = 1e30f;
     for (double& t : fw_tune_ms) t = 0.0;
-    // each candidate runs twice and keeps its faster run: the first launch of
-    // a kernel can carry one-time costs (module load, a profiler's setup)
-    for (size_t c = 0; c < 2 * cands.size() && s == LG_OK; ++c) {
-        const int cand = cands[c % cands.size()];
+    // one trial each, then a second trial of the two fastest (the first launch
+    // of a kernel can carry one-time costs: module load, a profiler's setup)
+    std::vector<int> trials = cands;
+    for (size_t c = 0; c < trials.size() && s == LG_OK; ++c) {
+        if (c == cands.size()) {
+            std::vector<int> order = cands;
+            std::sort(order.begin(), order.end(), [&](int a, int b) { return fw_tune_ms[a] < fw_tune_ms[b]; });
+            trials.push_back(order[0]);
+            trials.push_back(order[1]);
+        }
+        const int cand = trials[c];
         CK(cudaMemcpyAsync(d_fw_tune.p, d_S.p, sizeof(float) * s_floats, cudaMemcpyDeviceToDevice, st), "fw tune copy");
         CK(cudaEventRecord(e0, st), "event");
         s = run_fw_schedule(this, d_fw_tune.as<float>(), cand);
@@ -1503,7 +1533,9 @@ extern "C" lg_status lg_frame_device(lg_ctx* handle, int max_connect, double poi
     }
     // run the frame once (this also tunes and allocates), then capture the
     // same launch sequence for replay
+    ctx->fw_order_next = true;
     lg_status s = ctx->frame_enqueue(point_voxel_size, camera);
+    ctx->fw_order_next = false;
     if (s != LG_OK) return s;
     CK(cudaStreamSynchronize(ctx->st), "sync");
     if (ctx->graph_exec) { cudaGraphExecDestroy(ctx->graph_exec); ctx->graph_exec = nullptr; }

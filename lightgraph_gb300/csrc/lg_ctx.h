@@ -106,6 +106,13 @@ struct Ctx {
     size_t fw_sync_n = 2;  // uint32 words of d_fw_sync
     bool fw_queue_valid = false;
     std::vector<int64_t> fw_queue_key;  // (graph count, then offset and padded size per graph)
+    bool fw_general_built = false;      // d_fw_items holds the general queue
+    bool fw_sym_built = false;          // d_fw_items_sym holds the symmetric queue
+    int fw_queue_uses = 0;              // solves since the symmetric queue was built
+    bool fw_sym_ordered = false;        // the symmetric queue is in list-scheduled order
+    bool fw_order_next = false;         // order it at the next solve (a frame about to be captured)
+    std::vector<FwGraph> h_fwg;         // host copies for the deferred ordering
+    std::vector<int4> h_fw_items_sym;
     // schedule per (graph count, largest n): 0 = per-graph launches,
     // k > 0 = persistent with k CTAs per SM
     std::vector<std::pair<std::pair<int, int>, int>> fw_tuned;

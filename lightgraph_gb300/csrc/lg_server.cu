@@ -134,8 +134,10 @@ void lg_server::run(Slot* s, Request* q) {
     c.settings = r.settings;
     lg_status st = c.set_lights(q->lights.data(), (int)q->lights.size(), nullptr, 0, 0);
     if (st == LG_OK) st = c.load_graphs(r.n_graphs, q->pts.data(), q->offs.data(), q->r2.data(), r.max_connect);
-    // one graph: per-round launches; several: the persistent batched solve
-    if (st == LG_OK) c.fw_choice = r.n_graphs > 1 ? 1 : 0;
+    // the symmetric persistent solve at 1 CTA per SM (leaves room for the
+    // other slots' kernels; correct whatever the residency), its queue in
+    // structural order (one-off sizes do not pay for the list scheduling)
+    if (st == LG_OK) c.fw_choice = 3;
     if (st == LG_OK) st = c.build_edges();
     if (st == LG_OK) st = c.solve_all();
     if (st == LG_OK) st = c.splat(r.point_voxel_size);

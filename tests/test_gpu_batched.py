@@ -58,8 +58,8 @@ def test_schedules_bit_identical_and_match_oracle(gpu_ctx, uneven_graphs):
 
 def test_autotuner_picks_a_schedule(gpu_ctx, uneven_graphs):
     S, d, used, ms = solve_with(gpu_ctx, uneven_graphs, -1)
-    assert used in (0, 1, 2, 3, 4)
-    assert ms[0] > 0 and ms[1] > 0 and ms[3] > 0
+    assert used in (0, 2, 4)
+    assert ms[0] > 0 and ms[2] > 0 and ms[4] > 0
     _, d0, _, _ = solve_with(gpu_ctx, uneven_graphs, 0)
     for g in range(len(d)):
         assert np.array_equal(d[g], d0[g])
