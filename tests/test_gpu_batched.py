@@ -105,3 +105,43 @@ def test_fw_inner_loop_ceiling(gpu_ctx):
     and 70 TFLOP/s on a GB300 (152 SMs, ~1.9-2.07 GHz)."""
     t = gpu_ctx.fw_inner_loop_rate()
     assert 20.0 < t < 70.0, t
+
+
+def test_fw_full_size_properties(gpu_ctx):
+    """The production solve size (one 4096-point graph, 64 rounds), where the
+    FP32 oracle would take minutes: size-independent properties instead.
+    The symmetric persistent solve (schedule 4, what the autotuner picks) and
+    the per-round launches (schedule 0) give the same bits; the result is
+    exactly symmetric with a zero diagonal; finite entries are exactly the
+    pairs the graph connects; and sampled triples satisfy the triangle
+    inequality d_ij <= d_ik + d_kj (within 1e-6 relative: the solve rounds
+    each path sum in its own association order)."""
+    sc = scenes.small(n_points=4096, width=32, height=32, res=128)
+    sc.radius = [0.06]
+    scenes.load_into(gpu_ctx, sc)
+    gpu_ctx.build_graphs(sc.points, sc.radius_sq, sc.max_connect)
+    S = gpu_ctx.march_edges(want=True)[0]
+    assert S.shape == (4096, 4096)
+    out = {}
+    for schedule in (0, 4):
+        gpu_ctx.set_fw_schedule(schedule)
+        out[schedule] = gpu_ctx.solve_paths(want=True)[0]
+        assert gpu_ctx.fw_schedule()[0] == schedule
+    gpu_ctx.set_fw_schedule(-1)
+    d = out[4]
+    assert np.array_equal(d, out[0])
+    assert np.array_equal(d, d.T)
+    assert np.all(np.diag(d) == 0)
+    fin = np.isfinite(d)
+    # connectivity: finite exactly within the edge graph's components
+    from scipy.sparse import csr_matrix
+    from scipy.sparse.csgraph import connected_components
+    _, label = connected_components(csr_matrix(np.isfinite(S)), directed=False)
+    assert np.array_equal(fin, label[:, None] == label[None, :])
+    assert np.all(d[np.isfinite(S)] <= S[np.isfinite(S)])
+    rng = np.random.default_rng(7)
+    i, j, k = (rng.integers(0, 4096, 200000) for _ in range(3))
+    lhs = d[i, j].astype(np.float64)
+    rhs = d[i, k].astype(np.float64) + d[k, j].astype(np.float64)
+    ok = ~np.isfinite(rhs) | (lhs <= rhs * (1 + 1e-6))
+    assert ok.all()
