@@ -322,15 +322,21 @@ __global__ void __launch_bounds__(128, 8) k_shadow(DevScene sc, const ShadowTask
             while (!sdrop && next_span(G, sd, sa, sb)) {
                 float sStep = jitter_step(step1, draw_sub(sub, kTagShadowSpan | sspan));
                 ++sspan;
-                for (float sT = step1 * ceilf(sa / step1); sT <= sb && sT + sStep > sT;) {
+                // every jittered step is >= 0.75 step1: if that is not
+                // absorbed at sb, sT grows on every iteration up to sb
+                if (!(sb + 0.75f * step1 > sb)) continue;
+                for (float sT = step1 * ceilf(sa / step1); sT <= sb;) {
                     const uint32_t q = siter++;
                     const float rs = fminf(sample_index_t<DT>(G, srr.e[0] + sT * srr.d[0], srr.e[1] + sT * srr.d[1],
                                                               srr.e[2] + sT * srr.d[2]) * scale,
                                            sh.dMax);
-                    if (rs < cutoff) { sT += sStep; continue; }
-                    tau += rs * sStep;
+                    // a sample below the cutoff adds nothing and keeps its
+                    // step (no re-jitter); branch-free, the warp stays converged
+                    const bool take = rs >= cutoff;
+                    const float next = jitter_step(step1, draw_sub(sub, kTagShadowStep | q));
+                    tau = take ? fmaf(rs, sStep, tau) : tau;
                     if (tau > sh.tau_drop) { sdrop = true; break; }
-                    sStep = jitter_step(step1, draw_sub(sub, kTagShadowStep | q));
+                    sStep = take ? next : sStep;
                     sT += sStep;
                 }
             }

@@ -124,6 +124,7 @@ def test_fw_full_size_properties(gpu_ctx):
     assert S.shape == (4096, 4096)
     out = {}
     for schedule in (0, 4):
+        gpu_ctx.march_edges()  # the solve works in place: start each from the edges
         gpu_ctx.set_fw_schedule(schedule)
         out[schedule] = gpu_ctx.solve_paths(want=True)[0]
         assert gpu_ctx.fw_schedule()[0] == schedule
