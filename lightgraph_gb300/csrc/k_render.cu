@@ -283,19 +283,18 @@ __global__ void __launch_bounds__(128, 8) k_shadow(DevScene sc, const ShadowTask
                                                 const int32_t* __restrict__ order, float4* __restrict__ direct,
                                                 unsigned long long* __restrict__ ctr) {
     const int64_t total = min((int64_t)*total_ptr, task_cap);
-    const int64_t n_units = (total + kRayUnit - 1) / kRayUnit;
-    const int64_t per_light = n_units * kRayUnit;
-    const int64_t n_rays = per_light * sc.n_lights;
+    const uint64_t n_units = (uint64_t)(total + kRayUnit - 1) / kRayUnit;
+    const uint64_t per_light = n_units * kRayUnit;
     const DevGrid& G = sc.dens;
     const DevShader& sh = sc.sh;
     const float step1 = sc.step1, cutoff = sc.cutoff;
     const float scale = sh.dS * sh.shadowDS;
     uint32_t n_shadow = 0;
-    for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n_rays;
-         r += (int64_t)gridDim.x * blockDim.x) {
-        const int k = (int)(r / per_light);
-        const int64_t rr = r - k * per_light;
-        const int64_t t = (int64_t)order[k * n_units + rr / kRayUnit] * kRayUnit + rr % kRayUnit;
+    const uint64_t first = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x, stride = (uint64_t)gridDim.x * blockDim.x;
+    // lights in the outer loop: the (light, ray) index needs no 64-bit division
+    for (int k = 0; k < sc.n_lights; ++k)
+    for (uint64_t rr = first; rr < per_light; rr += stride) {
+        const int64_t t = (int64_t)order[k * n_units + rr / kRayUnit] * kRayUnit + (int64_t)(rr % kRayUnit);
         if (t >= total) continue;
         const ShadowTask tk = tasks[t];
         const DevLight& Lk = sc.lights[k];
