@@ -342,9 +342,9 @@ lg_status lg_render_stats(lg_ctx* ctx, uint64_t* primary_samples,
  * diffusion, splat, render. */
 lg_status lg_set_profiling(lg_ctx* ctx, int on);
 lg_status lg_stage_times(lg_ctx* ctx, double* ms, int n);
-/* The render stage of the last profiled frame split into its waves (ms):
- * primary count + scan, primary shading, shadow-ray ordering, shadow rays,
- * resolve. */
+/* The last render made with profiling on (inside a frame or by lg_render)
+ * split into its waves (ms): primary count + scan, primary shading,
+ * shadow-ray ordering, shadow rays, resolve. LG_ERR_STATE if there is none. */
 lg_status lg_render_wave_times(lg_ctx* ctx, double ms[5]);
 
 /* Frame replay: when on, lg_frame_device runs the frame once, captures the

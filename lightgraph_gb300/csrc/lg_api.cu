@@ -1406,6 +1406,7 @@ lg_status Ctx::render(const lg_camera* c) {
     CK(d_ps_scan.reserve(sizeof(int32_t) * (nps1 / 1024 + 2)), "render alloc");
     CK(d_ps_total.reserve(sizeof(int32_t) * 2), "render alloc");
     CK(d_ps_data.reserve(pixel_sample_bytes() * nps1), "render alloc");
+    waves_recorded = false;
     wmark(0);
     CK(launch_render_count(sc, cam, sg, d_ps_count.as<int32_t>(), st), "render count");
     CK(launch_exclusive_scan(d_ps_count.as<int32_t>(), n_ps, d_ps_offset.as<int32_t>(), d_ps_scan.as<int32_t>(),
@@ -1457,6 +1458,7 @@ lg_status Ctx::render(const lg_camera* c) {
                            d_emission.as<float4>(), d_counters.as<unsigned long long>(), sms, st,
                            profiling ? wev + 2 : nullptr),
        "render");
+    waves_recorded = profiling;
     return LG_OK;
 }
 
@@ -1533,6 +1535,7 @@ extern "C" lg_status lg_frame_device(lg_ctx* handle, int max_connect, double poi
         CK(cudaGraphLaunch(ctx->graph_exec, ctx->st), "frame graph launch");
         ++g_launch_counter;
         ctx->ev_recorded = ctx->profiling;
+        ctx->waves_recorded = ctx->profiling;
         return LG_OK;
     }
     // run the frame once (this also tunes and allocates), then capture the
@@ -1589,7 +1592,7 @@ lg_status Ctx::frame_enqueue(double point_voxel_size, const lg_camera* camera) {
 extern "C" lg_status lg_render_wave_times(lg_ctx* handle, double ms[5]) {
     Ctx* ctx = reinterpret_cast<Ctx*>(handle);
     GUARD(ctx);
-    if (!ctx->ev_recorded || !ctx->wev[Ctx::kWaves]) return ctx->fail(LG_ERR_STATE, "no profiled frame");
+    if (!ctx->waves_recorded || !ctx->wev[Ctx::kWaves]) return ctx->fail(LG_ERR_STATE, "no profiled render");
     if (!ms) return ctx->fail(LG_ERR_INVALID, "null output");
     CK(cudaEventSynchronize(ctx->wev[Ctx::kWaves]), "event sync");
     for (int k = 0; k < Ctx::kWaves; ++k) {

@@ -153,7 +153,8 @@ struct Ctx {
     static constexpr int kStages = 7;  // build, march, fw, light, diffuse, splat, render
     bool profiling = false;
     cudaEvent_t ev[kStages + 1] = {};
-    bool ev_recorded = false;
+    bool ev_recorded = false;     // a whole profiled frame (stage events)
+    bool waves_recorded = false;  // a profiled render (wave events), frame or lg_render
     void mark(int k) {
         if (profiling && ev[k]) cudaEventRecord(ev[k], st);
     }

@@ -381,6 +381,14 @@ class Context:
         self._ck(self.lib.lg_render(self.h, C.byref(cam), *[ptr(f) for f in films]))
         return Films(*films)
 
+    def render_wave_times(self):
+        """Wave durations (ms) of the last render made with profiling on:
+        primary count + scan, primary shading, shadow-ray ordering, shadow
+        rays, resolve."""
+        ms = (C.c_double * 5)()
+        self._ck(self.lib.lg_render_wave_times(self.h, ms))
+        return list(ms)
+
     def render_stats(self):
         """(primary density samples, shadow density samples) of the last render."""
         a, b = C.c_uint64(), C.c_uint64()

@@ -206,3 +206,21 @@ def test_deterministic(gpu_ctx, small_scene):
     b = gpu_ctx.render_frame(sc.points, sc.radius_sq, sc.opts, sc.max_connect)
     for name in ["rgba", "direct", "scatter", "emission"]:
         assert np.array_equal(getattr(a, name), getattr(b, name))
+
+
+def test_render_wave_times_after_lg_render(gpu_ctx, small_scene, small_solved):
+    """Profiling covers a render made through lg_render as well as a frame:
+    the five wave timers are positive and add up to less than the call."""
+    import time
+    sc = small_scene
+    gpu_ctx.lib.lg_set_profiling(gpu_ctx.h, 1)
+    try:
+        gpu_ctx.splat()
+        t0 = time.perf_counter()
+        gpu_ctx.render(sc.opts)
+        wall_ms = (time.perf_counter() - t0) * 1e3
+        waves = gpu_ctx.render_wave_times()
+    finally:
+        gpu_ctx.lib.lg_set_profiling(gpu_ctx.h, 0)
+    assert all(w > 0 for w in waves), waves
+    assert sum(waves) < wall_ms
