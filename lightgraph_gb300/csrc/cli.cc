@@ -28,7 +28,7 @@ namespace {
 
 void print_help() {
     std::cout <<
-        "-vdbIn                  : not supported in this build (no OpenVDB); use -synthetic or -rawIn\n"
+        "-vdbIn                  : not supported (no OpenVDB in this binary); use -synthetic or -rawIn\n"
         "-synthetic              : kind:res, kind in {sphere, cumulus}   ex: cumulus:512\n"
         "-rawIn                  : file:res:voxelSize (dense float32 res^3, x fastest)\n"
         "-exrOut                 : output EXR (13 channels, uncompressed)\n"
@@ -97,7 +97,7 @@ int main(int argc, char** argv) {
         if (a == "-h" || a == "-help" || a == "--help") { print_help(); return 0; }
         else if (a == "-v") verbose = true;
         else if (a == "-geoDump") geo_dump = true;
-        else if (a == "-vdbIn") { std::cerr << "-vdbIn needs OpenVDB, which this build does not link; use -synthetic or -rawIn\n"; return 1; }
+        else if (a == "-vdbIn") { std::cerr << "-vdbIn needs OpenVDB, which this binary does not link; use -synthetic or -rawIn\n"; return 1; }
         else if (a == "-synthetic") synthetic = next();
         else if (a == "-rawIn") raw_in = next();
         else if (a == "-exrOut") exr_out = next();

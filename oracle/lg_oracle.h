@@ -2,9 +2,9 @@
  * lg_oracle.h -- CPU oracle of the LightGraph multiple-scattering path.
  *
  * TEST INFRASTRUCTURE. Only tests/, __graft_entry__.smoke() and bench.py's CPU
- * baseline may load this library, and only as the checker or the timed CPU
- * baseline: the product (lightgraph_gb300) never links, calls or falls back
- * to it.
+ * baseline may load this library, and only to produce the results the GPU
+ * path is compared with or as the timed CPU baseline: the product
+ * (lightgraph_gb300) never links, calls or falls back to it.
  *
  * It restates, in FP64 C++ and in the loop order of the reference
  * (asiroisvigneux/LightGraph), the functions of the hot path:

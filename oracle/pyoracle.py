@@ -1,8 +1,9 @@
 """ctypes binding of the CPU oracle (oracle/lg_oracle.h).
 
 TEST INFRASTRUCTURE: imported only by tests/, __graft_entry__.smoke() and the
-CPU-baseline leg of bench.py, as the checker / the timed CPU baseline. The
-product package (lightgraph_gb300) never imports it.
+CPU-baseline leg of bench.py, as the reference results the GPU path is
+compared with, or as the timed CPU baseline. The product package
+(lightgraph_gb300) never imports it.
 
 PARITY UNPINNED: the reference has no tests or fixtures and cannot be built
 here; see lg_oracle.h.
