@@ -146,3 +146,35 @@ def test_fw_full_size_properties(gpu_ctx):
     rhs = d[i, k].astype(np.float64) + d[k, j].astype(np.float64)
     ok = ~np.isfinite(rhs) | (lhs <= rhs * (1 + 1e-6))
     assert ok.all()
+
+
+def test_fw_ragged_batch_edge_cases(gpu_ctx):
+    """A batch with an empty graph, single points, sizes off the 64 / 128
+    block grid and one that spans several rounds: the symmetric persistent
+    solve (4), the general one (2) and the per-round launches (0) agree bit
+    for bit, and match the FP32 oracle within 1e-6."""
+    sc = scenes.small(n_points=16, width=32, height=32)
+    sizes = [0, 1, 2, 65, 129, 300, 1]
+    sc.points = [scenes.points(sc.density.values, sc.density.voxel_size, n, seed=200 + g) if n > 0
+                 else np.zeros((0, 3), np.float32) for g, n in enumerate(sizes)]
+    sc.radius = [0.2] * len(sizes)
+    sc.opts.iter = len(sizes)
+    res = {}
+    for schedule in (0, 2, 4):
+        S, dist, used, _ = solve_with(gpu_ctx, sc, schedule)
+        assert used == schedule
+        res[schedule] = (S, dist)
+    gpu_ctx.set_fw_schedule(-1)
+    S0, d0 = res[0]
+    for schedule in (2, 4):
+        for g in range(len(sizes)):
+            assert np.array_equal(res[schedule][1][g], d0[g]), (schedule, g)
+    for g, n in enumerate(sizes):
+        assert d0[g].shape == (n, n)
+        if n == 0:
+            continue
+        ref = po.fw_minplus_f32(S0[g])
+        np.fill_diagonal(ref, 0.0)
+        fin = np.isfinite(ref)
+        assert np.array_equal(np.isfinite(d0[g]), fin), g
+        assert np.allclose(d0[g][fin], ref[fin], rtol=1e-6, atol=0), g
