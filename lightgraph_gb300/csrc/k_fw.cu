@@ -8,30 +8,34 @@
 //   S_ij = min(S_ij, S_ik + S_kj).
 // This file solves that recurrence in FP32 with the 3-phase blocked schedule,
 // k-blocks of 64:
-//   panel tiles : the diagonal tile is closed in shared memory, then one tile
-//                 of the k-block row or column panel (every panel CTA
-//                 recomputes the diagonal tile, which saves a launch and a
-//                 dependency per round);
+//   diagonal    : the 64 x 64 diagonal block is closed in shared memory
+//                 (blocked FW on 16 x 16 sub-blocks, close_diag_blocked);
+//   panels      : the k-block row and column panels, one min-plus product
+//                 each against the closed diagonal block;
 //   update tiles: every other element, S_ij = min(S_ij, min_k A_ik + B_kj),
 //                 a min-plus product on the CUDA cores. Each thread owns an
 //                 8x8 register tile and consumes k in pairs:
 //                   s = add.rn.f32x2({A_ik, A_ik+1}, {B_kj, B_k+1,j})
 //                   C_ij = min.f32(C_ij, s.x, s.y)        (3-input min)
-//                 i.e. 4 FP32 ops in 2 instructions.
+//                 i.e. 4 FP32 ops in 2 instructions. Each op still takes an
+//                 FP32 lane cycle, so min-plus tops out near half of the
+//                 FMA-counted FP32 peak (k_fw_inner_loop measures it).
 // It is not a dense contraction, so tensor cores do not apply.
 // All values must be >= 0 (or +inf); then row and column k do not change in
 // round k, which makes each round's updates independent of their order.
 //
-// Two drivers share the tile code:
-//   fw_solve         : one matrix, two launches per round (k_fw_panels,
-//                      k_fw_update);
-//   fw_solve_batched : many matrices of different sizes in ONE persistent
-//                      launch (k_fw_persistent). CTAs claim work items from a
-//                      queue ordered round by round with a one-round
-//                      look-ahead; an item waits (bounded) on the version
-//                      counters of the 64 x 64 blocks it reads, whose writers
-//                      always come earlier in the queue, so the schedule
-//                      cannot deadlock whatever the residency.
+// Three drivers share the tile code:
+//   fw_solve             : one matrix of any kind, two launches per round
+//                          (k_fw_panels, k_fw_update);
+//   fw_solve_batched     : many matrices of any kind and different sizes in
+//                          ONE persistent launch (k_fw_persistent);
+//   fw_solve_batched_sym : the same for symmetric matrices (LightGraph's),
+//                          computing only the blocks on and above the
+//                          diagonal (k_fw_persistent_sym, then k_fw_mirror).
+// In the persistent launches CTAs claim work items from a queue; an item waits
+// (bounded) on the version counters of the 64 x 64 blocks it reads, whose
+// writers always come earlier in the queue, so the schedule cannot deadlock
+// whatever the residency (fw_queue_replay checks every queue on the host).
 #include <algorithm>
 #include <functional>
 #include <queue>
