@@ -62,8 +62,20 @@ __global__ void __launch_bounds__(256) k_candidates(const float* __restrict__ pt
 }
 
 // One CTA per graph. Candidate rows are staged into shared memory in chunks
-// by the whole CTA; warp 0 then resolves the rows of the chunk in order.
+// of 64 rows, double buffered: warp 0 resolves the rows of one chunk in order
+// while warps 1-7 stage the next.
 constexpr int kGreedyChunk = 64;
+
+__device__ __forceinline__ void greedy_stage(const GraphInfo& g, const uint16_t* __restrict__ cand,
+                                             const int32_t* __restrict__ cand_cnt, int r0, int rows, uint16_t* cs,
+                                             int32_t* cc, int t, int nt) {
+    for (int k = t; k < rows * kCandCap; k += nt) {
+        const int r = k / kCandCap, c = k - r * kCandCap;
+        const int total = cand_cnt[g.pt_off + r0 + r];
+        if (c < min(total, kCandCap)) cs[k] = cand[(g.pt_off + r0 + r) * kCandCap + c];
+    }
+    for (int k = t; k < rows; k += nt) cc[k] = cand_cnt[g.pt_off + r0 + k];
+}
 
 __global__ void __launch_bounds__(256) k_greedy(const float* __restrict__ pts,
                                                 const GraphInfo* __restrict__ graphs,
@@ -74,26 +86,27 @@ __global__ void __launch_bounds__(256) k_greedy(const float* __restrict__ pts,
     extern __shared__ uint8_t smem[];
     const GraphInfo g = graphs[blockIdx.x];
     const int n = g.n;
-    uint16_t* cs = reinterpret_cast<uint16_t*>(smem);                   // chunk x cap
-    int32_t* cc = reinterpret_cast<int32_t*>(cs + kGreedyChunk * kCandCap);  // chunk
-    uint8_t* cnt = reinterpret_cast<uint8_t*>(cc + kGreedyChunk);         // n
+    uint16_t* cs2 = reinterpret_cast<uint16_t*>(smem);                       // 2 x chunk x cap
+    int32_t* cc2 = reinterpret_cast<int32_t*>(cs2 + 2 * kGreedyChunk * kCandCap);  // 2 x chunk
+    uint8_t* cnt = reinterpret_cast<uint8_t*>(cc2 + 2 * kGreedyChunk);        // n
     for (int k = threadIdx.x; k < n; k += blockDim.x) cnt[k] = 0;
+    if (n > 0) greedy_stage(g, cand, cand_cnt, 0, min(kGreedyChunk, n), cs2, cc2, threadIdx.x, blockDim.x);
     const int lane = threadIdx.x & 31;
     const float* P = pts + 3 * g.pt_off;
     const float lo = g.r2 * (1.f - 7.62939453125e-06f), hi = g.r2 * (1.f + 7.62939453125e-06f);
     int ecount = 0;  // valid in warp 0
     int2* E = edges + g.e_off;
-    for (int r0 = 0; r0 < n; r0 += kGreedyChunk) {
+    for (int r0 = 0, buf = 0; r0 < n; r0 += kGreedyChunk, buf ^= 1) {
         const int rows = min(kGreedyChunk, n - r0);
-        __syncthreads();
-        for (int k = threadIdx.x; k < rows * kCandCap; k += blockDim.x) {
-            const int r = k / kCandCap, c = k - r * kCandCap;
-            const int total = cand_cnt[g.pt_off + r0 + r];
-            if (c < min(total, kCandCap)) cs[k] = cand[(g.pt_off + r0 + r) * kCandCap + c];
-        }
-        for (int k = threadIdx.x; k < rows; k += blockDim.x) cc[k] = cand_cnt[g.pt_off + r0 + k];
-        __syncthreads();
-        if (threadIdx.x < 32) {
+        __syncthreads();  // chunk r0 staged; the other buffer is free
+        const uint16_t* cs = cs2 + buf * kGreedyChunk * kCandCap;
+        const int32_t* cc = cc2 + buf * kGreedyChunk;
+        if (threadIdx.x >= 32) {
+            const int r1 = r0 + kGreedyChunk;
+            if (r1 < n)
+                greedy_stage(g, cand, cand_cnt, r1, min(kGreedyChunk, n - r1), cs2 + (buf ^ 1) * kGreedyChunk * kCandCap,
+                             cc2 + (buf ^ 1) * kGreedyChunk, threadIdx.x - 32, blockDim.x - 32);
+        } else {
             for (int r = 0; r < rows; ++r) {
                 const int i = r0 + r;
                 int need = max_connect - (int)cnt[i];
@@ -180,7 +193,7 @@ cudaError_t launch_greedy(const float* pts, const GraphInfo* graphs, int n_graph
                           const uint16_t* cand, const int32_t* cand_cnt, int max_connect,
                           int2* edges, int32_t* edge_cnt, cudaStream_t st) {
     if (n_graphs == 0) return cudaSuccess;
-    const size_t smem = kGreedyChunk * kCandCap * sizeof(uint16_t) + kGreedyChunk * sizeof(int32_t) +
+    const size_t smem = 2 * kGreedyChunk * kCandCap * sizeof(uint16_t) + 2 * kGreedyChunk * sizeof(int32_t) +
                         (size_t)max_n;
     cudaError_t e = cudaFuncSetAttribute(k_greedy, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)smem);
