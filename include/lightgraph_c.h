@@ -233,6 +233,7 @@ lg_status lg_scatter_graphs(lg_ctx* ctx, const lg_scatter_opts* opts, int first_
  * reference's greedy rule: pairs closer than sqrt(radius_sq[g]) in FP64, at
  * most max_connect edges per point, decided in (i, j) order.
  * Replaces LightGraph::buildGraph (src/LightGraph.h:287-318).
+ *   n_graphs: 1..65535 graphs of 0..65535 points each (LG_ERR_INVALID otherwise)
  *   points  : sum(N_g) x 3 floats, graph g occupies rows offsets[g]..offsets[g+1]
  *   radius_sq: per graph, the FP32 value searchRadiusConnectSquared
  *   adj_out : optional, sum(N_g^2) bytes, graph g row-major at sum_{h<g} N_h^2

@@ -542,7 +542,8 @@ DevScene Ctx::scene() const {
 lg_status Ctx::load_graphs(int n_graphs, const float* points, const int64_t* offsets,
                            const float* radius_sq, int max_connect) {
     Ctx* ctx = this;
-    if (n_graphs < 1) return fail(LG_ERR_INVALID, "n_graphs must be >= 1");
+    // graph-indexed kernels put the graph in gridDim.y (at most 65535)
+    if (n_graphs < 1 || n_graphs > 65535) return fail(LG_ERR_INVALID, "n_graphs must be in [1, 65535]");
     if (!offsets || !radius_sq) return fail(LG_ERR_INVALID, "null offsets or radius");
     if (max_connect < 0 || max_connect > 255) return fail(LG_ERR_INVALID, "max_connect must be in [0, 255]");
     if (offsets[0] != 0) return fail(LG_ERR_INVALID, "offsets[0] must be 0");
