@@ -142,20 +142,17 @@ __global__ void __launch_bounds__(kDartThreads, 4) k_dart(DevGrid g, DartParams 
     for (uint32_t base = 0; base < prm.scatter_count; base += kDartBlock) {
         if (s_done) break;
         // 1a. twist: new[i] = f(old[i], old[i+1], x) with x = old[i+397] for
-        // i < 227 and new[i-227] after, i = 623 taking new[0] as its next
-        if (tid < 227) nxt[tid] = mt_twist_word(cur[tid], cur[tid + 1], cur[tid + kMtM]);
-        __syncthreads();
+        // i < 227 and new[i-227] after, i = 623 taking new[0] as its next.
+        // Word i >= 227 depends only on word i - 227, so thread t computes
+        // the chain t, t + 227, t + 454 alone; word 623 (from new[0] and
+        // new[396]) is computed by the one thread that uses it, in 1b.
         if (tid < 227) {
-            const int i = 227 + tid;
-            nxt[i] = mt_twist_word(cur[i], cur[i + 1], nxt[i - 227]);
+            uint32_t x = mt_twist_word(cur[tid], cur[tid + 1], cur[tid + kMtM]);
+            nxt[tid] = x;
+            x = mt_twist_word(cur[tid + 227], cur[tid + 228], x);
+            nxt[tid + 227] = x;
+            if (tid < 169) nxt[tid + 454] = mt_twist_word(cur[tid + 454], cur[tid + 455], x);
         }
-        __syncthreads();
-        if (tid < 169) {
-            const int i = 454 + tid;
-            nxt[i] = mt_twist_word(cur[i], cur[i + 1], nxt[i - 227]);
-        }
-        __syncthreads();
-        if (tid == 0) nxt[623] = mt_twist_word(cur[623], nxt[0], nxt[396]);
         __syncthreads();
         {
             uint32_t* t = cur;
@@ -164,6 +161,9 @@ __global__ void __launch_bounds__(kDartThreads, 4) k_dart(DevGrid g, DartParams 
         }
         // 1b. positions and densities of this block's candidates
         if (tid < kDartBlock) {
+            // the last word of the block (read only by this candidate, and by
+            // the next twist after several barriers)
+            if (tid == kDartBlock - 1) cur[kMtN - 1] = mt_twist_word(nxt[kMtN - 1], cur[0], cur[396]);
             const uint32_t n = base + (uint32_t)tid;
             bool ok = false;
             if (n < prm.scatter_count) {
