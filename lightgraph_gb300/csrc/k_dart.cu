@@ -12,8 +12,8 @@
 //
 // Here one CTA runs one iteration and reproduces that sequence exactly. It
 // takes the candidates a block of 208 at a time (208 x 3 = 624 draws: one
-// MT19937 state block, renewed by the CTA's threads in four dependent phases
-// of at most 227 words):
+// MT19937 state block, renewed with one barrier: word i >= 227 depends only
+// on word i - 227, so 227 threads each compute a chain of up to three words):
 //   1. every thread of a candidate computes its position and its density in
 //      FP32, re-tested with the reference's sampler arithmetic (float voxel
 //      values, double weights, a float result per interpolation step) when
@@ -35,7 +35,7 @@ namespace lg {
 
 namespace {
 
-constexpr int kDartThreads = 512;  // >= 227 (the widest twist phase); 4 CTAs per SM
+constexpr int kDartThreads = 512;  // >= 227 (the twist chains); 4 CTAs per SM
 constexpr int kDartBlock = 208;    // candidates per MT block (3 draws each)
 constexpr int kDartWarps = kDartThreads / 32;
 
