@@ -246,7 +246,9 @@ __global__ void __launch_bounds__(256) k_ray_bins(const ShadowTask* __restrict__
             p[2] = q.z;
         }
         for (int k = 0; k < rb.n; ++k) {
-            const unsigned long long key = valid ? (unsigned long long)ray_key(rb.b[k], p, u * kRayUnit) : ~0ull;
+            // keys index the counts array (fewer than 2^31 of them, checked by
+            // the host), so the cheaper 32-bit match groups them
+            const uint32_t key = valid ? (uint32_t)ray_key(rb.b[k], p, u * kRayUnit) : 0xFFFFFFFFu;
             const unsigned grp = __match_any_sync(0xffffffffu, key);
             if (!valid) continue;
             const int leader = __ffs(grp) - 1;

@@ -1430,6 +1430,7 @@ lg_status Ctx::render(const lg_camera* c) {
     ro.rb = ray_bins(sc, cap);
     ro.n_keys = 0;
     for (int k = 0; k < ro.rb.n; ++k) ro.n_keys += ro.rb.b[k].nkeys;
+    if (ro.n_keys >= INT32_MAX) return fail(LG_ERR_INVALID, "more than 2^31 shadow-ray order keys");
     const size_t order_bytes = sizeof(int32_t) * (size_t)(n_lights * ((cap + kRayUnit - 1) / kRayUnit));
     const size_t direct_bytes = sizeof(float4) * (size_t)(n_lights * cap);
     const size_t key_bytes = sizeof(int32_t) * (size_t)std::max<int64_t>(ro.n_keys, 1);
