@@ -38,7 +38,8 @@ sys.path.insert(0, ROOT)
 STAGES = ["build_graph", "edge_march", "floyd_warshall", "vertex_light", "diffuse", "splat", "render"]
 NOMINAL_FP32_TFLOPS = 152 * 128 * 2 * 2.070 / 1000  # GB300: SMs x FP32 lanes x 2 (FMA) x 2.07 GHz
 FW_SCHEDULES = {0: "per-round launches", 1: "persistent 1 CTA/SM", 2: "persistent 2 CTA/SM",
-                3: "symmetric persistent 1 CTA/SM", 4: "symmetric persistent 2 CTA/SM"}
+                3: "symmetric persistent 1 CTA/SM", 4: "symmetric persistent 2 CTA/SM",
+                5: "symmetric persistent 2 CTA/SM, TMA-staged update operands"}
 def fw_executed_flops(ld, schedule):
     """FP32 ops (add + min per update) the solve's kernels execute for one
     ld x ld matrix: the general schedules run every (i, j, k); the symmetric
@@ -54,7 +55,8 @@ def fw_executed_flops(ld, schedule):
 
 
 FW_KERNELS = {0: "k_fw_update+k_fw_panels", 1: "k_fw_persistent", 2: "k_fw_persistent",
-              3: "k_fw_persistent_sym+k_fw_mirror", 4: "k_fw_persistent_sym+k_fw_mirror"}
+              3: "k_fw_persistent_sym+k_fw_mirror", 4: "k_fw_persistent_sym+k_fw_mirror",
+              5: "k_fw_persistent_sym<tma>+k_fw_mirror"}
 
 
 def parse():
@@ -72,7 +74,7 @@ def parse():
     ap.add_argument("--rate", type=float, default=50.0, help="Poisson arrival rate of the serving stream (req/s)")
     ap.add_argument("--batched", type=int, default=1, help="run the 64-graph batched measurement (0: skip)")
     ap.add_argument("--fw-schedule", type=int, default=-1,
-                    help="pin the Floyd-Warshall schedule (0-4; -1: autotuned). Profiling runs pin the "
+                    help="pin the Floyd-Warshall schedule (0-5; -1: autotuned). Profiling runs pin the "
                          "schedule the autotuner picks without a profiler, whose per-launch overhead "
                          "distorts the trial timings")
     ap.add_argument("--ref-iters", type=int, default=500,

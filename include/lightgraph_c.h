@@ -361,10 +361,14 @@ uint64_t lg_frame_launches(const lg_ctx* ctx);
  * per graph; 1 or 2: one persistent launch for every graph with 1 or 2 CTAs
  * per SM (a work queue with per-graph dependency counters); 3 or 4: the
  * symmetric persistent solve (for the symmetric matrices the graph stage
- * builds) with 1 or 2 CTAs per SM. A schedule set here stays in force for
- * later graph builds until -1 is set again. */
+ * builds) with 1 or 2 CTAs per SM; 5: schedule 4 with the update tiles'
+ * operands staged into shared memory by TMA bulk copies (cp.async.bulk on an
+ * mbarrier) instead of through registers. All schedules give the same
+ * distances bit for bit. A schedule set here stays in force for later graph
+ * builds until -1 is set again. */
 lg_status lg_set_fw_schedule(lg_ctx* ctx, int schedule);
-/* The schedule in use and the autotuner's timings (ms) of schedules 0..4.
+/* The schedule in use and the autotuner's timings (ms) of schedules 0..5
+ * (0 for a schedule it did not time).
  * Returns LG_ERR_TIMEOUT if a persistent solve reported a stalled queue. */
 lg_status lg_fw_schedule(lg_ctx* ctx, int* schedule, double* tuned_ms, int n);
 /* The ceiling of the Floyd-Warshall update tiles on this GPU: FP32 ops/s
@@ -375,7 +379,7 @@ lg_status lg_fw_schedule(lg_ctx* ctx, int* schedule, double* tuned_ms, int n);
 lg_status lg_fw_inner_loop_rate(lg_ctx* ctx, double* tflops);
 /* Host-only check of the persistent schedules' work queue for graphs of the
  * given point counts (no device work). Builds the queue the solve would use
- * (sym != 0: the symmetric solve of schedules 3 and 4, in its structural
+ * (sym != 0: the symmetric solve of schedules 3 to 5, in its structural
  * and its list-scheduled order for 152 and 304 CTAs) and replays it in
  * order with the kernels' dependency waits and version updates. LG_OK when
  * every item's waits are met by earlier items (the launch cannot deadlock)

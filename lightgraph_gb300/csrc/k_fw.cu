@@ -979,6 +979,62 @@ size_t fw_panel_words(const FwGraph& g) { return (size_t)kPanelSlots * g.nu * 32
 
 __device__ __forceinline__ int up_block(int a, int b, int nt) { return a < b ? a * nt + b : b * nt + a; }
 
+// TMA bulk copies (cp.async.bulk, global -> shared) completed on an mbarrier:
+// the update tiles of the symmetric solve's TMA schedule stage their two
+// panel-slot operands this way. One mbarrier per CTA; each update item arms it
+// with its byte count (one arrival) and every thread waits for the phase.
+__device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(bar)) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n\t}" ::"r"(
+                     smem_addr(bar)),
+                 "r"(bytes)
+                 : "memory");
+}
+
+// Copy `bytes` (a multiple of 16; both addresses 16-byte aligned) from global
+// src to shared dst; completion counts against bar's transaction bytes. The
+// proxy fence orders the generic-proxy writes this thread has seen (panel
+// slots published by other CTAs) before the async-proxy read.
+__device__ __forceinline__ void tma_copy_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+    asm volatile("fence.proxy.async.global;" ::: "memory");
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_addr(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_addr(bar))
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try(uint64_t* bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, 20000;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Bounded wait for phase `parity` of bar (try_wait suspends the thread until
+// the phase completes or about 20 us pass). If it gives up it raises err (the
+// whole launch then stops at its next item) and waits once more, again
+// bounded, so that no copy is left writing this CTA's shared memory.
+__device__ __forceinline__ void mbar_wait(uint64_t* bar, uint32_t parity, uint32_t* err) {
+    uint32_t spins = 0;
+    while (!mbar_try(bar, parity)) {
+        if (++spins == (1u << 16)) atomicExch(err, 1u);
+        if (spins >= (1u << 17)) return;
+    }
+}
+
+// Generic-proxy shared-memory writes of this thread before a later TMA write
+// of the same bytes (an item's shared memory is the next item's TMA target).
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
 // Closes diagonal block kb held in sm.T, writes it back to d and its rows to
 // the round's panel slot Pr.
 __device__ __noinline__ void close_publish_diag(float* __restrict__ d, int ld, int kb, float2* __restrict__ Pr,
@@ -1116,12 +1172,25 @@ __device__ __forceinline__ void fw_strip_tile_sym(float* __restrict__ d, int ld,
 // that other items of the round own (row / column block kb: panel items;
 // row / column block kb + 1: strip items) and, in a diagonal tile, the block
 // below the diagonal are neither loaded nor stored.
+template <bool kTma>
 __device__ __forceinline__ void fw_update_tile_sym(float* __restrict__ d, int ld, int kb, int ti, int tj,
                                                    const float2* __restrict__ Pr, float2* __restrict__ As,
-                                                   float2* __restrict__ Bs) {
+                                                   float2* __restrict__ Bs, uint64_t* bar, uint32_t parity,
+                                                   uint32_t* err) {
     const int I0 = ti * kTile, J0 = tj * kTile;
     const int tid = threadIdx.x;
-    {
+    if (kTma) {
+        // both operands are contiguous 32 KB runs of the panel slot: one TMA
+        // copy each (lanes 0 and 1 of warp 0), in flight while the tile loads
+        if (tid < 32) {
+            if (tid == 0) mbar_expect_tx(bar, 2 * 32 * kTile * (uint32_t)sizeof(float2));
+            __syncwarp();
+            if (tid < 2)
+                tma_copy_g2s(tid == 0 ? As : Bs, Pr + (size_t)(tid == 0 ? ti : tj) * 32 * kTile,
+                             32 * kTile * (uint32_t)sizeof(float2), bar);
+        }
+    } else {
+        // through registers: every thread moves 8 + 8 float4
         const float4* pa = reinterpret_cast<const float4*>(Pr + (size_t)ti * 32 * kTile);
         const float4* pb = reinterpret_cast<const float4*>(Pr + (size_t)tj * 32 * kTile);
         float4* sa = reinterpret_cast<float4*>(As);
@@ -1159,7 +1228,8 @@ __device__ __forceinline__ void fw_update_tile_sym(float* __restrict__ d, int ld
             }
         }
     }
-    __syncthreads();
+    if (kTma) mbar_wait(bar, parity, err);
+    else __syncthreads();
 
 #pragma unroll 1
     for (int kp = 0; kp < 32; ++kp) {
@@ -1253,6 +1323,7 @@ __device__ __forceinline__ SymItem decode_sym(const int4* items, const FwGraph* 
     return m;
 }
 
+template <bool kTma>
 __global__ void __launch_bounds__(256, 2) k_fw_persistent_sym(float* __restrict__ base, const FwGraph* __restrict__ gs,
                                                               const int4* __restrict__ items, int n_items,
                                                               uint32_t* __restrict__ sync, float2* __restrict__ panels) {
@@ -1262,8 +1333,11 @@ __global__ void __launch_bounds__(256, 2) k_fw_persistent_sym(float* __restrict_
     PanelSmem& psm = *reinterpret_cast<PanelSmem*>(fw_smem);
     __shared__ int s_item;
     __shared__ int s_abort;
+    __shared__ __align__(8) uint64_t s_bar;  // the TMA copies of update items (kTma)
     uint32_t* head = sync;
     uint32_t* err = sync + 1;
+    uint32_t tma_phase = 0;  // update items so far: s_bar's phase (uniform over the CTA)
+    if (kTma && threadIdx.x == 0) mbar_init(&s_bar);
     for (;;) {
         if (threadIdx.x == 0) {
             const int it = (int)atomicAdd(head, 1u);
@@ -1313,8 +1387,12 @@ __global__ void __launch_bounds__(256, 2) k_fw_persistent_sym(float* __restrict_
             float2* Pnext = panels + g.pofs + (size_t)((w.y + 1) % kPanelSlots) * g.nu * 32 * kTile;
             fw_strip_tile_sym(d, g.ld, min(w.w, w.y + 1), max(w.w, w.y + 1), Pr, Pnext, As, Bs, psm);
         } else {
-            fw_update_tile_sym(d, g.ld, w.y, w.w / g.nu, w.w % g.nu, Pr, As, Bs);
+            fw_update_tile_sym<kTma>(d, g.ld, w.y, w.w / g.nu, w.w % g.nu, Pr, As, Bs, &s_bar, tma_phase & 1u,
+                                     err);
+            if (kTma) ++tma_phase;
         }
+        // this item's shared-memory writes come before the next TMA write
+        if (kTma) fence_async_smem();
         __threadfence();
         __syncthreads();
         if (threadIdx.x == 0) {
@@ -1363,19 +1441,25 @@ __global__ void __launch_bounds__(256) k_fw_mirror(float* __restrict__ base, con
 }
 
 cudaError_t fw_solve_batched_sym(float* base, const FwGraph* graphs, int n_graphs, int max_nt, const int4* items,
-                                 int n_items, uint32_t* sync, size_t sync_words, float2* panels, int ctas,
+                                 int n_items, uint32_t* sync, size_t sync_words, float2* panels, int ctas, bool tma,
                                  cudaStream_t st) {
     static bool attr_set = false;
     if (!attr_set) {
-        cudaError_t e = cudaFuncSetAttribute(k_fw_persistent_sym, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        cudaError_t e = cudaFuncSetAttribute(k_fw_persistent_sym<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)kUpdateSymSmem);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(k_fw_persistent_sym<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)kUpdateSymSmem);
         if (e != cudaSuccess) return e;
         attr_set = true;
     }
     cudaError_t e = cudaMemsetAsync(sync, 0, sizeof(uint32_t) * sync_words, st);
     if (e != cudaSuccess) return e;
     if (n_items == 0) return cudaSuccess;
-    k_fw_persistent_sym<<<ctas, 256, kUpdateSymSmem, st>>>(base, graphs, items, n_items, sync, panels);
+    if (tma)
+        k_fw_persistent_sym<true><<<ctas, 256, kUpdateSymSmem, st>>>(base, graphs, items, n_items, sync, panels);
+    else
+        k_fw_persistent_sym<false><<<ctas, 256, kUpdateSymSmem, st>>>(base, graphs, items, n_items, sync, panels);
     ++g_launch_counter;
     if (max_nt > 1) {
         k_fw_mirror<<<dim3(std::min(max_nt * max_nt, 4096), n_graphs), 256, 0, st>>>(base, graphs);
@@ -1386,11 +1470,16 @@ cudaError_t fw_solve_batched_sym(float* base, const FwGraph* graphs, int n_graph
 
 int fw_persistent_sym_ctas_per_sm() {
     int blocks = 0;
-    cudaFuncSetAttribute(k_fw_persistent_sym, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kUpdateSymSmem);
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, k_fw_persistent_sym, 256, kUpdateSymSmem) !=
-        cudaSuccess)
+    int blocks_tma = 0;
+    cudaFuncSetAttribute(k_fw_persistent_sym<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)kUpdateSymSmem);
+    cudaFuncSetAttribute(k_fw_persistent_sym<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kUpdateSymSmem);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, k_fw_persistent_sym<false>, 256, kUpdateSymSmem) !=
+            cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_tma, k_fw_persistent_sym<true>, 256, kUpdateSymSmem) !=
+            cudaSuccess)
         return 1;
-    return std::max(blocks, 1);
+    return std::max(std::min(blocks, blocks_tma), 1);
 }
 
 // ---------------------------------------------------------------------------

@@ -838,7 +838,8 @@ lg_status Ctx::march_edges() {
 // Schedules of the path solve: 0 = two launches per round per graph
 // (fw_solve); 1, 2 = one persistent launch for all graphs with 1 or 2 CTAs per
 // SM; 3, 4 = the symmetric persistent solve (the tiles on and above the
-// diagonal, then a mirror pass) with 1 or 2 CTAs per SM. The graph matrices
+// diagonal, then a mirror pass) with 1 or 2 CTAs per SM; 5 = schedule 4 with
+// the update tiles' operands staged by TMA bulk copies. The graph matrices
 // are symmetric by construction (k_march.cu stores every edge both ways).
 static lg_status run_fw_schedule(Ctx* ctx, float* base, int choice) {
     if (choice == 0) {
@@ -853,7 +854,8 @@ static lg_status run_fw_schedule(Ctx* ctx, float* base, int choice) {
     if (choice >= 3) {
         CK(fw_solve_batched_sym(base, ctx->d_fwg.as<FwGraph>(), ctx->n_graphs, ctx->fw_max_nt,
                                 ctx->d_fw_items_sym.as<int4>(), ctx->fw_items_sym_n, ctx->d_fw_sync.as<uint32_t>(),
-                                ctx->fw_sync_n, ctx->d_fw_panels.as<float2>(), (choice - 2) * sms, ctx->st),
+                                ctx->fw_sync_n, ctx->d_fw_panels.as<float2>(), (choice == 3 ? 1 : 2) * sms,
+                                choice == 5, ctx->st),
            "symmetric batched floyd-warshall");
         return LG_OK;
     }
@@ -965,6 +967,7 @@ lg_status Ctx::tune_fw() {
     std::vector<int> cands = {0};
     cands.push_back(fw_persistent_ctas_per_sm() >= 2 ? 2 : 1);
     cands.push_back(fw_persistent_sym_ctas_per_sm() >= 2 ? 4 : 3);
+    if (cands.back() == 4) cands.push_back(5);
     CK(d_fw_tune.reserve(sizeof(float) * std::max<int64_t>(s_floats, 1)), "fw tune alloc");
     cudaEvent_t e0, e1;
     CK(cudaEventCreate(&e0), "event");
@@ -1616,7 +1619,7 @@ extern "C" lg_status lg_set_graph_mode(lg_ctx* handle, int on) {
 extern "C" lg_status lg_set_fw_schedule(lg_ctx* handle, int schedule) {
     Ctx* ctx = reinterpret_cast<Ctx*>(handle);
     GUARD(ctx);
-    if (schedule < -1 || schedule > 4) return ctx->fail(LG_ERR_INVALID, "schedule must be -1, 0, 1, 2, 3 or 4");
+    if (schedule < -1 || schedule > 5) return ctx->fail(LG_ERR_INVALID, "schedule must be -1, 0, 1, 2, 3, 4 or 5");
     ctx->fw_pinned = schedule;
     if (schedule == -1) {
         ctx->fw_choice = -1;
@@ -1633,7 +1636,7 @@ extern "C" lg_status lg_fw_schedule(lg_ctx* handle, int* schedule, double* tuned
     Ctx* ctx = reinterpret_cast<Ctx*>(handle);
     GUARD(ctx);
     if (schedule) *schedule = ctx->fw_choice;
-    for (int k = 0; tuned_ms && k < n && k < 5; ++k) tuned_ms[k] = ctx->fw_tune_ms[k];
+    for (int k = 0; tuned_ms && k < n && k < kFwSchedules; ++k) tuned_ms[k] = ctx->fw_tune_ms[k];
     if (ctx->fw_choice > 0 && ctx->d_fw_sync.bytes >= 8) {
         uint32_t flags[2] = {0, 0};
         CK(cudaMemcpyAsync(flags, ctx->d_fw_sync.p, sizeof flags, cudaMemcpyDeviceToHost, ctx->st), "flag read");

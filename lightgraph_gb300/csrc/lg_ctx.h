@@ -118,7 +118,7 @@ struct Ctx {
     std::vector<std::pair<std::pair<int, int>, int>> fw_tuned;
     int fw_choice = -1;
     int fw_pinned = -1;  // lg_set_fw_schedule's choice, kept across graph builds (-1: autotuned)
-    double fw_tune_ms[5] = {0, 0, 0, 0, 0};
+    double fw_tune_ms[kFwSchedules] = {};
 
     // frame replay through a captured CUDA graph
     bool graph_mode = false;

@@ -41,6 +41,9 @@ cudaError_t launch_vertex_light(const DevScene& sc, const float* pts, const Grap
 // Floyd-Warshall on one matrix (general, any n, ld % 4 == 0).
 cudaError_t fw_solve(float* d, int n, int ld, cudaStream_t st);
 
+// Path-solve schedules (lg_set_fw_schedule): 0 .. kFwSchedules - 1.
+constexpr int kFwSchedules = 6;
+
 // Batched: many matrices in one persistent launch.
 struct FwGraph {
     int64_t off;   // first float of the matrix
@@ -71,9 +74,11 @@ cudaError_t fw_solve_batched(float* base, const FwGraph* graphs, const int4* ite
                              size_t sync_words, int ctas, cudaStream_t st);
 // The same solve for symmetric matrices (every S_ij == S_ji, as LightGraph's
 // path matrices are): computes the tiles on and above the diagonal and then
-// mirrors them below it. panels: sum of fw_panel_words float2.
+// mirrors them below it. panels: sum of fw_panel_words float2. tma: the update
+// tiles stage their operands with TMA bulk copies instead of through registers
+// (the same results bit for bit).
 cudaError_t fw_solve_batched_sym(float* base, const FwGraph* graphs, int n_graphs, int max_nt, const int4* items,
-                                 int n_items, uint32_t* sync, size_t sync_words, float2* panels, int ctas,
+                                 int n_items, uint32_t* sync, size_t sync_words, float2* panels, int ctas, bool tma,
                                  cudaStream_t st);
 int fw_persistent_ctas_per_sm();
 // FP32 ops/s (an add and a min per update) of the update tiles' inner loop

@@ -419,7 +419,8 @@ class Context:
 
     def set_fw_schedule(self, schedule: int) -> None:
         """-1 autotuned, 0 per-graph launches, 1/2 persistent (CTAs per SM),
-        3/4 symmetric persistent (CTAs per SM)."""
+        3/4 symmetric persistent (CTAs per SM), 5 = 4 with the update tiles'
+        operands staged by TMA bulk copies."""
         self._ck(self.lib.lg_set_fw_schedule(self.h, schedule))
 
     def fw_inner_loop_rate(self) -> float:
@@ -431,8 +432,8 @@ class Context:
 
     def fw_schedule(self):
         s = C.c_int()
-        ms = (C.c_double * 5)()
-        self._ck(self.lib.lg_fw_schedule(self.h, C.byref(s), ms, 5))
+        ms = (C.c_double * 6)()
+        self._ck(self.lib.lg_fw_schedule(self.h, C.byref(s), ms, 6))
         return s.value, list(ms)
 
     def set_graph_mode(self, on: bool) -> None:

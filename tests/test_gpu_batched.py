@@ -35,13 +35,14 @@ def solve_with(ctx, sc, schedule):
 
 
 def test_schedules_bit_identical_and_match_oracle(gpu_ctx, uneven_graphs):
-    """Every schedule, the symmetric ones (3, 4) included, gives the same bits;
+    """Every schedule, the symmetric ones (3, 4, and 5 with its TMA-staged
+    update operands) included, gives the same bits;
     the graphs up to 700 points run 12 rounds, so the symmetric solve reuses
     each of its three column-panel slots several times."""
     sc = uneven_graphs
     S0, d0, u0, _ = solve_with(gpu_ctx, sc, 0)
     assert u0 == 0
-    for schedule in (1, 2, 3, 4):
+    for schedule in (1, 2, 3, 4, 5):
         _, ds, us, _ = solve_with(gpu_ctx, sc, schedule)
         assert us == schedule
         for g in range(len(sc.points)):
@@ -58,8 +59,8 @@ def test_schedules_bit_identical_and_match_oracle(gpu_ctx, uneven_graphs):
 
 def test_autotuner_picks_a_schedule(gpu_ctx, uneven_graphs):
     S, d, used, ms = solve_with(gpu_ctx, uneven_graphs, -1)
-    assert used in (0, 2, 4)
-    assert ms[0] > 0 and ms[2] > 0 and ms[4] > 0
+    assert used in (0, 2, 4, 5)
+    assert ms[0] > 0 and ms[2] > 0 and ms[4] > 0 and ms[5] > 0
     _, d0, _, _ = solve_with(gpu_ctx, uneven_graphs, 0)
     for g in range(len(d)):
         assert np.array_equal(d[g], d0[g])
@@ -151,8 +152,8 @@ def test_fw_full_size_properties(gpu_ctx):
 def test_fw_ragged_batch_edge_cases(gpu_ctx):
     """A batch with an empty graph, single points, sizes off the 64 / 128
     block grid and one that spans several rounds: the symmetric persistent
-    solve (4), the general one (2) and the per-round launches (0) agree bit
-    for bit, and match the FP32 oracle within 1e-6."""
+    solve (4, and 5 with TMA staging), the general one (2) and the per-round
+    launches (0) agree bit for bit, and match the FP32 oracle within 1e-6."""
     sc = scenes.small(n_points=16, width=32, height=32)
     sizes = [0, 1, 2, 65, 129, 300, 1]
     sc.points = [scenes.points(sc.density.values, sc.density.voxel_size, n, seed=200 + g) if n > 0
@@ -160,13 +161,13 @@ def test_fw_ragged_batch_edge_cases(gpu_ctx):
     sc.radius = [0.2] * len(sizes)
     sc.opts.iter = len(sizes)
     res = {}
-    for schedule in (0, 2, 4):
+    for schedule in (0, 2, 4, 5):
         S, dist, used, _ = solve_with(gpu_ctx, sc, schedule)
         assert used == schedule
         res[schedule] = (S, dist)
     gpu_ctx.set_fw_schedule(-1)
     S0, d0 = res[0]
-    for schedule in (2, 4):
+    for schedule in (2, 4, 5):
         for g in range(len(sizes)):
             assert np.array_equal(res[schedule][1][g], d0[g]), (schedule, g)
     for g, n in enumerate(sizes):
