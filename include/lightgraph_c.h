@@ -490,6 +490,10 @@ lg_status lg_server_add_volume(lg_server* srv, const lg_grid_desc* density,
 /* Enqueues a request and returns at once; *ticket identifies it.
  * LG_ERR_BUSY: queue full; LG_ERR_NOMEM: larger than the whole budget. */
 lg_status lg_server_submit(lg_server* srv, const lg_request* req, int64_t* ticket);
+/* Non-blocking: *done = 1 once the request has finished (its result waits
+ * for lg_server_wait, which this call does not consume), else 0.
+ * LG_ERR_INVALID for an unknown (or already waited-for) ticket. */
+lg_status lg_server_poll(lg_server* srv, int64_t ticket, int* done);
 /* Waits for a request (timeout_ms < 0: no limit; LG_ERR_TIMEOUT otherwise)
  * and copies its beauty film (width x height x 4 floats) into rgba if
  * non-null. queue_us: submit -> admit, latency_us: submit -> done (host

@@ -145,6 +145,7 @@ SIGNATURES = {
     "lg_server_add_volume": (I32, [P, C.POINTER(GridDesc), P, C.POINTER(GridDesc), P, C.c_int,
                                    C.POINTER(C.c_int32)]),
     "lg_server_submit": (I32, [P, C.POINTER(RequestC), C.POINTER(I64)]),
+    "lg_server_poll": (I32, [P, I64, C.POINTER(C.c_int)]),
     "lg_server_wait": (I32, [P, I64, C.c_int, P, C.POINTER(D), C.POINTER(D)]),
     "lg_request_bytes": (U64, [C.POINTER(RequestC)]),
     "lg_shader_default": (None, [C.POINTER(ShaderC)]),

@@ -317,6 +317,18 @@ extern "C" lg_status lg_server_submit(lg_server* srv, const lg_request* req, int
     return LG_OK;
 }
 
+extern "C" lg_status lg_server_poll(lg_server* srv, int64_t ticket, int* done) {
+    if (!srv || !done) return LG_ERR_INVALID;
+    std::lock_guard<std::mutex> lk(srv->mu);
+    auto it = srv->requests.find(ticket);
+    if (it == srv->requests.end()) {
+        srv->err = "unknown ticket";
+        return LG_ERR_INVALID;
+    }
+    *done = it->second->done ? 1 : 0;
+    return LG_OK;
+}
+
 extern "C" lg_status lg_server_wait(lg_server* srv, int64_t ticket, int timeout_ms, float* rgba, double* queue_us,
                                     double* latency_us) {
     if (!srv) return LG_ERR_INVALID;

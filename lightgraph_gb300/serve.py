@@ -65,6 +65,14 @@ class Server:
         self._keep[tk.value] = req
         return tk.value
 
+    def poll(self, ticket: int) -> bool:
+        """True once the request has finished (its result stays for wait)."""
+        done = C.c_int()
+        st = self.lib.lg_server_poll(self.h, ticket, C.byref(done))
+        if st != _capi.LG_OK:
+            self._err(st)
+        return bool(done.value)
+
     def wait(self, ticket: int, timeout_ms: int = -1, want_image: bool = True):
         req = self._keep.pop(ticket, None)
         img = None

@@ -44,6 +44,19 @@ def test_version_and_no_device_is_reported():
         assert st == _capi.LG_ERR_NODEVICE
 
 
+def test_server_entry_points_reject_null_handles():
+    """The serving calls check their handle and out-pointers before any
+    device work (no GPU needed)."""
+    lib = _capi.load()
+    done = C.c_int(7)
+    assert lib.lg_server_poll(None, 0, C.byref(done)) == _capi.LG_ERR_INVALID
+    assert done.value == 7
+    assert lib.lg_server_wait(None, 0, 0, None, None, None) == _capi.LG_ERR_INVALID
+    tk = C.c_int64()
+    assert lib.lg_server_submit(None, None, C.byref(tk)) == _capi.LG_ERR_INVALID
+    assert lib.lg_server_destroy(None) in (_capi.LG_OK, _capi.LG_ERR_INVALID)
+
+
 def test_shader_defaults_and_coefficients():
     s = Shader()
     c = s.to_c()

@@ -51,6 +51,20 @@ def test_budget_admission_and_errors(small_stream):
         # unknown ticket
         with pytest.raises(LightGraphError):
             srv.wait(123456, 0)
+        with pytest.raises(LightGraphError):
+            srv.poll(123456)
+        # poll does not consume the result: a finished request polls done
+        # until it is waited for, and is unknown after
+        tk = srv.submit(stream[0][1])
+        for _ in range(20000):
+            if srv.poll(tk):
+                break
+            __import__("time").sleep(0.001)
+        assert srv.poll(tk)
+        img, _, _ = srv.wait(tk, 0)
+        assert np.array_equal(img, imgs[0])
+        with pytest.raises(LightGraphError):
+            srv.poll(tk)
         # a request larger than the whole budget is refused up front
         big = serve.request_stream(vs, 1, rate=0, seed=1, n_min=3000, n_max=3000, images=(1024,))[0][1]
         with pytest.raises(LightGraphError) as e:
