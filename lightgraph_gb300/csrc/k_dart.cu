@@ -12,8 +12,9 @@
 //
 // Here one CTA runs one iteration and reproduces that sequence exactly. It
 // takes the candidates a block of 208 at a time (208 x 3 = 624 draws: one
-// MT19937 state block, renewed with one barrier: word i >= 227 depends only
-// on word i - 227, so 227 threads each compute a chain of up to three words):
+// MT19937 state block; word i >= 227 depends only on word i - 227, so 227
+// threads each compute a chain of up to three words, while warp 0 walks the
+// previous block), with three barriers per block:
 //   1. every thread of a candidate computes its position and its density in
 //      FP32, re-tested with the reference's sampler arithmetic (float voxel
 //      values, double weights, a float result per interpolation step) when
@@ -112,6 +113,27 @@ __device__ __forceinline__ bool closer(const float* a, const float* b, float m2)
     return e2 < (double)m2;
 }
 
+// One MT19937 state block: new[i] = f(old[i], old[i+1], x) with x =
+// old[i+397] for i < 227 and new[i-227] after, i = 623 taking new[0] as its
+// next. Word i >= 227 depends only on word i - 227, so thread t < 227
+// computes the chain t, t + 227, t + 454 alone; word 623 (from new[0] and
+// new[396]) is left to the one thread that uses it. t >= 227 does nothing.
+__device__ __forceinline__ void mt_twist_block(const uint32_t* cur, uint32_t* nxt, int t) {
+    if (t < 0 || t >= 227) return;
+    uint32_t x = mt_twist_word(cur[t], cur[t + 1], cur[t + kMtM]);
+    nxt[t] = x;
+    x = mt_twist_word(cur[t + 227], cur[t + 228], x);
+    nxt[t + 227] = x;
+    if (t < 169) nxt[t + 454] = mt_twist_word(cur[t + 454], cur[t + 455], x);
+}
+
+// The reference's radius update: minDist^2 *= pcSize / expectedSize, in
+// double, rounded back to float.
+__device__ __forceinline__ void radius_update(float& m2, int pc, uint32_t expected) {
+    const double ratio = (double)pc / (double)expected;
+    m2 = __double2float_rn(__dmul_rn((double)m2, ratio));
+}
+
 __global__ void __launch_bounds__(kDartThreads, 4) k_dart(DevGrid g, DartParams prm, const uint32_t* __restrict__ expected,
                                                           float* __restrict__ out_pts, int32_t* __restrict__ out_count,
                                                           float* __restrict__ out_last_m2) {
@@ -139,30 +161,22 @@ __global__ void __launch_bounds__(kDartThreads, 4) k_dart(DevGrid g, DartParams 
     __syncthreads();
     uint32_t* cur = mt_a;
     uint32_t* nxt = mt_b;
+    mt_twist_block(cur, nxt, tid);
+    __syncthreads();
     for (uint32_t base = 0; base < prm.scatter_count; base += kDartBlock) {
         if (s_done) break;
-        // 1a. twist: new[i] = f(old[i], old[i+1], x) with x = old[i+397] for
-        // i < 227 and new[i-227] after, i = 623 taking new[0] as its next.
-        // Word i >= 227 depends only on word i - 227, so thread t computes
-        // the chain t, t + 227, t + 454 alone; word 623 (from new[0] and
-        // new[396]) is computed by the one thread that uses it, in 1b.
-        if (tid < 227) {
-            uint32_t x = mt_twist_word(cur[tid], cur[tid + 1], cur[tid + kMtM]);
-            nxt[tid] = x;
-            x = mt_twist_word(cur[tid + 227], cur[tid + 228], x);
-            nxt[tid + 227] = x;
-            if (tid < 169) nxt[tid + 454] = mt_twist_word(cur[tid + 454], cur[tid + 455], x);
-        }
-        __syncthreads();
+        // the block's words (twisted during the previous walk) become current
         {
             uint32_t* t = cur;
             cur = nxt;
             nxt = t;
         }
-        // 1b. positions and densities of this block's candidates
+        // 1. positions and densities of this block's candidates; a radius
+        // update at the block's first candidate is applied alongside by an
+        // idle thread (the accepted count is final: the last walk is done)
         if (tid < kDartBlock) {
             // the last word of the block (read only by this candidate, and by
-            // the next twist after several barriers)
+            // the next twist after a barrier)
             if (tid == kDartBlock - 1) cur[kMtN - 1] = mt_twist_word(nxt[kMtN - 1], cur[0], cur[396]);
             const uint32_t n = base + (uint32_t)tid;
             bool ok = false;
@@ -178,10 +192,13 @@ __global__ void __launch_bounds__(kDartThreads, 4) k_dart(DevGrid g, DartParams 
                 ok = density_passes(g, p, prm);
             }
             dens_ok[tid] = ok;
+        } else if (tid == kDartThreads - 1 && (base + 1u) % prm.batch == 0u) {
+            radius_update(s_m2, s_pc, expected[base / prm.batch]);
         }
         __syncthreads();
         // 2-3. segments between radius updates (candidate n updates before
-        // its tests when (n + 1) % batch == 0)
+        // its tests when (n + 1) % batch == 0): one per block but for the
+        // blocks that hold a radius update past their first candidate
         int j0 = 0;
         const int jend = (int)min((uint32_t)kDartBlock, prm.scatter_count - base);
         while (j0 < jend && !s_done) {
@@ -190,12 +207,11 @@ __global__ void __launch_bounds__(kDartThreads, 4) k_dart(DevGrid g, DartParams 
             const uint32_t m = base + (uint32_t)j0 + 1u;
             const uint64_t nb = ((uint64_t)(m + 1u) + prm.batch - 1u) / prm.batch * prm.batch - 1u;
             const int j1 = (int)min((uint64_t)jend, nb - base);
-            // the update belongs to candidate j0 when it is a boundary
-            if (tid == 0 && (base + (uint32_t)j0 + 1u) % prm.batch == 0u) {
-                const double ratio = (double)s_pc / (double)expected[(base + j0) / prm.batch];
-                s_m2 = __double2float_rn(__dmul_rn((double)s_m2, ratio));
+            if (j0 > 0) {
+                // the update belongs to candidate j0, a boundary
+                if (tid == 0) radius_update(s_m2, s_pc, expected[(base + j0) / prm.batch]);
+                __syncthreads();
             }
-            __syncthreads();
             const int p0 = s_pc;
             const float m2 = s_m2;
             // 2. survivors of the points accepted before the segment
@@ -211,16 +227,19 @@ __global__ void __launch_bounds__(kDartThreads, 4) k_dart(DevGrid g, DartParams 
                 if (lane == 0) hit[j] = h;
             }
             __syncthreads();
-            // 3. walk the survivors in order (warp 0; lane 0 accepts)
+            // 3. walk the survivors in order (warp 0; lane 0 accepts); after
+            // the block's last segment, warps 1-8 twist the next block's
+            // words meanwhile (they read this block's words, which the walk
+            // does not touch, and overwrite the previous block's)
             if (warp == 0) {
                 for (int c0 = j0; c0 < j1; c0 += 32) {
                     const int j = c0 + lane;
                     const unsigned live = __ballot_sync(0xffffffffu, j < j1 && dens_ok[j] && !hit[j]);
                     if (lane == 0) {
-                        unsigned m = live;
-                        while (m && !s_done) {
-                            const int jj = c0 + __ffs(m) - 1;
-                            m &= m - 1;
+                        unsigned mk = live;
+                        while (mk && !s_done) {
+                            const int jj = c0 + __ffs(mk) - 1;
+                            mk &= mk - 1;
                             bool h = false;
                             for (int q = p0; q < s_pc && !h; ++q) h = closer(cand[jj], acc_pts + 3 * q, m2);
                             if (h) continue;
@@ -237,6 +256,8 @@ __global__ void __launch_bounds__(kDartThreads, 4) k_dart(DevGrid g, DartParams 
                     }
                     __syncwarp();
                 }
+            } else if (j1 == jend) {
+                mt_twist_block(cur, nxt, tid - 32);
             }
             __syncthreads();
             j0 = j1;
