@@ -3,7 +3,7 @@ autotuner, and frame replay through a captured CUDA graph."""
 import numpy as np
 import pytest
 
-from lightgraph_gb300 import scenes
+from lightgraph_gb300 import LightGraphError, _capi, scenes
 from oracle import pyoracle as po
 
 pytestmark = pytest.mark.gpu
@@ -55,6 +55,19 @@ def test_schedules_bit_identical_and_match_oracle(gpu_ctx, uneven_graphs):
         fin = np.isfinite(ref)
         assert np.array_equal(np.isfinite(d0[g]), fin)
         assert np.allclose(d0[g][fin], ref[fin], rtol=1e-6, atol=0), g
+
+
+def test_fw_schedule_range(gpu_ctx, uneven_graphs):
+    """Schedules -1..5 are accepted; anything else is LG_ERR_INVALID and
+    leaves the schedule in force."""
+    _, _, used, _ = solve_with(gpu_ctx, uneven_graphs, 5)
+    assert used == 5
+    for bad in (-2, 6):
+        with pytest.raises(LightGraphError) as e:
+            gpu_ctx.set_fw_schedule(bad)
+        assert e.value.status == _capi.LG_ERR_INVALID
+        assert gpu_ctx.fw_schedule()[0] == 5
+    gpu_ctx.set_fw_schedule(-1)
 
 
 def test_autotuner_picks_a_schedule(gpu_ctx, uneven_graphs):
