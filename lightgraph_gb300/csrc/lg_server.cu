@@ -40,6 +40,17 @@ struct Volume {
     Ctx* owner = nullptr;  // context that uploaded the grids
 };
 
+// Every device buffer a DevGrid points into (cell records, leaf bitmap)
+// passes from the upload context to the volume, whose copy of the DevGrid
+// keeps pointing at them.
+void take_buffers(GridStore& to, GridStore& from) {
+    DevBuf* const pairs[2][2] = {{&to.bricks, &from.bricks}, {&to.bits, &from.bits}};
+    for (auto& pr : pairs) {
+        std::swap(pr[0]->p, pr[1]->p);
+        std::swap(pr[0]->bytes, pr[1]->bytes);
+    }
+}
+
 struct Request {
     int64_t ticket = 0;
     lg_request r{};
@@ -241,10 +252,7 @@ extern "C" lg_status lg_server_add_volume(lg_server* srv, const lg_grid_desc* de
     lg_status st = c.upload_grid(LG_GRID_DENSITY, density, density_values, storage_dtype);
     if (st != LG_OK) { srv->err = c.err; return st; }
     // move the uploaded stores into the volume (the buffers change owner)
-    std::swap(v->dens.bricks.p, c.dens.bricks.p);
-    std::swap(v->dens.bricks.bytes, c.dens.bricks.bytes);
-    std::swap(v->dens.bits.p, c.dens.bits.p);
-    std::swap(v->dens.bits.bytes, c.dens.bits.bytes);
+    take_buffers(v->dens, c.dens);
     v->dens.g = c.dens.g;
     v->dens.desc = c.dens.desc;
     std::copy(c.dens.vbbox, c.dens.vbbox + 6, v->dens.vbbox);
@@ -255,10 +263,7 @@ extern "C" lg_status lg_server_add_volume(lg_server* srv, const lg_grid_desc* de
     if (temperature && temperature_values) {
         st = c.upload_grid(LG_GRID_TEMPERATURE, temperature, temperature_values, storage_dtype);
         if (st != LG_OK) { srv->err = c.err; return st; }
-        std::swap(v->temp.bricks.p, c.temp.bricks.p);
-        std::swap(v->temp.bricks.bytes, c.temp.bricks.bytes);
-        std::swap(v->temp.bits.p, c.temp.bits.p);
-        std::swap(v->temp.bits.bytes, c.temp.bits.bytes);
+        take_buffers(v->temp, c.temp);
         v->temp.g = c.temp.g;
         v->temp.desc = c.temp.desc;
         v->temp.valid = true;
