@@ -166,6 +166,18 @@ def run_batched_graphs(local: int):
     torch.cuda.synchronize()
     lib.lg_set_profiling(ctx.h, 0)
     stage /= reps
+    # the same frame captured once as a CUDA graph and replayed
+    ctx.set_graph_mode(True)
+    for _ in range(2):  # run + capture, then a replay
+        lib.lg_frame_device(ctx.h, sc.max_connect, C.c_double(0.0), C.byref(sc.opts.camera_c()))
+    torch.cuda.synchronize()
+    ev2, ev3 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev2.record(stream)
+    for _ in range(reps):
+        lib.lg_frame_device(ctx.h, sc.max_connect, C.c_double(0.0), C.byref(sc.opts.camera_c()))
+    ev3.record(stream)
+    torch.cuda.synchronize()
+    ctx.set_graph_mode(False)
     sched, tuned = ctx.fw_schedule()
     lds = [(len(p) + 127) // 128 * 128 for p in sc.points]
     flops = sum(2.0 * ld ** 3 for ld in lds)
@@ -174,11 +186,13 @@ def run_batched_graphs(local: int):
                        "256^2 at 1 spp", "points": int(sum(len(p) for p in sc.points)),
            "sizes": [int(min(len(p) for p in sc.points)), int(max(len(p) for p in sc.points))],
            "frame_ms": ev0.elapsed_time(ev1) / reps,
+           "frame_ms_graph_replay": ev2.elapsed_time(ev3) / reps,
            "stages_ms": {k: round(float(v), 4) for k, v in zip(STAGES, stage)},
            "fw": {"schedule": FW_SCHEDULES.get(sched, str(sched)),
                   "autotuner_ms": [round(x, 4) for x in tuned], "tflops": flops / (fw_ms * 1e-3) / 1e12,
                   "frac_of_nominal_fp32": flops / (fw_ms * 1e-3) / 1e12 / NOMINAL_FP32_TFLOPS},
-           "timing": "CUDA events on the frame stream, frames through lg_frame_device (graph build to render)"}
+           "timing": "CUDA events on the frame stream, frames through lg_frame_device (graph build to render); "
+                     "frame_ms with per-stage events, frame_ms_graph_replay as one captured CUDA graph"}
     ctx.close()
     return out
 
