@@ -214,12 +214,32 @@ __global__ void k_env_marginal(const float* __restrict__ cond_int, int h, float*
     dist1d_build(marg_func, h, marg_cdf, marg_int);
 }
 
+// Guide table entry g of each of `rows` CDFs of n + 1 values (row stride
+// n + 1): the first index with cdf > g / kEnvGuide, by binary search.
+__global__ void k_env_guide(const float* __restrict__ cdf, int n, int rows, int* __restrict__ guide) {
+    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= (int64_t)rows * (kEnvGuide + 1)) return;
+    const int r = (int)(e / (kEnvGuide + 1)), g = (int)(e % (kEnvGuide + 1));
+    const float x = (float)g / (float)kEnvGuide;  // exact
+    const float* c = cdf + (int64_t)r * (n + 1);
+    int first = 0, len = n + 1;
+    while (len > 0) {
+        const int half = len >> 1, middle = first + half;
+        if (c[middle] <= x) { first = middle + 1; len -= half + 1; }
+        else len = half;
+    }
+    guide[e] = first;
+}
+
 cudaError_t launch_env_cdf(const float* rgb, int w, int h, float* cond_func, float* cond_cdf,
                            float* cond_int, float* marg_func, float* marg_cdf, float* marg_int,
-                           cudaStream_t st) {
+                           int* cond_guide, int* marg_guide, cudaStream_t st) {
     k_env_rows<<<(h + 63) / 64, 64, 0, st>>>(rgb, w, h, cond_func, cond_cdf, cond_int);
     k_env_marginal<<<1, 32, 0, st>>>(cond_int, h, marg_func, marg_cdf, marg_int);
-    g_launch_counter += 2;
+    const int64_t ne = (int64_t)h * (kEnvGuide + 1);
+    k_env_guide<<<(unsigned)((ne + 255) / 256), 256, 0, st>>>(cond_cdf, w, h, cond_guide);
+    k_env_guide<<<(kEnvGuide + 1 + 255) / 256, 256, 0, st>>>(marg_cdf, h, 1, marg_guide);
+    g_launch_counter += 4;
     return cudaGetLastError();
 }
 

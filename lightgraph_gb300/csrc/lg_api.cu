@@ -451,10 +451,13 @@ lg_status Ctx::set_lights(const lg_light* ls, int n, const float* env_rgb, int e
         CK(env_marg_func.reserve(sizeof(float) * h), "env alloc");
         CK(env_marg_cdf.reserve(sizeof(float) * (h + 1)), "env alloc");
         CK(env_marg_int.reserve(sizeof(float) * 4), "env alloc");
+        CK(env_cond_guide.reserve(sizeof(int) * (kEnvGuide + 1) * h), "env alloc");
+        CK(env_marg_guide.reserve(sizeof(int) * (kEnvGuide + 1)), "env alloc");
         CK(cudaMemcpyAsync(env_rgb_d.p, env_rgb, sizeof(float) * w * h * 3, cudaMemcpyHostToDevice, st), "env upload");
         CK(launch_env_cdf(env_rgb_d.as<float>(), env_w, env_h, env_cond_func.as<float>(), env_cond_cdf.as<float>(),
                           env_cond_int.as<float>(), env_marg_func.as<float>(), env_marg_cdf.as<float>(),
-                          env_marg_int.as<float>(), st), "env cdf");
+                          env_marg_int.as<float>(), env_cond_guide.as<int>(), env_marg_guide.as<int>(), st),
+           "env cdf");
         float mi = 0.f;
         CK(cudaMemcpyAsync(&mi, env_marg_int.p, sizeof(float), cudaMemcpyDeviceToHost, st), "env int");
         CK(cudaStreamSynchronize(st), "env sync");
@@ -520,6 +523,8 @@ DevScene Ctx::scene() const {
     if (env_valid) {
         sc.env.rgb = env_rgb_d.as<float>();
         sc.env.cond_cdf = env_cond_cdf.as<float>();
+        sc.env.cond_guide = env_cond_guide.as<int>();
+        sc.env.marg_guide = env_marg_guide.as<int>();
         sc.env.cond_func = env_cond_func.as<float>();
         sc.env.cond_int = env_cond_int.as<float>();
         sc.env.marg_cdf = env_marg_cdf.as<float>();

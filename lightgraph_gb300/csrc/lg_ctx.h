@@ -81,6 +81,7 @@ struct Ctx {
     lg_settings settings{};
     std::vector<lg_light> lights;
     DevBuf env_rgb_d, env_cond_func, env_cond_cdf, env_cond_int, env_marg_func, env_marg_cdf, env_marg_int;
+    DevBuf env_cond_guide, env_marg_guide;  // guide tables of the CDFs (DevEnv)
     float env_marg_int_h = 0.f;
     int env_w_ = 0, env_h_ = 0;
     bool env_valid = false;

@@ -288,8 +288,15 @@ struct DevLight {
     float rot[9];          // env: row-vector rotation
 };
 
+// Guide tables of the environment CDFs: entry g of a table is the first
+// index i with cdf[i] > g / kEnvGuide (std::upper_bound), so the interval of
+// a draw u lies between entries floor(u kEnvGuide) and the next one.
+constexpr int kEnvGuide = 256;  // a power of two: u * kEnvGuide is exact
+
 struct DevEnv {
     const float* rgb = nullptr;        // h x w x 3
+    const int* cond_guide = nullptr;   // h x (kEnvGuide + 1)
+    const int* marg_guide = nullptr;   // kEnvGuide + 1
     const float* cond_cdf = nullptr;   // h x (w + 1)
     const float* cond_func = nullptr;  // h x w
     const float* cond_int = nullptr;   // h
@@ -333,8 +340,11 @@ __device__ __forceinline__ void ramp_color(const DevShader& sh, float temp, floa
 
 // Distribution1D::SampleContinuous (src/Sampling.h:102-119) over a CDF of n+1
 // entries; FindInterval (src/Sampling.h:59-72) is the same bisection.
-__device__ __forceinline__ float sample_1d(const float* cdf, int n, float u, int* off_out) {
-    int first = 0, len = n + 1;
+__device__ __forceinline__ float sample_1d(const float* cdf, const int* guide, int n, float u, int* off_out) {
+    // the upper bound of u among cdf[0..n], searched only between the guide
+    // entries around u (the same index a search of the whole array finds)
+    const int g = min(max((int)(u * (float)kEnvGuide), 0), kEnvGuide - 1);
+    int first = __ldg(guide + g), len = __ldg(guide + g + 1) - first;
     while (len > 0) {
         const int half = len >> 1, middle = first + half;
         if (__ldg(cdf + middle) <= u) { first = middle + 1; len -= half + 1; }
@@ -355,8 +365,9 @@ __device__ __forceinline__ float sample_1d(const float* cdf, int n, float u, int
 __device__ __forceinline__ void env_illuminate(const DevEnv& env, const DevLight& L, float u,
                                                float v, float dir_out[3], float I_out[3]) {
     int row;
-    const float d1 = sample_1d(env.marg_cdf, env.h, v, &row);
-    const float d0 = sample_1d(env.cond_cdf + (int64_t)row * (env.w + 1), env.w, u, nullptr);
+    const float d1 = sample_1d(env.marg_cdf, env.marg_guide, env.h, v, &row);
+    const float d0 = sample_1d(env.cond_cdf + (int64_t)row * (env.w + 1), env.cond_guide + (int64_t)row * (kEnvGuide + 1),
+                               env.w, u, nullptr);
     const float xs = d0 * (float)env.w, ys = d1 * (float)env.h;
     int col_lo = (int)floorf(xs), row_lo = (int)floorf(ys);
     int col_hi = (int)ceilf(xs), row_hi = (int)ceilf(ys);

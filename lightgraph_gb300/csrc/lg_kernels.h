@@ -217,6 +217,7 @@ cudaError_t launch_dart(const DevGrid& g, const DartParams& prm, int n_iter, con
 // Environment map CDFs (FP64 prefix sums)
 cudaError_t launch_env_cdf(const float* rgb, int w, int h, float* cond_func, float* cond_cdf,
                            float* cond_int, float* marg_func, float* marg_cdf, float* marg_int,
+                           int* cond_guide, int* marg_guide,
                            cudaStream_t st);
 
 // Grid upload helpers
