@@ -360,10 +360,12 @@ __global__ void __launch_bounds__(128, 8) k_shadow(DevScene sc, const ShadowTask
     }
 }
 
-// One warp per pixel: for each sample in order, lane l sums the sample's
-// tasks l, l + 32, ... (a task's direct light is the sum of its lights'
-// contributions in light order), a butterfly reduction combines the lanes and
-// lane 0 (whose summation order is fixed) forms the antialiasing averages.
+// One warp per pixel. Its samples run side by side, G lanes each (G a power
+// of two, spp * G <= 32, so 32 / G samples per pass): lane l of a sample's
+// group sums the sample's tasks l, l + G, ... (a task's direct light is the
+// sum of its lights' contributions in light order), a butterfly inside the
+// group combines the lanes, and lane 0 (whose summation order is fixed)
+// takes the samples in order to form the antialiasing averages.
 __global__ void __launch_bounds__(128) k_resolve(DevCamera cam, const int32_t* __restrict__ offsets,
                                                  const int32_t* __restrict__ counts,
                                                  const PixelSample* __restrict__ pss,
@@ -373,37 +375,51 @@ __global__ void __launch_bounds__(128) k_resolve(DevCamera cam, const int32_t* _
     const int64_t pix = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (pix >= (int64_t)cam.width * cam.height) return;  // uniform across the warp
-    const float ratio = 1.f / (float)cam.spp;
+    const int spp = cam.spp;
+    int G = 32;
+    while (G > 1 && G * spp > 32) G >>= 1;
+    const int per_pass = 32 / G, gl = lane & (G - 1);
+    const float ratio = 1.f / (float)spp;
     float tAA[3] = {0.f, 0.f, 0.f}, lAA[3] = {0.f, 0.f, 0.f}, dAA[3] = {0.f, 0.f, 0.f};
     float sAA[3] = {0.f, 0.f, 0.f}, eAA[3] = {0.f, 0.f, 0.f};
-    for (int s = 0; s < cam.spp; ++s) {
-        const int64_t ps = pix * cam.spp + s;
-        const PixelSample o = pss[ps];
+    for (int s0 = 0; s0 < spp; s0 += per_pass) {
+        const int s = s0 + lane / G;
         float d[3] = {0.f, 0.f, 0.f};
-        const int64_t b = offsets[ps], e = min((int64_t)b + counts[ps], task_cap);
-        for (int64_t t = b + lane; t < e; t += 32) {
-            float acc[3] = {0.f, 0.f, 0.f};
-            for (int k = 0; k < n_lights; ++k) {
-                const float4 v = direct[(int64_t)k * task_cap + t];
-                acc[0] += v.x;
-                acc[1] += v.y;
-                acc[2] += v.z;
+        if (s < spp) {
+            const int64_t ps = pix * spp + s;
+            const int64_t b = offsets[ps], e = min((int64_t)b + counts[ps], task_cap);
+            for (int64_t t = b + gl; t < e; t += G) {
+                float acc[3] = {0.f, 0.f, 0.f};
+                for (int k = 0; k < n_lights; ++k) {
+                    const float4 v = direct[(int64_t)k * task_cap + t];
+                    acc[0] += v.x;
+                    acc[1] += v.y;
+                    acc[2] += v.z;
+                }
+                d[0] += acc[0];
+                d[1] += acc[1];
+                d[2] += acc[2];
             }
-            d[0] += acc[0];
-            d[1] += acc[1];
-            d[2] += acc[2];
         }
-#pragma unroll
-        for (int off = 16; off > 0; off >>= 1)
+        for (int off = G >> 1; off > 0; off >>= 1)
 #pragma unroll
             for (int c = 0; c < 3; ++c) d[c] += __shfl_xor_sync(0xffffffffu, d[c], off);
+        const int ns = min(per_pass, spp - s0);
+        for (int jj = 0; jj < ns; ++jj) {
+            float dj[3];
 #pragma unroll
-        for (int c = 0; c < 3; ++c) {
-            lAA[c] += (d[c] + o.scat[c] + o.emis[c]) * ratio;
-            dAA[c] += d[c] * ratio;
-            sAA[c] += o.scat[c] * ratio;
-            eAA[c] += o.emis[c] * ratio;
-            tAA[c] += o.trans[c] * ratio;
+            for (int c = 0; c < 3; ++c) dj[c] = __shfl_sync(0xffffffffu, d[c], jj * G);
+            if (lane == 0) {
+                const PixelSample o = pss[pix * spp + s0 + jj];
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    lAA[c] += (dj[c] + o.scat[c] + o.emis[c]) * ratio;
+                    dAA[c] += dj[c] * ratio;
+                    sAA[c] += o.scat[c] * ratio;
+                    eAA[c] += o.emis[c] * ratio;
+                    tAA[c] += o.trans[c] * ratio;
+                }
+            }
         }
     }
     if (lane != 0) return;
