@@ -275,7 +275,9 @@ cudaError_t launch_ray_bins(const ShadowTask* tasks, const int32_t* total, int64
 
 // One thread per (light k, ordered slot r): the shadow rays of light k (all
 // its samples) from task kRayUnit * order[k * n_units + r / kRayUnit] +
-// r % kRayUnit. The threads in flight march neighbouring rays.
+// r % kRayUnit; warps claim 32 consecutive (light, slot) pairs at a time from
+// ctr[2] (zero at launch), so the lanes of a warp march neighbouring rays.
+// ctr[1] accumulates the shadow samples.
 // direct[k * task_cap + t] = albedo * (sum_ls I * T / ns) * w.
 // kEnv = false leaves the environment-light branch out (no light of the
 // scene is an environment light), which frees registers for occupancy.
@@ -292,10 +294,23 @@ __global__ void __launch_bounds__(128, 8) k_shadow(DevScene sc, const ShadowTask
     const float step1 = sc.step1, cutoff = sc.cutoff;
     const float scale = sh.dS * sh.shadowDS;
     uint32_t n_shadow = 0;
-    const uint64_t first = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x, stride = (uint64_t)gridDim.x * blockDim.x;
-    // lights in the outer loop: the (light, ray) index needs no 64-bit division
-    for (int k = 0; k < sc.n_lights; ++k)
-    for (uint64_t rr = first; rr < per_light; rr += stride) {
+    // each warp claims the next 32 (light, ordered slot) pairs, lights in
+    // order, until none are left: the warps stay busy to the end whatever
+    // the rays cost (every ray's result goes to its own slot)
+    const uint64_t n_slots = (uint64_t)sc.n_lights * per_light;
+    const int lane = threadIdx.x & 31;
+    for (;;) {
+        unsigned long long base = 0;
+        if (lane == 0) base = atomicAdd(ctr + 2, 32ull);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= n_slots) break;
+        if (base + lane >= n_slots) continue;
+        int k = 0;
+        uint64_t rr = base + lane;
+        while (rr >= per_light) {
+            rr -= per_light;
+            ++k;
+        }
         const int64_t t = (int64_t)order[k * n_units + rr / kRayUnit] * kRayUnit + (int64_t)(rr % kRayUnit);
         if (t >= total) continue;
         const ShadowTask tk = tasks[t];
@@ -352,7 +367,7 @@ __global__ void __launch_bounds__(128, 8) k_shadow(DevScene sc, const ShadowTask
         for (int c = 0; c < 3; ++c) o[c] = sh.albedo[c] * (lum[c] * inv_ns) * tk.w[c];
         direct[(int64_t)k * task_cap + t] = make_float4(o[0], o[1], o[2], 0.f);
     }
-    if (ctr) {
+    {
         unsigned long long q = n_shadow;
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) q += __shfl_xor_sync(0xffffffffu, q, o);

@@ -1388,8 +1388,9 @@ lg_status Ctx::render(const lg_camera* c) {
     if (!D().valid) return fail(LG_ERR_STATE, "no density grid uploaded");
     const int64_t np = (int64_t)c->width * c->height;
     for (DevBuf* b : {&d_rgba, &d_direct, &d_scatter, &d_emission}) CK(b->reserve(sizeof(float4) * np), "film alloc");
-    CK(d_counters.reserve(2 * sizeof(unsigned long long)), "counter alloc");
-    CK(cudaMemsetAsync(d_counters.p, 0, 2 * sizeof(unsigned long long), st), "counter clear");
+    // primary samples, shadow samples, the shadow wave's claim counter
+    CK(d_counters.reserve(3 * sizeof(unsigned long long)), "counter alloc");
+    CK(cudaMemsetAsync(d_counters.p, 0, 3 * sizeof(unsigned long long), st), "counter clear");
     DevScatterGrid sg{};
     if (splat_done) {
         sg.v = d_sg.as<float4>();
