@@ -72,12 +72,15 @@ __device__ __forceinline__ bool primary_ray(const DevScene& sc, const DevCamera&
     const float jx = draw(stream, kTagJitterX), jy = draw(stream, kTagJitterY);
     const float sx = (2.f * ((float)i + jx) / (float)cam.width - 1.f) * cam.sw;
     const float sy = (1.f - 2.f * ((float)j + jy) / (float)cam.height) * cam.sh;
+    // rounding spelled out: the count and shading passes must trace the same
+    // rays
     float d[3];
 #pragma unroll
-    for (int c = 0; c < 3; ++c) d[c] = sx * cam.m[c] + sy * cam.m[3 + c] - cam.m[6 + c];
-    const float invl = rsqrtf(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+    for (int c = 0; c < 3; ++c) d[c] = __fsub_rn(__fmaf_rn(sx, cam.m[c], __fmul_rn(sy, cam.m[3 + c])), cam.m[6 + c]);
+    const float invl = rsqrtf(__fmaf_rn(d[0], d[0], __fmaf_rn(d[1], d[1], __fmul_rn(d[2], d[2]))));
     d[0] *= invl; d[1] *= invl; d[2] *= invl;
-    const float tscale = 1.f / (d[0] * cam.cdir[0] + d[1] * cam.cdir[1] + d[2] * cam.cdir[2]);
+    const float tscale =
+        1.f / __fmaf_rn(d[0], cam.cdir[0], __fmaf_rn(d[1], cam.cdir[1], __fmul_rn(d[2], cam.cdir[2])));
     make_iray(pr, (cam.eye[0] - G.wo[0]) * G.inv_h, (cam.eye[1] - G.wo[1]) * G.inv_h,
               (cam.eye[2] - G.wo[2]) * G.inv_h, d[0], d[1], d[2], cam.znear * tscale * G.inv_h,
               cam.zfar * tscale * G.inv_h);
@@ -89,90 +92,118 @@ struct PixelSample {
     float scat[3], emis[3], trans[3];
 };
 
-// One thread per pixel-sample ps = pixel * spp + s. kWrite = false only
-// counts the shading samples; kWrite = true accumulates the scatter and
-// emission AOVs and writes the shadow tasks at offsets[ps].
+// One pixel sample ps = pixel * spp + s of the primary wave. kWrite = false
+// only counts the shading samples (counts[ps]); kWrite = true accumulates the
+// scatter and emission AOVs and writes the shadow tasks at offsets[ps]. The
+// two passes must agree on every sample, so the arithmetic that decides
+// which samples shade (positions, transmittance, termination, step jitter)
+// is spelled out rounding by rounding (no contraction left to the compiler).
+// Returns the primary samples taken.
+template <bool kWrite, int DT>
+__device__ __forceinline__ uint32_t primary_sample(const DevScene& sc, const DevCamera& cam, const DevScatterGrid& sg,
+                                                   int64_t ps, int32_t* __restrict__ counts,
+                                                   const int32_t* __restrict__ offsets, ShadowTask* __restrict__ tasks,
+                                                   int64_t task_cap, PixelSample* __restrict__ out) {
+    uint32_t n_primary = 0;
+    const int64_t pix = ps / cam.spp;
+    const int i = (int)(pix % cam.width), j = (int)(pix / cam.width);
+    const DevGrid& G = sc.dens;
+    const DevShader& sh = sc.sh;
+    const Stream stream = make_stream(sc.seed, kDomainPixel | (uint64_t)ps);
+    const float step0 = sc.step0, cutoff = sc.cutoff;
+    float pT3[3] = {1.f, 1.f, 1.f}, sL[3] = {0.f, 0.f, 0.f}, eL[3] = {0.f, 0.f, 0.f};
+    int32_t shading = 0;
+    IRay pr;
+    if (primary_ray(sc, cam, i, j, stream, pr)) {
+        LeafDDA dda;
+        dda_init(dda, pr, G);
+        float ta, tb;
+        uint32_t span_ord = 0, n_iter = 0;
+        bool pdrop = false;
+        int64_t base = kWrite ? offsets[ps] : 0;
+        while (!pdrop && next_span(G, dda, ta, tb)) {
+            float pStep = jitter_step(step0, draw(stream, kTagPrimarySpan | span_ord));
+            ++span_ord;
+            // (pT + pStep > pT stops a march whose step underflows against pT)
+            for (float pT = step0 * ceilf(ta / step0); pT <= tb && pT + pStep > pT;) {
+                const uint32_t n = n_iter++;
+                ++n_primary;
+                const float p[3] = {__fmaf_rn(pT, pr.d[0], pr.e[0]), __fmaf_rn(pT, pr.d[1], pr.e[1]),
+                                    __fmaf_rn(pT, pr.d[2], pr.e[2])};
+                const float rho = fminf(sample_index_t<DT>(G, p[0], p[1], p[2]) * sh.dS, sh.dMax);
+                if (rho < cutoff) { pT += pStep; continue; }
+                float omdT[3], dT[3];
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    const float e1 = expm1f(-sh.a[c] * rho * pStep);
+                    dT[c] = 1.f + e1;
+                    omdT[c] = -e1;
+                }
+                if (kWrite) {
+                    const float pw[3] = {p[0] * G.h + G.wo[0], p[1] * G.h + G.wo[1], p[2] * G.h + G.wo[2]};
+                    float sgv[3], em[3];
+                    sample_scatter(sg, pw[0], pw[1], pw[2], sgv);
+                    const float mask = powf(fminf(fmaxf(rho, 0.f), 1.f), sh.mask_power) * sh.scatter_scale;
+                    const float temp = sc.has_temp ? sample_world(sc.temp, pw[0], pw[1], pw[2]) : 0.f;
+                    ramp_color(sh, temp, em);
+                    const int64_t t = base + shading;
+                    if (t < task_cap) {
+                        ShadowTask tk;
+                        tk.p[0] = p[0]; tk.p[1] = p[1]; tk.p[2] = p[2];
+#pragma unroll
+                        for (int c = 0; c < 3; ++c) tk.w[c] = pT3[c] * omdT[c];
+                        tk.sa = stream.a;
+                        tk.iw = shadow_iter_word(stream, n);
+                        tasks[t] = tk;
+                    }
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) {
+                        sL[c] += sgv[c] * sh.inv_scatter[c] * mask * pT3[c] * omdT[c];
+                        eL[c] += em[c] * sh.emission_scale * pT3[c] * omdT[c];
+                    }
+                }
+                ++shading;
+#pragma unroll
+                for (int c = 0; c < 3; ++c) pT3[c] *= dT[c];
+                if (__fmaf_rn(pT3[0], pT3[0], __fmaf_rn(pT3[1], pT3[1], __fmul_rn(pT3[2], pT3[2]))) < cutoff) {
+                    pdrop = true;
+                    break;
+                }
+                pStep = jitter_step(step0, draw(stream, kTagPrimaryStep | n));
+                pT += pStep;
+            }
+        }
+    }
+    if (!kWrite) counts[ps] = shading;
+    if (kWrite) {
+        PixelSample o;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) { o.scat[c] = sL[c]; o.emis[c] = eL[c]; o.trans[c] = pT3[c]; }
+        out[ps] = o;
+    }
+    return n_primary;
+}
+
+// Warps claim 32 consecutive pixel samples at a time from *claim (zero at
+// launch) until none are left: a persistent grid in which no warp slot waits
+// on another warp's long ray.
 template <bool kWrite, int DT>
 __global__ void __launch_bounds__(128, 6) k_primary(DevScene sc, DevCamera cam, DevScatterGrid sg,
                                                  int32_t* __restrict__ counts, const int32_t* __restrict__ offsets,
                                                  ShadowTask* __restrict__ tasks, int64_t task_cap,
-                                                 PixelSample* __restrict__ out, unsigned long long* __restrict__ ctr) {
-    const int64_t ps = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+                                                 PixelSample* __restrict__ out, unsigned long long* __restrict__ ctr,
+                                                 unsigned long long* __restrict__ claim) {
     const int64_t n_ps = (int64_t)cam.width * cam.height * cam.spp;
+    const int lane = threadIdx.x & 31;
     uint32_t n_primary = 0;
-    if (ps < n_ps) {
-        const int64_t pix = ps / cam.spp;
-        const int i = (int)(pix % cam.width), j = (int)(pix / cam.width);
-        const DevGrid& G = sc.dens;
-        const DevShader& sh = sc.sh;
-        const Stream stream = make_stream(sc.seed, kDomainPixel | (uint64_t)ps);
-        const float step0 = sc.step0, cutoff = sc.cutoff;
-        float pT3[3] = {1.f, 1.f, 1.f}, sL[3] = {0.f, 0.f, 0.f}, eL[3] = {0.f, 0.f, 0.f};
-        int32_t shading = 0;
-        IRay pr;
-        if (primary_ray(sc, cam, i, j, stream, pr)) {
-            LeafDDA dda;
-            dda_init(dda, pr, G);
-            float ta, tb;
-            uint32_t span_ord = 0, n_iter = 0;
-            bool pdrop = false;
-            int64_t base = kWrite ? offsets[ps] : 0;
-            while (!pdrop && next_span(G, dda, ta, tb)) {
-                float pStep = jitter_step(step0, draw(stream, kTagPrimarySpan | span_ord));
-                ++span_ord;
-                // (pT + pStep > pT stops a march whose step underflows against pT)
-                for (float pT = step0 * ceilf(ta / step0); pT <= tb && pT + pStep > pT;) {
-                    const uint32_t n = n_iter++;
-                    ++n_primary;
-                    const float p[3] = {pr.e[0] + pT * pr.d[0], pr.e[1] + pT * pr.d[1], pr.e[2] + pT * pr.d[2]};
-                    const float rho = fminf(sample_index_t<DT>(G, p[0], p[1], p[2]) * sh.dS, sh.dMax);
-                    if (rho < cutoff) { pT += pStep; continue; }
-                    float omdT[3], dT[3];
-#pragma unroll
-                    for (int c = 0; c < 3; ++c) {
-                        const float e1 = expm1f(-sh.a[c] * rho * pStep);
-                        dT[c] = 1.f + e1;
-                        omdT[c] = -e1;
-                    }
-                    if (kWrite) {
-                        const float pw[3] = {p[0] * G.h + G.wo[0], p[1] * G.h + G.wo[1], p[2] * G.h + G.wo[2]};
-                        float sgv[3], em[3];
-                        sample_scatter(sg, pw[0], pw[1], pw[2], sgv);
-                        const float mask = powf(fminf(fmaxf(rho, 0.f), 1.f), sh.mask_power) * sh.scatter_scale;
-                        const float temp = sc.has_temp ? sample_world(sc.temp, pw[0], pw[1], pw[2]) : 0.f;
-                        ramp_color(sh, temp, em);
-                        const int64_t t = base + shading;
-                        if (t < task_cap) {
-                            ShadowTask tk;
-                            tk.p[0] = p[0]; tk.p[1] = p[1]; tk.p[2] = p[2];
-#pragma unroll
-                            for (int c = 0; c < 3; ++c) tk.w[c] = pT3[c] * omdT[c];
-                            tk.sa = stream.a;
-                            tk.iw = shadow_iter_word(stream, n);
-                            tasks[t] = tk;
-                        }
-#pragma unroll
-                        for (int c = 0; c < 3; ++c) {
-                            sL[c] += sgv[c] * sh.inv_scatter[c] * mask * pT3[c] * omdT[c];
-                            eL[c] += em[c] * sh.emission_scale * pT3[c] * omdT[c];
-                        }
-                    }
-                    ++shading;
-#pragma unroll
-                    for (int c = 0; c < 3; ++c) pT3[c] *= dT[c];
-                    if (pT3[0] * pT3[0] + pT3[1] * pT3[1] + pT3[2] * pT3[2] < cutoff) { pdrop = true; break; }
-                    pStep = jitter_step(step0, draw(stream, kTagPrimaryStep | n));
-                    pT += pStep;
-                }
-            }
-        }
-        if (!kWrite) counts[ps] = shading;
-        if (kWrite) {
-            PixelSample o;
-#pragma unroll
-            for (int c = 0; c < 3; ++c) { o.scat[c] = sL[c]; o.emis[c] = eL[c]; o.trans[c] = pT3[c]; }
-            out[ps] = o;
-        }
+    for (;;) {
+        unsigned long long claimed = 0;
+        if (lane == 0) claimed = atomicAdd(claim, 32ull);
+        claimed = __shfl_sync(0xffffffffu, claimed, 0);
+        if ((int64_t)claimed >= n_ps) break;
+        const int64_t ps = (int64_t)claimed + lane;
+        if (ps < n_ps)
+            n_primary += primary_sample<kWrite, DT>(sc, cam, sg, ps, counts, offsets, tasks, task_cap, out);
     }
     if (kWrite && ctr) {
         unsigned long long q = n_primary;
@@ -444,17 +475,38 @@ __global__ void __launch_bounds__(128) k_resolve(DevCamera cam, const int32_t* _
     if (efilm) efilm[pix] = make_float4(eAA[0], eAA[1], eAA[2], 0.f);
 }
 
+// Resident 128-thread CTAs per SM of the k_primary instance (kWrite, dtype).
+static int primary_ctas_per_sm(bool write, int dtype) {
+    static int cache[2][3] = {{0, 0, 0}, {0, 0, 0}};
+    int& n = cache[write ? 1 : 0][dtype];
+    if (n == 0) {
+        cudaError_t e;
+        if (write)
+            e = dtype == 1   ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_primary<true, 1>, 128, 0)
+                : dtype == 2 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_primary<true, 2>, 128, 0)
+                             : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_primary<true, 0>, 128, 0);
+        else
+            e = dtype == 1   ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_primary<false, 1>, 128, 0)
+                : dtype == 2 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_primary<false, 2>, 128, 0)
+                             : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_primary<false, 0>, 128, 0);
+        if (e != cudaSuccess || n < 1) n = 1;
+    }
+    return n;
+}
+
 cudaError_t launch_render_count(const DevScene& sc, const DevCamera& cam, const DevScatterGrid& sg, int32_t* counts,
-                                cudaStream_t st) {
+                                unsigned long long* claim, int sms, cudaStream_t st) {
     const int64_t n_ps = (int64_t)cam.width * cam.height * cam.spp;
     if (n_ps == 0) return cudaSuccess;
-    const unsigned blocks = (unsigned)((n_ps + 127) / 128);
+    // one resident wave, at most one warp per 32 pixel samples
+    const unsigned blocks = (unsigned)std::min<int64_t>((n_ps + 127) / 128,
+                                                        (int64_t)sms * primary_ctas_per_sm(false, sc.dens.dtype));
     if (sc.dens.dtype == 1)
-        k_primary<false, 1><<<blocks, 128, 0, st>>>(sc, cam, sg, counts, nullptr, nullptr, 0, nullptr, nullptr);
+        k_primary<false, 1><<<blocks, 128, 0, st>>>(sc, cam, sg, counts, nullptr, nullptr, 0, nullptr, nullptr, claim);
     else if (sc.dens.dtype == 2)
-        k_primary<false, 2><<<blocks, 128, 0, st>>>(sc, cam, sg, counts, nullptr, nullptr, 0, nullptr, nullptr);
+        k_primary<false, 2><<<blocks, 128, 0, st>>>(sc, cam, sg, counts, nullptr, nullptr, 0, nullptr, nullptr, claim);
     else
-        k_primary<false, 0><<<blocks, 128, 0, st>>>(sc, cam, sg, counts, nullptr, nullptr, 0, nullptr, nullptr);
+        k_primary<false, 0><<<blocks, 128, 0, st>>>(sc, cam, sg, counts, nullptr, nullptr, 0, nullptr, nullptr, claim);
     ++g_launch_counter;
     return cudaGetLastError();
 }
@@ -491,17 +543,21 @@ cudaError_t launch_render_shade(const DevScene& sc, const DevCamera& cam, const 
     const int64_t n_pix = (int64_t)cam.width * cam.height;
     if (n_ps == 0) return cudaSuccess;
     PixelSample* pss = reinterpret_cast<PixelSample*>(pixel_samples);
-    const unsigned blocks = (unsigned)((n_ps + 127) / 128);
+    const unsigned blocks = (unsigned)std::min<int64_t>((n_ps + 127) / 128,
+                                                        (int64_t)sms * primary_ctas_per_sm(true, sc.dens.dtype));
     auto mark = [&](int k) {
         if (marks && marks[k]) cudaEventRecord(marks[k], st);
     };
     cudaError_t e;
     if (sc.dens.dtype == 1)
-        k_primary<true, 1><<<blocks, 128, 0, st>>>(sc, cam, sg, nullptr, offsets, tasks, task_cap, pss, counters);
+        k_primary<true, 1><<<blocks, 128, 0, st>>>(sc, cam, sg, nullptr, offsets, tasks, task_cap, pss, counters,
+                                                   counters + 4);
     else if (sc.dens.dtype == 2)
-        k_primary<true, 2><<<blocks, 128, 0, st>>>(sc, cam, sg, nullptr, offsets, tasks, task_cap, pss, counters);
+        k_primary<true, 2><<<blocks, 128, 0, st>>>(sc, cam, sg, nullptr, offsets, tasks, task_cap, pss, counters,
+                                                   counters + 4);
     else
-        k_primary<true, 0><<<blocks, 128, 0, st>>>(sc, cam, sg, nullptr, offsets, tasks, task_cap, pss, counters);
+        k_primary<true, 0><<<blocks, 128, 0, st>>>(sc, cam, sg, nullptr, offsets, tasks, task_cap, pss, counters,
+                                                   counters + 4);
     ++g_launch_counter;
     mark(0);
     // order the shadow rays: count keys, scan, scatter task indices

@@ -1388,9 +1388,10 @@ lg_status Ctx::render(const lg_camera* c) {
     if (!D().valid) return fail(LG_ERR_STATE, "no density grid uploaded");
     const int64_t np = (int64_t)c->width * c->height;
     for (DevBuf* b : {&d_rgba, &d_direct, &d_scatter, &d_emission}) CK(b->reserve(sizeof(float4) * np), "film alloc");
-    // primary samples, shadow samples, the shadow wave's claim counter
-    CK(d_counters.reserve(3 * sizeof(unsigned long long)), "counter alloc");
-    CK(cudaMemsetAsync(d_counters.p, 0, 3 * sizeof(unsigned long long), st), "counter clear");
+    // primary samples, shadow samples, and the claim counters of the shadow
+    // wave, the count pass and the shading pass
+    CK(d_counters.reserve(5 * sizeof(unsigned long long)), "counter alloc");
+    CK(cudaMemsetAsync(d_counters.p, 0, 5 * sizeof(unsigned long long), st), "counter clear");
     DevScatterGrid sg{};
     if (splat_done) {
         sg.v = d_sg.as<float4>();
@@ -1418,7 +1419,10 @@ lg_status Ctx::render(const lg_camera* c) {
     CK(d_ps_data.reserve(pixel_sample_bytes() * nps1), "render alloc");
     waves_recorded = false;
     wmark(0);
-    CK(launch_render_count(sc, cam, sg, d_ps_count.as<int32_t>(), st), "render count");
+    int sms_c = 0;
+    CK(cudaDeviceGetAttribute(&sms_c, cudaDevAttrMultiProcessorCount, device), "device query");
+    CK(launch_render_count(sc, cam, sg, d_ps_count.as<int32_t>(), d_counters.as<unsigned long long>() + 3, sms_c, st),
+       "render count");
     CK(launch_exclusive_scan(d_ps_count.as<int32_t>(), n_ps, d_ps_offset.as<int32_t>(), d_ps_scan.as<int32_t>(),
                              d_ps_total.as<int32_t>(), st), "render scan");
     wmark(1);

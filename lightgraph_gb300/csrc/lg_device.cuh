@@ -199,7 +199,9 @@ struct LeafDDA {
 // step direction, the first crossing time and the crossing interval.
 __device__ __forceinline__ int dda_axis(float e, float d, float inv, float t0, int blo, int& step, float& next,
                                         float& delta) {
-    const float p = e + t0 * d;
+    // fused multiply-adds written out, so every kernel that walks a ray (the
+    // two primary passes above all) finds the same cells and crossings
+    const float p = __fmaf_rn(t0, d, e);
     const int ca = ((int)floorf(p)) >> 3;
     if (d == 0.f) {
         step = 0;
@@ -207,11 +209,11 @@ __device__ __forceinline__ int dda_axis(float e, float d, float inv, float t0, i
         delta = kInf;
     } else if (inv > 0.f) {
         step = 1;
-        next = t0 + ((float)(ca * 8 + 8) - p) * inv;
+        next = __fmaf_rn((float)(ca * 8 + 8) - p, inv, t0);
         delta = 8.f * inv;
     } else {
         step = -1;
-        next = t0 + ((float)(ca * 8) - p) * inv;
+        next = __fmaf_rn((float)(ca * 8) - p, inv, t0);
         delta = -8.f * inv;
     }
     return ca - blo + 1;

@@ -168,8 +168,10 @@ constexpr int kRayUnit = 2;  // consecutive tasks ordered as one unit
 cudaError_t launch_ray_bins(const ShadowTask* tasks, const int32_t* total, int64_t task_cap, const RayBins& rb,
                             int32_t* counts, int32_t* order, int sms, cudaStream_t st);
 // Wave 1: counts[ps] = shading samples of each pixel-sample.
+// claim: a zeroed counter the persistent grid's warps claim pixel samples
+// from.
 cudaError_t launch_render_count(const DevScene& sc, const DevCamera& cam, const DevScatterGrid& sg, int32_t* counts,
-                                cudaStream_t st);
+                                unsigned long long* claim, int sms, cudaStream_t st);
 // Shadow-ray ordering buffers: key_counts and key_offsets hold rb's keys,
 // key_scan the scan's block sums (keys / 1024 + 2), order n_lights * units
 // (units of kRayUnit tasks).
