@@ -186,9 +186,10 @@ __device__ __forceinline__ uint32_t primary_sample(const DevScene& sc, const Dev
 
 // Warps claim 32 consecutive pixel samples at a time from *claim (zero at
 // launch) until none are left: a persistent grid in which no warp slot waits
-// on another warp's long ray.
+// on another warp's long ray. The shading pass runs 5 CTAs per SM so that
+// its registers do not spill; the count pass, lighter, runs 6.
 template <bool kWrite, int DT>
-__global__ void __launch_bounds__(128, 6) k_primary(DevScene sc, DevCamera cam, DevScatterGrid sg,
+__global__ void __launch_bounds__(128, kWrite ? 5 : 6) k_primary(DevScene sc, DevCamera cam, DevScatterGrid sg,
                                                  int32_t* __restrict__ counts, const int32_t* __restrict__ offsets,
                                                  ShadowTask* __restrict__ tasks, int64_t task_cap,
                                                  PixelSample* __restrict__ out, unsigned long long* __restrict__ ctr,
