@@ -432,9 +432,12 @@ lg_status lg_fw_host(lg_ctx* ctx, float* dist, int n);
  * Scratch space is a fixed __device__ array inside the library sized for
  * n <= LG_NOALLOC_MAX_POINTS (larger n returns LG_ERR_INVALID). Every GPU
  * that loads the library keeps that array (about 1.7 MB) until the process
- * exits. All calls share it, so calls that overlap on the GPU race; serialise
- * them. The first call on each device looks up the array's device address, so
- * make that first call before any CUDA graph capture on the device. */
+ * exits. All calls share it, so calls whose work overlaps on the GPU race.
+ * The work is asynchronous: a host mutex around the calls does not order it.
+ * Order the calls on the device instead: issue them on one stream, or put an
+ * event wait or a synchronisation between calls on different streams. The
+ * first call on each device looks up the array's device address, so make that
+ * first call before any stream capture on the device. */
 #define LG_NOALLOC_MAX_POINTS 8192
 lg_status lg_diffuse_noalloc(const float* dist_device, int n, int ld,
                              const float* light_device, float* diffuse_device,

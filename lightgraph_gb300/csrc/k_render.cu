@@ -477,10 +477,14 @@ __global__ void __launch_bounds__(128) k_resolve(DevCamera cam, const int32_t* _
 }
 
 // Resident 128-thread CTAs per SM of the k_primary instance (kWrite, dtype).
+// Server slots render from several host threads at once: the value is
+// computed into a local and published through an atomic slot.
 static int primary_ctas_per_sm(bool write, int dtype) {
-    static int cache[2][3] = {{0, 0, 0}, {0, 0, 0}};
-    int& n = cache[write ? 1 : 0][dtype];
-    if (n == 0) {
+    static std::atomic<int> cache[2][3];
+    if (dtype < 0 || dtype > 2) dtype = 0;
+    std::atomic<int>& c = cache[write ? 1 : 0][dtype];
+    if (c.load() == 0) {
+        int n = 0;
         cudaError_t e;
         if (write)
             e = dtype == 1   ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_primary<true, 1>, 128, 0)
@@ -491,8 +495,9 @@ static int primary_ctas_per_sm(bool write, int dtype) {
                 : dtype == 2 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_primary<false, 2>, 128, 0)
                              : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_primary<false, 0>, 128, 0);
         if (e != cudaSuccess || n < 1) n = 1;
+        c.store(n);
     }
-    return n;
+    return c.load();
 }
 
 cudaError_t launch_render_count(const DevScene& sc, const DevCamera& cam, const DevScatterGrid& sg, int32_t* counts,

@@ -13,10 +13,12 @@
 // The array holds the partial column sums and column weights for up to
 // LG_NOALLOC_MAX_POINTS points (about 1.7 MB) plus one GraphInfo record. Every
 // GPU that loads this library keeps it until the process exits. All calls
-// share it: calls that overlap on the GPU (two streams, two threads) race on
-// it and must be serialised by the caller. Every scratch element is written
-// before it is read in each call, so the previous call's contents never leak
-// into a result and nothing needs clearing.
+// share it: calls whose work overlaps on the GPU race on it. The work is
+// asynchronous, so a host-side lock around the calls does not order them;
+// the caller orders them on the device (one stream, or an event or a
+// synchronisation between calls on different streams). Every scratch
+// element is written before it is read in each call, so the previous call's
+// contents never leak into a result and nothing needs clearing.
 #include <mutex>
 
 #include "lg_kernels.h"
@@ -56,6 +58,15 @@ lg_status device_ptrs(DevicePtrs& out) {
     return LG_OK;
 }
 
+// One record: a single graph of n points whose matrix starts at the caller's
+// pointer, with its points and vectors at row 0.
+__global__ void k_noalloc_record(int n, int ld) {
+    GraphInfo gi{};
+    gi.n = n;
+    gi.ld = ld;
+    g_noalloc_graph = gi;
+}
+
 }  // namespace
 }  // namespace lg
 
@@ -72,16 +83,10 @@ extern "C" lg_status lg_diffuse_noalloc(const float* dist_device, int n, int ld,
     const lg_status s = device_ptrs(p);
     if (s != LG_OK) return s;
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
-    GraphInfo gi{};
-    gi.pt_off = 0;
-    gi.s_off = 0;
-    gi.e_off = 0;
-    gi.n = n;
-    gi.ld = ld;
-    gi.max_edges = 0;
-    gi.r2 = 0.f;
-    // the record goes through a copy into the static array (no allocation)
-    if (cudaMemcpyAsync(p.graph, &gi, sizeof gi, cudaMemcpyHostToDevice, st) != cudaSuccess) return LG_ERR_CUDA;
+    // the graph record is written on the device, in stream order, from the
+    // kernel's arguments: no host buffer has to outlive this call
+    k_noalloc_record<<<1, 1, 0, st>>>(n, ld);
+    ++g_launch_counter;
     DevShader sh{};
     for (int c = 0; c < 3; ++c) sh.a[c] = (float)(-extinction[c]);
     float* part = p.scratch;

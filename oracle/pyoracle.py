@@ -210,6 +210,15 @@ def randgen_draws(seed, n):
     return out, raw
 
 
+def diffuse(T_solved, L):
+    """lgo_diffuse: diffuseLight on an RGB path matrix (diagonal 1) and vertex radiance."""
+    n = T_solved.shape[0]
+    D = np.zeros((n, 3))
+    load().lgo_diffuse(n, _p(np.ascontiguousarray(T_solved, np.float64)), _p(np.ascontiguousarray(L, np.float64)),
+                       _p(D))
+    return D
+
+
 def fw_minplus_f32(S):
     S = np.ascontiguousarray(S, np.float32).copy()
     load().lgo_fw_minplus_f32(S.shape[0], _p(S))

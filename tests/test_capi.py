@@ -57,6 +57,26 @@ def test_server_entry_points_reject_null_handles():
     assert lib.lg_server_destroy(None) in (_capi.LG_OK, _capi.LG_ERR_INVALID)
 
 
+def test_noalloc_diffuse_argument_checks():
+    """lg_diffuse_noalloc validates its arguments before touching the device:
+    bad sizes, a leading dimension below n, null buffers and a positive
+    extinction are refused, and n == 0 is a no-op (no GPU needed)."""
+    lib = _capi.load()
+    ext = (C.c_double * 3)(-1.0, -1.0, -1.0)
+    buf = C.c_void_p(16)  # never dereferenced: every call below returns before any device work
+    call = lib.lg_diffuse_noalloc
+    assert call(None, 0, 0, None, None, ext, None) == _capi.LG_OK
+    assert call(buf, -1, 0, buf, buf, ext, None) == _capi.LG_ERR_INVALID
+    assert call(buf, 8193, 8193, buf, buf, ext, None) == _capi.LG_ERR_INVALID
+    assert call(buf, 10, 9, buf, buf, ext, None) == _capi.LG_ERR_INVALID
+    assert call(None, 10, 10, buf, buf, ext, None) == _capi.LG_ERR_INVALID
+    assert call(buf, 10, 10, None, buf, ext, None) == _capi.LG_ERR_INVALID
+    assert call(buf, 10, 10, buf, None, ext, None) == _capi.LG_ERR_INVALID
+    assert call(buf, 10, 10, buf, buf, None, None) == _capi.LG_ERR_INVALID
+    for bad in ((0.5, -1.0, -1.0), (-1.0, float("nan"), -1.0)):
+        assert call(buf, 10, 10, buf, buf, (C.c_double * 3)(*bad), None) == _capi.LG_ERR_INVALID
+
+
 def test_shader_defaults_and_coefficients():
     s = Shader()
     c = s.to_c()
