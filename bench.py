@@ -364,56 +364,150 @@ def profile_traffic(name: str):
 # CPU baseline: the oracle (the reference's loops in FP64, OpenMP) on a sample
 # ---------------------------------------------------------------------------
 
-def cpu_sample(sc, fw_rounds: int, row_stride: int):
-    """Times the reference's stages on the host cores on a bounded sample and
-    scales each to the full frame. Returns (ms_per_frame, detail)."""
-    import ctypes as C
+FW_WINDOWS = 8        # Floyd-Warshall: windows of consecutive rounds, spread over the solve
+SAMPLE_FRACTION = 32  # 1/32 of the Floyd-Warshall rounds and 1/32 of the image rows are timed
+
+
+class CpuFrameSample:
+    """The reference's frame on the host cores, timed on a bounded sample.
+
+    One rule, used by both the --impl reference arm and the cpu_baseline leg:
+      * graph build, edge march, vertex light, diffusion and splat run whole;
+      * Floyd-Warshall (floydAlgo's FP64 max-times loop, OpenMP over rows):
+        FW_WINDOWS windows of n / (FW_WINDOWS * SAMPLE_FRACTION) consecutive
+        rounds, centred in equal parts of the solve, each started from the
+        matrix as it stands at that round, scaled x SAMPLE_FRACTION. A round's
+        cost depends on how far the matrix has filled in, so a prefix of
+        rounds would under-count it. The states at the window starts are
+        reached once, untimed, by FP32 min-plus rounds, which give floydAlgo's
+        sparsity pattern after the same rounds;
+      * render: the rows (r + 1/2) H / R, R = H / SAMPLE_FRACTION, in one call
+        parallel over their pixels, scaled x SAMPLE_FRACTION.
+    setup() does the untimed preparation once; step() times one sample."""
+
+    def __init__(self, sc):
+        self.sc = sc
+
+    def setup(self):
+        import ctypes as C
+        from oracle import pyoracle as po
+        sc = self.sc
+        self.po = po
+        lib = self.lib = po.load()
+        lib.lgo_fw_maxtimes_rounds.argtypes = [C.c_int, C.c_void_p, C.c_int, C.c_int]
+        lib.lgo_fw_minplus_f32_rounds.argtypes = [C.c_int, C.c_void_p, C.c_int, C.c_int]
+        lib.lgo_transmittance_of.argtypes = [C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p]
+        self.o = po.Oracle(sc.density, sc.shader, sc.opts, sc.lights, temperature=sc.temperature,
+                           env_map=sc.env_map)
+        self.pts = sc.points[0]
+        n = self.n = len(self.pts)
+        adj, _ = self.o.build_graph(self.pts, sc.radius_sq[0], sc.max_connect)
+        _, S = self.o.march_edges(self.pts, adj, want_T=False)
+        self.ext = np.ascontiguousarray(sc.shader.getExtinction(), np.float64)
+        self.K = max(1, n // (FW_WINDOWS * SAMPLE_FRACTION))
+        part = n / FW_WINDOWS
+        self.k0 = [min(n - self.K, max(0, int((w + 0.5) * part - self.K / 2))) for w in range(FW_WINDOWS)]
+        state = np.ascontiguousarray(S, np.float32)
+        self.states, k = [], 0
+        for k0 in self.k0:
+            lib.lgo_fw_minplus_f32_rounds(n, state.ctypes.data, k, k0)
+            k = k0
+            self.states.append(state.copy())
+        lib.lgo_fw_minplus_f32_rounds(n, state.ctypes.data, k, n)
+        np.fill_diagonal(state, 0.0)
+        self.T_solved = self._transmittance(state)
+        self.T_window = np.empty((n, n, 3))
+        H = sc.opts.height
+        R = max(1, H // SAMPLE_FRACTION)
+        self.rows = np.ascontiguousarray([min(H - 1, int((r + 0.5) * H / R)) for r in range(R)], np.int32)
+        self.row_scale = H / R
+        self.fw_scale = n / (FW_WINDOWS * self.K)
+        return self
+
+    def _transmittance(self, S, out=None):
+        n = S.shape[0]
+        out = np.empty((n, n, 3)) if out is None else out
+        S64 = np.ascontiguousarray(S, np.float64)
+        self.lib.lgo_transmittance_of(n * n, S64.ctypes.data, self.ext.ctypes.data, out.ctypes.data)
+        return out
+
+    def describe(self):
+        return (f"build/march/light/diffuse/splat whole; Floyd-Warshall {FW_WINDOWS} windows of {self.K} rounds "
+                f"spread over {self.n} (each from the matrix's state at its round) scaled x{self.fw_scale:g}; "
+                f"render rows (r+1/2)H/{len(self.rows)} ({len(self.rows)} of {self.sc.opts.height}) in one "
+                f"pixel-parallel call scaled x{self.row_scale:g}")
+
+    def step(self):
+        """One timed sample: (ms per frame, per-stage ms)."""
+        import ctypes as C
+        o, sc, pts, n, lib = self.o, self.sc, self.pts, self.n, self.lib
+        det = {}
+        t = time.perf_counter()
+        adj, _ = o.build_graph(pts, sc.radius_sq[0], sc.max_connect)
+        det["build_graph"] = (time.perf_counter() - t) * 1e3
+        t = time.perf_counter()
+        o.march_edges(pts, adj)
+        det["edge_march"] = (time.perf_counter() - t) * 1e3
+        fw = 0.0
+        for k0, st in zip(self.k0, self.states):
+            self._transmittance(st, self.T_window)
+            t = time.perf_counter()
+            lib.lgo_fw_maxtimes_rounds(n, self.T_window.ctypes.data, k0, k0 + self.K)
+            fw += time.perf_counter() - t
+        det["floyd_warshall"] = fw * 1e3 * self.fw_scale
+        t = time.perf_counter()
+        L = o.vertex_light(pts)
+        det["vertex_light"] = (time.perf_counter() - t) * 1e3
+        t = time.perf_counter()
+        D = o.diffuse(self.T_solved, L)
+        det["diffuse"] = (time.perf_counter() - t) * 1e3
+        t = time.perf_counter()
+        lo, dims, sg, _ = o.splat(pts, D)
+        det["splat"] = (time.perf_counter() - t) * 1e3
+        W, H = sc.opts.width, sc.opts.height
+        films = [np.zeros((H, W, 4), np.float32) for _ in range(4)]
+        vals = np.ascontiguousarray(sg, np.float32)
+        cam = sc.opts.camera_c()
+        lib.lgo_render_rows.argtypes = None
+        t = time.perf_counter()
+        lib.lgo_render_rows(C.byref(o.dens), C.byref(o.temp) if o.temp else None, C.byref(o.shader),
+                            C.byref(o.settings), o.lights, o.n_lights, C.byref(o.env) if o.env else None,
+                            C.byref(cam), (C.c_int32 * 3)(*lo), (C.c_int32 * 3)(*dims),
+                            C.c_double(sc.density.voxel_size * sc.opts.scatterGridResFactor),
+                            C.c_void_p(vals.ctypes.data), C.c_void_p(self.rows.ctypes.data), C.c_int(len(self.rows)),
+                            *[C.c_void_p(f.ctypes.data) for f in films], None)
+        det["render"] = (time.perf_counter() - t) * 1e3 * self.row_scale
+        return sum(det.values()), det
+
+
+def cpu_full_frame_ms(sc):
+    """The whole frame on the host cores, nothing sampled: FP64 max-times
+    Floyd-Warshall over every round and every image row."""
     from oracle import pyoracle as po
-    lib = po.load()
-    lib.lgo_fw_maxtimes_rounds.argtypes = [C.c_int, C.c_void_p, C.c_int, C.c_int]
     o = po.Oracle(sc.density, sc.shader, sc.opts, sc.lights, temperature=sc.temperature, env_map=sc.env_map)
     pts = sc.points[0]
-    n = len(pts)
-    det = {}
     t = time.perf_counter()
     adj, _ = o.build_graph(pts, sc.radius_sq[0], sc.max_connect)
-    det["build_graph"] = (time.perf_counter() - t) * 1e3
-    t = time.perf_counter()
-    T, S = o.march_edges(pts, adj)
-    det["edge_march"] = (time.perf_counter() - t) * 1e3
-    T2 = np.ascontiguousarray(T.copy())
-    k1 = min(n, fw_rounds)
-    t = time.perf_counter()
-    lib.lgo_fw_maxtimes_rounds(n, T2.ctypes.data, 0, k1)
-    det["floyd_warshall"] = (time.perf_counter() - t) * 1e3 * (n / k1)
-    # the rest of the chain needs the solved matrix: solve it outside the timer
-    # with the FP64 min-plus form (same result)
-    a = -np.array(sc.shader.getExtinction())
-    Sd = po.fw_minplus_f64(S)
-    Tsol = np.exp(-a[None, None, :] * Sd[:, :, None])
-    idx = np.arange(n)
-    Tsol[idx, idx, :] = 1.0
-    t = time.perf_counter()
+    T, _ = o.march_edges(pts, adj)
+    Tsol = o.fw_maxtimes(T)
     L = o.vertex_light(pts)
-    det["vertex_light"] = (time.perf_counter() - t) * 1e3
-    t = time.perf_counter()
     D = o.diffuse(Tsol, L)
-    det["diffuse"] = (time.perf_counter() - t) * 1e3
-    from lightgraph_gb300 import _capi
-    hp = _capi.load().lg_point_voxel_size(n, pts.ctypes.data, 8)
-    t = time.perf_counter()
-    lo, dims, sg, _ = o.splat(pts, D, hp)
-    det["splat"] = (time.perf_counter() - t) * 1e3
-    H = sc.opts.height
-    rows = list(range(0, H, row_stride))
-    t = time.perf_counter()
-    for r in rows:
-        o.render((lo, dims, sg), rows=(r, r + 1))
-    det["render"] = (time.perf_counter() - t) * 1e3 * (H / len(rows))
-    total = sum(det.values())
-    sample = (f"all of build/march/light/diffuse/splat; Floyd-Warshall rounds 0..{k1} of {n} scaled x{n / k1:.0f}; "
-              f"render rows every {row_stride} ({len(rows)} of {H}) scaled x{H / len(rows):.0f}")
-    return total, det, sample, o.threads()
+    lo, dims, sg, _ = o.splat(pts, D)
+    o.render((lo, dims, sg))
+    return (time.perf_counter() - t) * 1e3
+
+
+def sampler_error():
+    """The sampling rule checked once against a whole frame it can afford:
+    the small 128^3 / 1024-point / 256^2 frame timed complete on the host
+    cores beside its sampled estimate (best of two each)."""
+    from lightgraph_gb300 import scenes
+    sc = scenes.small()
+    full = min(cpu_full_frame_ms(sc) for _ in range(2))
+    smp = CpuFrameSample(sc).setup()
+    est = min(smp.step()[0] for _ in range(2))
+    return {"workload": "small 128^3 sphere-fBm, 1024-point LightGraph, 256x256 at 1 spp",
+            "full_frame_ms": full, "sampled_estimate_ms": est, "relative_error": (est - full) / full}
 
 
 def run_reference(args):
@@ -421,23 +515,25 @@ def run_reference(args):
     if rank != 0:
         return 0
     sc = make_scene(args.small, args.image, args.spp, args.res)
-    fw_rounds, stride = (32, 256) if not args.small else (64, 32)
-    vals = []
+    check = sampler_error()
+    smp = CpuFrameSample(sc).setup()
     for _ in range(args.warmup):
-        cpu_sample(sc, fw_rounds, stride)
-    det_acc = None
-    threads = 1
+        smp.step()
+    vals, det_acc = [], {}
     for _ in range(args.steps):
-        v, det, sample, threads = cpu_sample(sc, fw_rounds, stride)
+        v, det = smp.step()
         vals.append(v)
-        det_acc = det
+        for k, x in det.items():
+            det_acc[k] = det_acc.get(k, 0.0) + x / args.steps
     value = float(np.mean(vals))
+    threads = smp.o.threads()
     line = {"metric": "ms/frame", "value": value, "unit": "ms", "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": value, "higher_is_better": False, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
             "config": workload_config(sc, args.small),
             "cpu_baseline": {"value": value, "unit": "ms/frame", "cores": threads, "kind": "port",
-                             "sample": sample, "stages_ms": det_acc},
+                             "sample": smp.describe(), "stages_ms": {k: round(x, 3) for k, x in det_acc.items()},
+                             "sampler_check": check},
             "e2e": {"value": value, "unit": "ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
@@ -586,10 +682,12 @@ def run_ours(args):
     if rank == 0 and world == 1 and args.batched and not args.small:
         line["batched_graphs"] = run_batched_graphs(local)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        fw_rounds, stride = (128, 64) if not args.small else (256, 16)
-        v, det, sample, threads = cpu_sample(sc, fw_rounds, stride)
-        line["cpu_baseline"] = {"value": v, "unit": "ms/frame", "cores": threads, "kind": "port",
-                                "sample": sample, "stages_ms": {k: round(x, 3) for k, x in det.items()}}
+        smp = CpuFrameSample(sc).setup()
+        smp.step()  # warm-up
+        v, det = smp.step()
+        line["cpu_baseline"] = {"value": v, "unit": "ms/frame", "cores": smp.o.threads(), "kind": "port",
+                                "sample": smp.describe(), "stages_ms": {k: round(x, 3) for k, x in det.items()},
+                                "sampler_check": sampler_error()}
     if rank == 0:
         print(json.dumps(line), flush=True)
     ctx.close()

@@ -281,8 +281,12 @@ lg_status lg_solve_graphs(lg_ctx* ctx, float* diffuse_out);
  *   src/LightGraph.h:714); <= 0 selects lg_point_voxel_size() of the points. */
 lg_status lg_splat(lg_ctx* ctx, double point_voxel_size);
 
-/* The estimate used when lg_splat gets point_voxel_size <= 0: the edge of a
- * cube holding points_per_voxel points on average over the points' bbox. */
+/* The point index's voxel size that lg_splat uses when it gets
+ * point_voxel_size <= 0: points::computeVoxelSize(positions, 8) as
+ * LightGraph::buildVdbPointGrid calls it (src/LightGraph.h:713-714) -- a
+ * bounding-box estimate refined on the voxels the points occupy, rounded to
+ * five decimal places; 0.1 for fewer than two or coincident points. Host
+ * only (no device work). */
 double lg_point_voxel_size(int64_t n_points, const float* points, int points_per_voxel);
 
 /* Copies out the scatter grid: dims/origin of the coarse dense box and, if
@@ -509,6 +513,9 @@ uint64_t lg_request_bytes(const lg_request* req);
 /* ------------------------------------------------------------------------- */
 /* Host helpers: the reference's scene description (no device work)          */
 /* ------------------------------------------------------------------------- */
+/* These, lg_write_exr and lg_read_exr_rgba live in liblightgraph_host.so, a
+ * host-only library with no CUDA code (link it beside liblightgraph_gb300.so);
+ * every other function of this header is in liblightgraph_gb300.so. */
 
 /* Shader() defaults (src/Shader.h:123-138). */
 void lg_shader_default(lg_shader* shader);

@@ -1,8 +1,13 @@
 """ctypes binding of include/lightgraph_c.h and include/lightgraph_scene.h.
 
-The shared library is built in-tree (lightgraph_gb300/_build) by
-``lightgraph_gb300.build``; importing this module without it raises, so the
-GPU path can never silently fall back to anything else.
+Two in-tree libraries (lightgraph_gb300/_build, made by
+``lightgraph_gb300.build``) export these symbols:
+  * liblightgraph_gb300.so -- the CUDA path and its C ABI (:func:`load`);
+  * liblightgraph_host.so  -- host-only helpers with no CUDA code: scene
+    description defaults and parsers, the EXR reader and writer, and the
+    seeded synthetic scenes (:func:`load_host`).
+Loading a missing library raises, so the GPU path can never silently fall back
+to anything else.
 """
 from __future__ import annotations
 
@@ -92,7 +97,8 @@ P = C.c_void_p
 I32, I64, U64, D, F = C.c_int32, C.c_int64, C.c_uint64, C.c_double, C.c_float
 
 # name -> (restype, argtypes). Every symbol of include/lightgraph_c.h and
-# include/lightgraph_scene.h is listed; tests check the library exports them.
+# include/lightgraph_scene.h is listed in one of the two tables; tests check
+# that the libraries export them.
 SIGNATURES = {
     "lg_create": (I32, [C.c_int, C.POINTER(P)]),
     "lg_destroy": (I32, [P]),
@@ -120,8 +126,6 @@ SIGNATURES = {
     "lg_get_scatter_grid": (I32, [P, P, P, P]),
     "lg_get_vertex_data": (I32, [P, P, P]),
     "lg_geo_dump": (I32, [P, C.c_char_p, C.c_char_p, C.c_int]),
-    "lg_write_exr": (I32, [C.c_char_p, C.c_int, C.c_int, C.c_int, P, P]),
-    "lg_read_exr_rgba": (I32, [C.c_char_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32), P]),
     "lg_render": (I32, [P, C.POINTER(CameraC), P, P, P, P]),
     "lg_render_frame": (I32, [P, C.c_int, P, P, P, C.c_int, D, C.POINTER(CameraC), P, P, P, P]),
     "lg_frame_device": (I32, [P, C.c_int, D, C.POINTER(CameraC)]),
@@ -148,6 +152,12 @@ SIGNATURES = {
     "lg_server_poll": (I32, [P, I64, C.POINTER(C.c_int)]),
     "lg_server_wait": (I32, [P, I64, C.c_int, P, C.POINTER(D), C.POINTER(D)]),
     "lg_request_bytes": (U64, [C.POINTER(RequestC)]),
+}
+
+# liblightgraph_host.so: scene description helpers, EXR files, synthetic scenes
+HOST_SIGNATURES = {
+    "lg_read_exr_rgba": (I32, [C.c_char_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32), P]),
+    "lg_write_exr": (I32, [C.c_char_p, C.c_int, C.c_int, C.c_int, P, P]),
     "lg_shader_default": (None, [C.POINTER(ShaderC)]),
     "lg_shader_set_coefficients": (None, [C.POINTER(ShaderC), C.POINTER(D), C.POINTER(D), C.POINTER(D)]),
     "lg_settings_default": (None, [C.POINTER(SettingsC)]),
@@ -160,25 +170,36 @@ SIGNATURES = {
 }
 
 _lib = None
+_host = None
 
 
-def load() -> C.CDLL:
-    """Load the in-tree library; raise if it has not been built."""
-    global _lib
-    if _lib is not None:
-        return _lib
-    path = _build.lib_path()
+def _open(path: str, table: dict) -> C.CDLL:
     if not os.path.exists(path):
         raise ImportError(
             f"lightgraph_gb300 native library missing at {path}; run "
             "`python -c 'import __graft_entry__ as g; g.build()'` (needs nvcc for sm_103a)")
     lib = C.CDLL(path)
-    for name, (res, args) in SIGNATURES.items():
+    for name, (res, args) in table.items():
         fn = getattr(lib, name)
         fn.restype = res
         fn.argtypes = args
-    _lib = lib
     return lib
+
+
+def load() -> C.CDLL:
+    """Load the in-tree CUDA library; raise if it has not been built."""
+    global _lib
+    if _lib is None:
+        _lib = _open(_build.lib_path(), SIGNATURES)
+    return _lib
+
+
+def load_host() -> C.CDLL:
+    """Load the in-tree host-only helper library; raise if it has not been built."""
+    global _host
+    if _host is None:
+        _host = _open(_build.host_lib_path(), HOST_SIGNATURES)
+    return _host
 
 
 class LightGraphError(RuntimeError):

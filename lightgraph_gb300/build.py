@@ -2,9 +2,13 @@
 
 Compiles, in parallel and only when sources changed:
   * lightgraph_gb300/_build/liblightgraph_gb300.so  -- CUDA kernels for sm_103a
-    (nvcc -gencode arch=compute_103a,code=sm_103a) plus the C ABI and the
-    synthetic-scene generator (g++ -fopenmp -ffp-contract=off);
-  * lightgraph_gb300/_build/lightgraph              -- the command-line renderer;
+    (nvcc -gencode arch=compute_103a,code=sm_103a) plus the C ABI;
+  * lightgraph_gb300/_build/liblightgraph_host.so   -- host-only helpers, no CUDA
+    (g++ -fopenmp -ffp-contract=off): the seeded synthetic scenes, the scene
+    description defaults and parsers, and the EXR reader and writer. The CPU
+    baseline builds its scenes through this library alone;
+  * lightgraph_gb300/_build/lightgraph              -- the command-line renderer
+    (links both libraries);
   * oracle/_build/liblg_oracle.so                   -- the CPU oracle used by the
     tests and the CPU baseline (test infrastructure, never linked into the
     product library).
@@ -26,11 +30,12 @@ ORACLE_DIR = os.path.join(ROOT, "oracle")
 ORACLE_BUILD = os.path.join(ORACLE_DIR, "_build")
 
 LIB_NAME = "liblightgraph_gb300.so"
+HOST_LIB_NAME = "liblightgraph_host.so"
 ORACLE_NAME = "liblg_oracle.so"
 
 CU_SOURCES = ["lg_api.cu", "k_graph.cu", "k_march.cu", "k_fw.cu", "k_diffuse.cu", "k_splat.cu",
               "k_render.cu", "k_grid.cu", "k_dart.cu", "lg_server.cu", "lg_noalloc.cu"]
-CC_SOURCES = ["scene.cc", "lg_parse.cc", "lg_exr.cc"]
+HOST_SOURCES = ["scene.cc", "lg_parse.cc", "lg_exr.cc"]
 CLI_SOURCE = "cli.cc"
 ORACLE_SOURCES = ["lg_oracle.cc"]
 
@@ -43,6 +48,10 @@ GXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-fopenmp", "-ffp-contract=off", "-I"
 
 def lib_path() -> str:
     return os.path.join(BUILD, LIB_NAME)
+
+
+def host_lib_path() -> str:
+    return os.path.join(BUILD, HOST_LIB_NAME)
 
 
 def oracle_path() -> str:
@@ -91,31 +100,34 @@ def build_library(verbose: bool = False, jobs: int | None = None) -> str:
     nvcc = _nvcc()
     hdrs = _headers(CSRC, INCLUDE)
     jobs_list = []
-    objs = []
+    objs, host_objs = [], []
     for src in CU_SOURCES:
         s = os.path.join(CSRC, src)
         o = os.path.join(BUILD, src + ".o")
         objs.append(o)
         if _stale(o, [s] + hdrs):
             jobs_list.append([nvcc] + NVCC_FLAGS + ["-c", s, "-o", o])
-    for src in CC_SOURCES:
+    for src in HOST_SOURCES:
         s = os.path.join(CSRC, src)
         o = os.path.join(BUILD, src + ".o")
-        objs.append(o)
+        host_objs.append(o)
         if _stale(o, [s] + hdrs):
             jobs_list.append(["g++"] + GXX_FLAGS + ["-c", s, "-o", o])
     n = jobs or min(len(jobs_list), os.cpu_count() or 4) or 1
     with cf.ThreadPoolExecutor(max_workers=n) as ex:
         for f in [ex.submit(_run, j, verbose) for j in jobs_list]:
             f.result()
+    host = host_lib_path()
+    if _stale(host, host_objs):
+        _run(["g++", "-shared", "-o", host] + host_objs + ["-fopenmp"], verbose)
     lib = lib_path()
     if _stale(lib, objs):
         _run([nvcc] + ARCH + ["-shared", "-o", lib] + objs + ["-Xcompiler", "-fopenmp", "-lgomp"], verbose)
     cli = cli_path()
     cli_src = os.path.join(CSRC, CLI_SOURCE)
-    if _stale(cli, [cli_src, lib] + hdrs):
+    if _stale(cli, [cli_src, lib, host] + hdrs):
         _run(["g++", "-O2", "-std=c++17", "-I" + INCLUDE, cli_src, "-o", cli, "-L" + BUILD, "-llightgraph_gb300",
-              "-Wl,-rpath,$ORIGIN"], verbose)
+              "-llightgraph_host", "-Wl,-rpath,$ORIGIN"], verbose)
     return lib
 
 
@@ -141,4 +153,5 @@ def build_all(verbose: bool = False) -> None:
 if __name__ == "__main__":
     build_all(verbose="-v" in sys.argv)
     print(lib_path())
+    print(host_lib_path())
     print(oracle_path())

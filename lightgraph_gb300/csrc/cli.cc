@@ -72,6 +72,20 @@ double now_s() {
 
 }  // namespace
 
+// Edge of the cube that holds one point on average over the points' bbox
+// (0.1 for fewer than two points or a flat box).
+static double mean_spacing(int64_t n, const float* p) {
+    if (n < 2) return 0.1;
+    double lo[3] = {p[0], p[1], p[2]}, hi[3] = {p[0], p[1], p[2]};
+    for (int64_t i = 1; i < n; ++i)
+        for (int a = 0; a < 3; ++a) {
+            lo[a] = std::min(lo[a], (double)p[3 * i + a]);
+            hi[a] = std::max(hi[a], (double)p[3 * i + a]);
+        }
+    const double vol = (hi[0] - lo[0]) * (hi[1] - lo[1]) * (hi[2] - lo[2]);
+    return vol > 0 ? std::cbrt(vol / (double)n) : 0.1;
+}
+
 int main(int argc, char** argv) {
     lg_shader shader;
     lg_shader_default(&shader);
@@ -238,9 +252,7 @@ int main(int argc, char** argv) {
         double r = connect_radius;
         if (r <= 0) {
             // 1.7 x the mean spacing of the graph's points (CONNECT_SEARCH_RADIUS_MULT)
-            const int64_t n = offs[g + 1] - offs[g];
-            const double hp = lg_point_voxel_size(n, pts.data() + 3 * offs[g], 1);
-            r = 1.7 * hp;
+            r = 1.7 * mean_spacing(offs[g + 1] - offs[g], pts.data() + 3 * offs[g]);
         }
         r2[g] = (float)r * (float)r;
     }

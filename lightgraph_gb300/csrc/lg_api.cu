@@ -2,11 +2,13 @@
 // scene state and the stage entry points that replace the reference's
 // LightGraph / ScatterGrid / VolumeRender member functions.
 #include <algorithm>
+#include <array>
 #include <climits>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <limits>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -1243,30 +1245,106 @@ extern "C" lg_status lg_geo_dump(lg_ctx* handle, const char* dir, const char* st
 // stage 2: scatter grid
 // ---------------------------------------------------------------------------
 
-extern "C" double lg_point_voxel_size(int64_t n, const float* pts, int points_per_voxel) {
-    // computeVoxelSize's starting estimate (src/LightGraph.h:713-714): the
-    // edge of a cube holding points_per_voxel points on average over the
-    // points' bounding box. 0.1 (OpenVDB's default) for fewer than 2 points.
-    if (n <= 1 || !pts || points_per_voxel <= 0) return 0.1;
-    double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
-    for (int64_t i = 0; i < n; ++i)
-        for (int a = 0; a < 3; ++a) {
-            lo[a] = std::min(lo[a], (double)pts[3 * i + a]);
-            hi[a] = std::max(hi[a], (double)pts[3 * i + a]);
-        }
-    double ext[3];
-    double maxe = 0;
-    for (int a = 0; a < 3; ++a) {
-        ext[a] = hi[a] - lo[a];
-        maxe = std::max(maxe, ext[a]);
+// points::computeVoxelSize(positions, 8) as LightGraph::buildVdbPointGrid
+// calls it (src/LightGraph.h:713-714): OpenVDB's procedure with its defaults
+// (identity transform, five decimal places). It starts from the points'
+// bounding box, voxel = float(pow(volume / target, 1/3)) with target =
+// max(1, n / points_per_voxel), then refines on the occupancy: the points
+// fall into `count` distinct cell-centred voxels round(p / voxel), volume =
+// float(voxel^3) * count, and the voxel is recomputed from that volume until
+// the volume stops shrinking, the count stops growing or the voxel shrinks by
+// less than 10%. The result is rounded to five decimal places (more if that
+// gives 0). Occupancy is counted in a byte map over the points' cell box
+// (a sort of the cell keys when that box is large).
+namespace {
+bool voxel_from_volume(double volume, size_t target, float& voxel) {
+    const double fmax = (double)std::numeric_limits<float>::max();
+    double vv = volume / (double)target;
+    bool ok = true;
+    if (vv < 3e-15) {
+        vv = 3e-15;
+        ok = false;
+    } else if (vv > fmax * fmax * fmax) {
+        vv = fmax * fmax * fmax;
+        ok = false;
     }
-    if (maxe <= 0) return 0.1;
-    // flat point sets: a degenerate axis gets the extent of the largest one
-    for (int a = 0; a < 3; ++a)
-        if (ext[a] <= 0) ext[a] = maxe;
-    const double target = std::max<double>(1.0, (double)(n / points_per_voxel));
-    const double vol = ext[0] * ext[1] * ext[2];
-    return std::cbrt(vol / target);
+    voxel = (float)std::pow(vv, 1.0 / 3.0);
+    return ok;
+}
+
+int64_t occupied_voxels(int64_t n, const float* pts, const double lo[3], const double hi[3], float voxel) {
+    const double inv = 1.0 / (double)voxel;
+    int64_t c0[3], dim[3];
+    int64_t cells = 1;
+    for (int a = 0; a < 3; ++a) {
+        // round(p * inv) is monotonic in p: the box of the cells is the cells of the box
+        c0[a] = (int64_t)std::floor(lo[a] * inv + 0.5);
+        dim[a] = (int64_t)std::floor(hi[a] * inv + 0.5) - c0[a] + 1;
+        cells = (cells > (int64_t)1 << 40) ? cells : cells * dim[a];
+    }
+    if (cells <= ((int64_t)1 << 28)) {
+        std::vector<uint8_t> seen((size_t)cells, 0);
+        int64_t count = 0;
+        for (int64_t i = 0; i < n; ++i) {
+            int64_t k = 0;
+            for (int a = 2; a >= 0; --a)
+                k = k * dim[a] + ((int64_t)std::floor((double)pts[3 * i + a] * inv + 0.5) - c0[a]);
+            count += seen[(size_t)k] == 0;
+            seen[(size_t)k] = 1;
+        }
+        return count;
+    }
+    std::vector<std::array<int64_t, 3>> keys((size_t)n);
+    for (int64_t i = 0; i < n; ++i)
+        for (int a = 0; a < 3; ++a) keys[(size_t)i][a] = (int64_t)std::floor((double)pts[3 * i + a] * inv + 0.5);
+    std::sort(keys.begin(), keys.end());
+    return (int64_t)(std::unique(keys.begin(), keys.end()) - keys.begin());
+}
+}  // namespace
+
+extern "C" double lg_point_voxel_size(int64_t n, const float* pts, int points_per_voxel) {
+    float voxel = 0.1f;  // OpenVDB's default, kept for fewer than two or coincident points
+    if (n <= 1 || !pts || points_per_voxel <= 0) return voxel;
+    size_t target = (size_t)n / (size_t)points_per_voxel;
+    if (target == 0) target = 1;
+    double lo[3], hi[3];
+    for (int a = 0; a < 3; ++a) lo[a] = hi[a] = (double)pts[a];
+    for (int64_t i = 1; i < n; ++i)
+        for (int a = 0; a < 3; ++a) {
+            const double v = (double)pts[3 * i + a];
+            lo[a] = v < lo[a] ? v : lo[a];
+            hi[a] = v > hi[a] ? v : hi[a];
+        }
+    if (lo[0] == hi[0] && lo[1] == hi[1] && lo[2] == hi[2]) return voxel;
+    double ext[3] = {hi[0] - lo[0], hi[1] - lo[1], hi[2] - lo[2]};
+    double volume = ext[0] * ext[1] * ext[2];
+    if (std::fabs(volume) <= 1e-15) {  // coplanar: largest x next^2; collinear: largest^3
+        std::sort(ext, ext + 3);
+        volume = std::fabs(ext[1]) <= 1e-15 ? ext[2] * ext[2] * ext[2] : ext[2] * ext[1] * ext[1];
+    }
+    double prev_volume = volume;
+    if (!voxel_from_volume(volume, target, voxel)) return voxel;
+    int64_t prev_count = 0, count = 1;
+    while (count > prev_count) {
+        prev_count = count;
+        count = occupied_voxels(n, pts, lo, hi, voxel);
+        volume = (double)((voxel * voxel * voxel) * (float)count);
+        if (volume >= prev_volume) break;
+        prev_volume = volume;
+        const float prev_voxel = voxel;
+        if (!voxel_from_volume(volume, target, voxel)) {
+            voxel = prev_voxel;
+            break;
+        }
+        if (voxel / prev_voxel > 0.9f) break;
+    }
+    float out = voxel;
+    double tenth = 1e5;
+    for (int d = 5; d < 11; ++d, tenth *= 10.0) {
+        out = (float)(std::floor((double)voxel * tenth + 0.5) / tenth);
+        if (out != 0.0f) break;
+    }
+    return (double)out;
 }
 
 lg_status Ctx::splat(double point_voxel_size) {
@@ -1300,7 +1378,8 @@ lg_status Ctx::splat(double point_voxel_size) {
     // ScatterGrid::operator() kernel size (src/ScatterGrid.h:69-75), with
     // K = ptsPerKernel * iter (src/main.cc:586)
     const double K = (double)settings.pts_per_kernel * (double)settings.iter;
-    const double radius = std::cbrt((3.0 * K * hp * hp * hp) / (32.0 * 3.14159265358979323846));
+    const double hp3 = hp * hp * hp;
+    const double radius = std::pow((3.0 * K * hp3) / (32.0 * 3.14159265358979323846), 1.0 / 3.0);
     const double sigma2 = -(radius * radius) / (2.0 * std::log(0.1));
     const float inv2s2 = (float)(1.0 / (2.0 * sigma2));
     // point bins

@@ -49,7 +49,7 @@ class ColorRamp:
     @classmethod
     def parse(cls, spec: str) -> "ColorRamp":
         """-tempColorRamp syntax (src/main.cc:280-319)."""
-        lib = _capi.load()
+        lib = _capi.load_host()
         s = ShaderC()
         _check(lib, None, lib.lg_parse_color_ramp(spec.encode(), C.byref(s)))
         return cls([s.ramp_pos[k] for k in range(s.ramp_n)],
@@ -95,7 +95,7 @@ class Shader:
         return tuple(-(s + a) for s, a in zip(self.scattering, self.absorption))
 
     def to_c(self) -> ShaderC:
-        lib = _capi.load()
+        lib = _capi.load_host()
         s = ShaderC()
         lib.lg_shader_default(C.byref(s))
         s.density_scale = self.density_scale
@@ -139,7 +139,7 @@ class Light:
 
     @classmethod
     def parse(cls, spec: str) -> "Light":
-        lib = _capi.load()
+        lib = _capi.load_host()
         c = LightC()
         st = lib.lg_parse_light(spec.encode(), C.byref(c))
         if st != _capi.LG_OK:

@@ -48,7 +48,7 @@ class Scene:
 
 
 def volume(kind: int, res: int, octaves: int, seed: int, scale: float = 1.0, mask=None) -> np.ndarray:
-    lib = _capi.load()
+    lib = _capi.load_host()
     out = np.empty((res, res, res), np.float32)
     m = None if mask is None else np.ascontiguousarray(mask, np.float32)
     lib.lgs_volume(kind, res, octaves, seed, scale, _capi.ptr(m), _capi.ptr(out))
@@ -56,7 +56,7 @@ def volume(kind: int, res: int, octaves: int, seed: int, scale: float = 1.0, mas
 
 
 def points(density: np.ndarray, voxel_size: float, n: int, seed: int) -> np.ndarray:
-    lib = _capi.load()
+    lib = _capi.load_host()
     res = density.shape[0]
     out = np.empty((n, 3), np.float32)
     got = lib.lgs_points(_capi.ptr(np.ascontiguousarray(density)), res, voxel_size, n, seed, 1e-3, n * 100000,
@@ -66,7 +66,7 @@ def points(density: np.ndarray, voxel_size: float, n: int, seed: int) -> np.ndar
 
 def envmap(w: int = 512, h: int = 256, elev: float = 30.0, azim: float = 60.0, sigma: float = 2.0,
            intensity: float = 50.0) -> np.ndarray:
-    lib = _capi.load()
+    lib = _capi.load_host()
     out = np.empty((h, w, 3), np.float32)
     lib.lgs_envmap(w, h, elev, azim, sigma, intensity, _capi.ptr(out))
     return out

@@ -13,6 +13,8 @@
 #include <vector>
 #include <climits>
 #include <random>
+#include <set>
+#include <tuple>
 
 namespace {
 
@@ -721,6 +723,97 @@ extern "C" void lgo_diffuse(int n, const double* T, const double* L, double* D) 
 // ---------------------------------------------------------------------------
 static int floor_div(int a, int b) { return (a >= 0) ? a / b : -((-a + b - 1) / b); }
 
+// points::computeVoxelSize(positions, pointsPerVoxel) as LightGraph::
+// buildVdbPointGrid calls it (src/LightGraph.h:713-714; identity transform,
+// five decimal places). OpenVDB is not under the reference tree and no version
+// is pinned; this restates its documented procedure (OpenVDB 7/8,
+// openvdb/points/PointConversion.h):
+//  * 0.1 for fewer than two points or coincident points;
+//  * target = max(1, n / pointsPerVoxel) voxels (integer division);
+//  * start from the points' bounding box: voxel = float(pow(volume / target,
+//    1/3)); a flat box uses maxExtent * nextExtent^2, a line maxExtent^3;
+//  * refine: count the distinct voxels the points fall in (cell-centred index
+//    round(p / voxel)), volume = float(voxel^3) * count; stop when the volume
+//    does not shrink, when the count stops growing, or when the new voxel is
+//    more than 0.9 of the last;
+//  * round the result to five decimal places (six, seven, ... if that gives
+//    zero): floor(v * 10^d + 0.5) / 10^d, stored as float.
+// Returned as the double the point grid's transform reports.
+namespace {
+bool voxel_from_volume(double volume, size_t target, float& voxel) {
+    const double vmin = 3e-15;  // ScaleMap's smallest voxel volume
+    const double fmax = (double)std::numeric_limits<float>::max();
+    const double vmax = fmax * fmax * fmax;
+    double vv = volume / (double)target;
+    bool ok = true;
+    if (vv < vmin) {
+        vv = vmin;
+        ok = false;
+    } else if (vv > vmax) {
+        vv = vmax;
+        ok = false;
+    }
+    voxel = (float)std::pow(vv, 1.0 / 3.0);
+    return ok;
+}
+}  // namespace
+
+extern "C" double lgo_point_voxel_size(int64_t n, const float* pts, int points_per_voxel) {
+    float voxel = 0.1f;
+    if (n <= 1 || points_per_voxel <= 0) return voxel;
+    size_t target = (size_t)n / (size_t)points_per_voxel;
+    if (target == 0) target = 1;
+    double lo[3], hi[3];
+    for (int a = 0; a < 3; ++a) lo[a] = hi[a] = (double)pts[a];
+    for (int64_t i = 1; i < n; ++i)
+        for (int a = 0; a < 3; ++a) {
+            lo[a] = std::min(lo[a], (double)pts[3 * i + a]);
+            hi[a] = std::max(hi[a], (double)pts[3 * i + a]);
+        }
+    if (lo[0] == hi[0] && lo[1] == hi[1] && lo[2] == hi[2]) return voxel;
+    double ext[3] = {hi[0] - lo[0], hi[1] - lo[1], hi[2] - lo[2]};
+    double volume = ext[0] * ext[1] * ext[2];
+    if (std::fabs(volume) <= 1e-15) {
+        std::sort(ext, ext + 3);  // ascending: ext[2] largest
+        if (std::fabs(ext[1]) <= 1e-15)
+            volume = ext[2] * ext[2] * ext[2];
+        else
+            volume = ext[2] * ext[1] * ext[1];
+    }
+    double prev_volume = volume;
+    if (!voxel_from_volume(volume, target, voxel)) return voxel;
+    size_t prev_count = 0, count = 1;
+    while (count > prev_count) {
+        const double inv = 1.0 / (double)voxel;
+        std::set<std::tuple<int, int, int>> cells;
+        for (int64_t i = 0; i < n; ++i) {
+            int c[3];
+            for (int a = 0; a < 3; ++a) c[a] = (int)std::floor((double)pts[3 * i + a] * inv + 0.5);
+            cells.insert(std::make_tuple(c[0], c[1], c[2]));
+        }
+        prev_count = count;
+        count = cells.size();
+        const float cube = voxel * voxel * voxel;
+        volume = (double)(cube * (float)count);
+        if (volume >= prev_volume) break;
+        prev_volume = volume;
+        const float prev_voxel = voxel;
+        if (!voxel_from_volume(volume, target, voxel)) {
+            voxel = prev_voxel;
+            break;
+        }
+        if (voxel / prev_voxel > 0.9f) break;
+    }
+    float out = voxel;
+    for (int d = 5; d < 11; ++d) {
+        double tenth = 1.0;
+        for (int k = 0; k < d; ++k) tenth *= 10.0;
+        out = (float)(std::floor((double)voxel * tenth + 0.5) / tenth);
+        if (out != 0.0f) break;
+    }
+    return (double)out;
+}
+
 extern "C" double lgo_splat(const lgo_grid* dens, int f, int64_t np, const float* pts, const double* D,
                             double hp, double K, int32_t out_lo[3], int32_t out_dims[3], double* out) {
     Grid g;
@@ -765,7 +858,9 @@ extern "C" double lgo_splat(const lgo_grid* dens, int f, int64_t np, const float
                 act[((size_t)cz * dims[1] + cy) * dims[0] + cx] = any;
             }
     const double H = g.h * f;
-    const double radius = std::cbrt((3.0 * K * hp * hp * hp) / (32.0 * kPi));
+    // src/ScatterGrid.h:69-75: voxelSizeCubed first, then the cube root by pow
+    const double hp3 = hp * hp * hp;
+    const double radius = std::pow((3.0 * K * hp3) / (32.0 * kPi), 1.0 / 3.0);
     const double sigma2 = -(radius * radius) / (2.0 * std::log(0.1));
     // uniform cells of edge `radius` over the points' bbox for the search
     double plo[3] = {0, 0, 0}, phi[3] = {0, 0, 0};
@@ -910,11 +1005,16 @@ struct ScatterLookup {
 
 }  // namespace
 
-extern "C" void lgo_render(const lgo_grid* dens, const lgo_grid* temp, const lg_shader* sh, const lg_settings* st,
-                           const lg_light* lights, int n_lights, const lgo_env* env, const lg_camera* cam_in,
-                           const int32_t sg_lo[3], const int32_t sg_dims[3], double sg_h, const float* sg_values,
-                           int row0, int row1, float* rgba, float* direct, float* scatter, float* emission,
-                           uint64_t* counters) {
+// VolumeRender::operator() over the pixels of the listed image rows, in
+// parallel over pixels (the reference's TBB body runs over rows of a full
+// frame; a pixel-level schedule keeps every thread busy when only a few rows
+// are rendered). Results do not depend on the schedule: every random draw is
+// keyed by pixel and sample.
+static void render_rows(const lgo_grid* dens, const lgo_grid* temp, const lg_shader* sh, const lg_settings* st,
+                        const lg_light* lights, int n_lights, const lgo_env* env, const lg_camera* cam_in,
+                        const int32_t sg_lo[3], const int32_t sg_dims[3], double sg_h, const float* sg_values,
+                        const int32_t* rows, int n_rows, float* rgba, float* direct, float* scatter,
+                        float* emission, uint64_t* counters) {
     Grid g, tg;
     g.init(dens);
     if (temp) tg.init(temp);
@@ -933,9 +1033,11 @@ extern "C" void lgo_render(const lgo_grid* dens, const lgo_grid* temp, const lg_
     const double step0 = st->step[0], step1 = st->step[1], cutoff = st->cutoff, jit = 0.5;
     const int spp = cam_in->samples;
     uint64_t cnt_p = 0, cnt_s = 0;
-#pragma omp parallel for schedule(dynamic, 1) reduction(+ : cnt_p, cnt_s)
-    for (int j = row0; j < row1; ++j) {
-        for (int i = 0; i < cam.w; ++i) {
+    const int64_t n_pix = (int64_t)n_rows * cam.w;
+#pragma omp parallel for schedule(dynamic, 8) reduction(+ : cnt_p, cnt_s)
+    for (int64_t q = 0; q < n_pix; ++q) {
+        {
+            const int j = rows[q / cam.w], i = (int)(q % cam.w);
             const int64_t pix = (int64_t)j * cam.w + i;
             V3 pTransAA(0.0), pLumiAA(0.0), dirAA(0.0), scatAA(0.0), emitAA(0.0);
             const double ratioAA = 1.0 / (double)spp;
@@ -1055,6 +1157,50 @@ extern "C" void lgo_render(const lgo_grid* dens, const lgo_grid* temp, const lg_
     if (counters) {
         counters[0] = cnt_p;
         counters[1] = cnt_s;
+    }
+}
+
+extern "C" void lgo_render(const lgo_grid* dens, const lgo_grid* temp, const lg_shader* sh, const lg_settings* st,
+                           const lg_light* lights, int n_lights, const lgo_env* env, const lg_camera* cam,
+                           const int32_t sg_lo[3], const int32_t sg_dims[3], double sg_h, const float* sg_values,
+                           int row0, int row1, float* rgba, float* direct, float* scatter, float* emission,
+                           uint64_t* counters) {
+    std::vector<int32_t> rows;
+    for (int j = std::max(row0, 0); j < row1 && j < cam->height; ++j) rows.push_back(j);
+    render_rows(dens, temp, sh, st, lights, n_lights, env, cam, sg_lo, sg_dims, sg_h, sg_values, rows.data(),
+                (int)rows.size(), rgba, direct, scatter, emission, counters);
+}
+
+extern "C" void lgo_render_rows(const lgo_grid* dens, const lgo_grid* temp, const lg_shader* sh,
+                                const lg_settings* st, const lg_light* lights, int n_lights, const lgo_env* env,
+                                const lg_camera* cam, const int32_t sg_lo[3], const int32_t sg_dims[3], double sg_h,
+                                const float* sg_values, const int32_t* rows, int n_rows, float* rgba, float* direct,
+                                float* scatter, float* emission, uint64_t* counters) {
+    render_rows(dens, temp, sh, st, lights, n_lights, env, cam, sg_lo, sg_dims, sg_h, sg_values, rows, n_rows, rgba,
+                direct, scatter, emission, counters);
+}
+
+extern "C" void lgo_fw_minplus_f32_rounds(int n, float* S, int k0, int k1) {
+    for (int k = k0; k < k1 && k < n; ++k) {
+#pragma omp parallel for schedule(static)
+        for (int i = 0; i < n; ++i) {
+            const float sik = S[(size_t)i * n + k];
+            if (!(sik < std::numeric_limits<float>::infinity())) continue;
+            float* si = S + (size_t)i * n;
+            const float* sk = S + (size_t)k * n;
+            for (int j = 0; j < n; ++j) {
+                const float v = sik + sk[j];
+                if (v < si[j]) si[j] = v;
+            }
+        }
+    }
+}
+
+extern "C" void lgo_transmittance_of(int64_t count, const double* S, const double ext[3], double* T) {
+#pragma omp parallel for schedule(static)
+    for (int64_t e = 0; e < count; ++e) {
+        const double v = S[e];
+        for (int c = 0; c < 3; ++c) T[3 * e + c] = v < std::numeric_limits<double>::infinity() ? std::exp(ext[c] * v) : 0.0;
     }
 }
 

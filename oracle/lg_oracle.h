@@ -14,6 +14,7 @@
  *   LightGraph::floydAlgo          src/LightGraph.h:512-542   lgo_fw_maxtimes
  *   LightGraph::computeLighting    src/LightGraph.h:427-505   lgo_vertex_light
  *   LightGraph::diffuseLight       src/LightGraph.h:554-587   lgo_diffuse
+ *   LightGraph::buildVdbPointGrid  src/LightGraph.h:706-755   lgo_point_voxel_size
  *   ScatterGrid::buildScatterGrid  src/ScatterGrid.h:105-144  lgo_splat
  *   ScatterGrid::operator()        src/ScatterGrid.h:61-98    lgo_splat
  *   VolumeRender::operator()       src/Renderer.h:505-693     lgo_render
@@ -32,7 +33,8 @@
  *   Ray::clip to the active leaf bbox padded by one voxel,
  *   VolumeHDDA spans = maximal runs of leaf nodes along the index ray,
  *   GridTransformer + dilateActiveValues topology of the scatter grid,
- *   PointIndexGrid radial search (points with |x - p| < r).
+ *   PointIndexGrid radial search (points with |x - p| < r),
+ *   points::computeVoxelSize (bbox estimate refined on voxel occupancy).
  */
 #ifndef LG_ORACLE_H_
 #define LG_ORACLE_H_
@@ -85,6 +87,12 @@ void lgo_vertex_light(const lgo_grid* dens, const lgo_grid* temp, const lg_shade
  * D_i = sum_j L_j * P_ij. */
 void lgo_diffuse(int n, const double* T, const double* L, double* D);
 
+/* points::computeVoxelSize(positions, points_per_voxel) with OpenVDB's
+ * defaults (identity transform, five decimal places), as
+ * LightGraph::buildVdbPointGrid calls it (src/LightGraph.h:713-714): the
+ * point index grid's voxel size, which sets the splat radius. */
+double lgo_point_voxel_size(int64_t n, const float* pts, int points_per_voxel);
+
 /* Scatter-grid topology + splat. Output box: lo = floor(origin/f) - 1, dims
  * from that to floor((origin+dims-1)/f) + 1 (same box as the GPU).
  * out: dims product x 3 doubles. Returns the splat radius. */
@@ -100,6 +108,23 @@ void lgo_render(const lgo_grid* dens, const lgo_grid* temp, const lg_shader* sh,
                 const int32_t sg_lo[3], const int32_t sg_dims[3], double sg_h, const float* sg_values,
                 int row0, int row1, float* rgba, float* direct, float* scatter, float* emission,
                 uint64_t* counters);
+
+/* lgo_render over a list of image rows (any order), in parallel over their
+ * pixels: the bounded sample of a frame that the CPU baseline times. */
+void lgo_render_rows(const lgo_grid* dens, const lgo_grid* temp, const lg_shader* sh, const lg_settings* st,
+                     const lg_light* lights, int n_lights, const lgo_env* env, const lg_camera* cam,
+                     const int32_t sg_lo[3], const int32_t sg_dims[3], double sg_h, const float* sg_values,
+                     const int32_t* rows, int n_rows, float* rgba, float* direct, float* scatter, float* emission,
+                     uint64_t* counters);
+
+/* Rounds k0 <= k < k1 of FP32 min-plus FW (rows with S_ik = +inf skipped).
+ * It reaches the same sparsity pattern as floydAlgo after the same rounds, so
+ * the CPU baseline uses it to bring the matrix to a sampled round cheaply. */
+void lgo_fw_minplus_f32_rounds(int n, float* S, int k0, int k1);
+
+/* T[e][c] = exp(ext[c] * S[e]) (0 where S is +inf): the RGB transmittance of
+ * an optical-depth matrix, as floydAlgo holds it. */
+void lgo_transmittance_of(int64_t count, const double* S, const double ext[3], double* T);
 
 /* The env map's importance-sampling CDFs as EnvLight builds them (FP64 prefix
  * sums stored as FP32): cond_func h*w, cond_cdf h*(w+1), cond_int h,

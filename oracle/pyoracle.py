@@ -55,6 +55,8 @@ def load() -> C.CDLL:
     lib.lgo_vertex_light.argtypes = [C.POINTER(OGrid), C.POINTER(OGrid), C.POINTER(ShaderC), C.POINTER(SettingsC),
                                      C.POINTER(LightC), C.c_int, C.POINTER(OEnv), C.c_int, P, C.c_int, P]
     lib.lgo_diffuse.argtypes = [C.c_int, P, P, P]
+    lib.lgo_point_voxel_size.restype = C.c_double
+    lib.lgo_point_voxel_size.argtypes = [C.c_int64, P, C.c_int]
     lib.lgo_splat.restype = C.c_double
     lib.lgo_splat.argtypes = [C.POINTER(OGrid), C.c_int, C.c_int64, P, P, C.c_double, C.c_double, P, P, P]
     lib.lgo_render.argtypes = [C.POINTER(OGrid), C.POINTER(OGrid), C.POINTER(ShaderC), C.POINTER(SettingsC),
@@ -139,8 +141,13 @@ class Oracle:
                              _p(np.ascontiguousarray(L, np.float64)), _p(D))
         return D
 
-    def splat(self, pts, D, point_voxel_size, factor=None, kernel_points=None):
+    def splat(self, pts, D, point_voxel_size=None, factor=None, kernel_points=None):
+        """ScatterGrid topology and splat of the points' radiance D. The point
+        index's voxel size is the oracle's own computeVoxelSize of the points
+        unless given."""
         pts = np.ascontiguousarray(pts, np.float32)
+        if point_voxel_size is None:
+            point_voxel_size = point_voxel_size_of(pts)
         D = np.ascontiguousarray(D, np.float64)
         f = factor or self.opts.scatterGridResFactor
         K = kernel_points if kernel_points is not None else self.opts.ptsPerKernel * self.opts.iter
@@ -208,6 +215,12 @@ def randgen_draws(seed, n):
     raw = np.zeros(n, np.uint32)
     load().lgo_randgen_draws(seed, n, _p(out), _p(raw))
     return out, raw
+
+
+def point_voxel_size_of(pts, points_per_voxel=8):
+    """lgo_point_voxel_size: computeVoxelSize of an (n, 3) float32 point set."""
+    pts = np.ascontiguousarray(pts, np.float32)
+    return load().lgo_point_voxel_size(len(pts), _p(pts), points_per_voxel)
 
 
 def diffuse(T_solved, L):

@@ -23,7 +23,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 
-from lightgraph_gb300 import _capi, scenes  # noqa: E402
+from lightgraph_gb300 import scenes  # noqa: E402
 from oracle import pyoracle as po  # noqa: E402
 
 
@@ -46,7 +46,7 @@ def compute(name: str) -> dict:
     Smin = po.fw_minplus_f64(S)
     L = o.vertex_light(pts)
     D = o.diffuse(Tsol, L)
-    hp = _capi.load().lg_point_voxel_size(len(pts), pts.ctypes.data, 8)
+    hp = po.point_voxel_size_of(pts)
     lo, dims, sg, radius = o.splat(pts, D, hp)
     films = o.render((lo, dims, sg))
     return {"points": pts, "radius_sq": np.float32(sc.radius_sq[0]), "adj": adj, "n_edges": np.int64(ne),

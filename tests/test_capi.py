@@ -24,13 +24,26 @@ def declared_functions():
 
 
 def test_exports_every_declared_symbol():
-    lib = _capi.load()
+    """Every function the headers declare is exported by the library whose
+    ctypes table lists it: the CUDA library or the host-only helper library
+    (which has no CUDA code, so a CPU-only caller can build scenes with it)."""
+    lib, host = _capi.load(), _capi.load_host()
     names = declared_functions()
     assert len(names) > 30
-    missing = [n for n in sorted(names) if not hasattr(lib, n)]
+    tables = set(_capi.SIGNATURES) | set(_capi.HOST_SIGNATURES)
+    assert names <= tables, sorted(names - tables)
+    assert not set(_capi.SIGNATURES) & set(_capi.HOST_SIGNATURES)
+    missing = [n for n in sorted(names) if not hasattr(lib if n in _capi.SIGNATURES else host, n)]
     assert not missing, missing
-    # and the ctypes table covers them all
-    assert names <= set(_capi.SIGNATURES), sorted(names - set(_capi.SIGNATURES))
+
+
+def test_host_library_has_no_cuda_dependency():
+    """The host helper library links no CUDA runtime, so the CPU baseline can
+    build its scenes without mapping the CUDA library."""
+    import subprocess
+    from lightgraph_gb300 import build
+    out = subprocess.run(["ldd", build.host_lib_path()], capture_output=True, text=True).stdout
+    assert "cuda" not in out.lower() and "lightgraph_gb300" not in out
 
 
 def test_version_and_no_device_is_reported():
@@ -116,16 +129,6 @@ def test_parse_color_ramp():
     assert r.positions == [0.0, 0.33, 0.66, 1.0]
     assert r.colors[1] == [1.0, 0.076, 0.0]
     assert (r.in_, r.out) == (0.35, 1.5)
-
-
-def test_point_voxel_size_estimate():
-    lib = _capi.load()
-    rng = np.random.default_rng(0)
-    pts = rng.random((8000, 3)).astype(np.float32)
-    h = lib.lg_point_voxel_size(len(pts), pts.ctypes.data, 8)
-    # ~8 points per h^3 over a unit-ish box
-    assert h == pytest.approx(np.cbrt(np.prod(pts.max(0) - pts.min(0)) / 1000), rel=1e-6)
-    assert lib.lg_point_voxel_size(1, pts.ctypes.data, 8) == 0.1
 
 
 def test_scene_generator_is_deterministic():

@@ -11,7 +11,7 @@ from lightgraph_gb300 import _capi
 
 
 def write(path, w, h, planes: dict):
-    lib = _capi.load()
+    lib = _capi.load_host()
     names = (C.c_char_p * len(planes))(*[k.encode() for k in planes])
     arrs = [np.ascontiguousarray(v, np.float32) for v in planes.values()]
     ptrs = (C.c_void_p * len(arrs))(*[a.ctypes.data for a in arrs])
@@ -19,7 +19,7 @@ def write(path, w, h, planes: dict):
 
 
 def read(path):
-    lib = _capi.load()
+    lib = _capi.load_host()
     w, h = C.c_int32(), C.c_int32()
     assert lib.lg_read_exr_rgba(str(path).encode(), C.byref(w), C.byref(h), None) == 0
     out = np.zeros((h.value, w.value, 4), np.float32)

@@ -169,8 +169,7 @@ def test_splat_and_render(gpu_ctx, small_scene, small_oracle, small_solved):
     sc, o = small_scene, small_oracle
     gpu_ctx.splat()
     lo, dims, sg = gpu_ctx.scatter_grid()
-    hp = gpu_ctx.lib.lg_point_voxel_size(len(sc.points[0]), sc.points[0].ctypes.data, 8)
-    lo_r, dims_r, sg_ref, _ = o.splat(sc.points[0], small_solved["D_gpu"].astype(np.float64), hp)
+    lo_r, dims_r, sg_ref, _ = o.splat(sc.points[0], small_solved["D_gpu"].astype(np.float64))
     assert tuple(lo) == tuple(lo_r) and tuple(dims) == tuple(dims_r)
     assert np.allclose(sg, sg_ref, rtol=1e-4, atol=1e-6)
     films = gpu_ctx.render(sc.opts)
@@ -191,8 +190,7 @@ def test_full_frame_vs_fp64_oracle(gpu_ctx, small_scene, small_oracle):
     Tsol = o.fw_maxtimes(T)
     L = o.vertex_light(sc.points[0])
     D = o.diffuse(Tsol, L)
-    hp = gpu_ctx.lib.lg_point_voxel_size(len(sc.points[0]), sc.points[0].ctypes.data, 8)
-    lo, dims, sg, _ = o.splat(sc.points[0], D, hp)
+    lo, dims, sg, _ = o.splat(sc.points[0], D)
     ref = o.render((lo, dims, sg))
     for k, name in enumerate(["rgba", "direct", "scatter", "emission"]):
         e = rel_rmse(getattr(films, name), ref[k])
@@ -219,8 +217,7 @@ def test_tiny_env_maps_vs_fp64_oracle(gpu_ctx, wh):
     T, _ = o.march_edges(sc.points[0], adj)
     L = o.vertex_light(sc.points[0])
     D = o.diffuse(o.fw_maxtimes(T), L)
-    hp = gpu_ctx.lib.lg_point_voxel_size(len(sc.points[0]), sc.points[0].ctypes.data, 8)
-    lo, dims, sg, _ = o.splat(sc.points[0], D, hp)
+    lo, dims, sg, _ = o.splat(sc.points[0], D)
     ref = o.render((lo, dims, sg))
     for k, name in enumerate(["rgba", "direct", "scatter", "emission"]):
         e = rel_rmse(getattr(films, name), ref[k])
