@@ -62,6 +62,9 @@ def load() -> C.CDLL:
     lib.lgo_render.argtypes = [C.POINTER(OGrid), C.POINTER(OGrid), C.POINTER(ShaderC), C.POINTER(SettingsC),
                                C.POINTER(LightC), C.c_int, C.POINTER(OEnv), C.POINTER(CameraC), P, P, C.c_double, P,
                                C.c_int, C.c_int, P, P, P, P, P]
+    lib.lgo_render_rows.argtypes = [C.POINTER(OGrid), C.POINTER(OGrid), C.POINTER(ShaderC), C.POINTER(SettingsC),
+                                    C.POINTER(LightC), C.c_int, C.POINTER(OEnv), C.POINTER(CameraC), P, P,
+                                    C.c_double, P, P, C.c_int, P, P, P, P, P]
     lib.lgo_env_cdf.argtypes = [C.POINTER(OEnv), P, P, P, P, P, P]
     lib.lgo_threads.restype = C.c_int
     lib.lgo_scatter_points.argtypes = [C.POINTER(OGrid), C.c_void_p, C.c_int, C.c_int, P, P, P]
@@ -165,10 +168,17 @@ class Oracle:
         return tuple(lo), tuple(dims), out, r
 
     def render(self, sg=None, rows=None, counters=False):
-        """sg = (lo, dims, values (z,y,x,3)) of the scatter grid, or None."""
+        """sg = (lo, dims, values (z,y,x,3)) of the scatter grid, or None.
+        rows: None (the whole image), a (first, end) pair, or a list of row
+        indices (only those rows of the films are written)."""
         cam = self.opts.camera_c()
         W, H = self.opts.width, self.opts.height
-        r0, r1 = (0, H) if rows is None else rows
+        row_list = None
+        if rows is not None and not (isinstance(rows, tuple) and len(rows) == 2):
+            row_list = np.ascontiguousarray(rows, np.int32)
+            r0 = r1 = 0
+        else:
+            r0, r1 = (0, H) if rows is None else rows
         films = [np.zeros((H, W, 4), np.float32) for _ in range(4)]
         cnt = np.zeros(2, np.uint64)
         if sg is not None:
@@ -178,10 +188,13 @@ class Oracle:
             sg_h = self.dens.desc.voxel_size * self.opts.scatterGridResFactor
         else:
             vals32, lo_c, dims_c, sg_h = None, None, None, 1.0
-        self.lib.lgo_render(C.byref(self.dens), C.byref(self.temp) if self.temp else None, C.byref(self.shader),
-                            C.byref(self.settings), self.lights, self.n_lights,
-                            C.byref(self.env) if self.env else None, C.byref(cam), lo_c, dims_c, sg_h, _p(vals32),
-                            r0, r1, *[_p(f) for f in films], _p(cnt))
+        args = (C.byref(self.dens), C.byref(self.temp) if self.temp else None, C.byref(self.shader),
+                C.byref(self.settings), self.lights, self.n_lights, C.byref(self.env) if self.env else None,
+                C.byref(cam), lo_c, dims_c, sg_h, _p(vals32))
+        if row_list is None:
+            self.lib.lgo_render(*args, r0, r1, *[_p(f) for f in films], _p(cnt))
+        else:
+            self.lib.lgo_render_rows(*args, _p(row_list), len(row_list), *[_p(f) for f in films], _p(cnt))
         return (films, cnt) if counters else films
 
     def env_cdf(self):
@@ -230,6 +243,35 @@ def diffuse(T_solved, L):
     load().lgo_diffuse(n, _p(np.ascontiguousarray(T_solved, np.float64)), _p(np.ascontiguousarray(L, np.float64)),
                        _p(D))
     return D
+
+
+def apsp_dijkstra_f64(S, sources=None):
+    """Exact FP64 shortest path lengths of an optical-depth matrix S (+inf =
+    no edge) by Dijkstra (scipy), from every vertex or from `sources`;
+    diagonal 0. The min-plus form of floydAlgo's solution at sizes where the
+    O(n^3) loops are too slow for a test (max-times FW = min-plus on
+    -ln T, checked in tests/test_oracle.py)."""
+    from scipy.sparse import csr_matrix
+    from scipy.sparse.csgraph import dijkstra
+    S = np.asarray(S, np.float64)
+    fin = np.isfinite(S)
+    np.fill_diagonal(fin, False)
+    i, j = np.nonzero(fin)
+    # explicit zeros are edges for scipy only when stored; keep every edge > 0
+    w = np.maximum(S[i, j], np.finfo(np.float64).tiny)
+    g = csr_matrix((w, (i, j)), shape=S.shape)
+    return dijkstra(g, directed=True, indices=sources)
+
+
+def transmittance_of(dist, extinction):
+    """RGB path transmittance exp(extinction_c * dist) with diagonal 1 (the
+    matrix floydAlgo leaves for diffuseLight)."""
+    n = dist.shape[0]
+    a = np.asarray(extinction, np.float64)
+    T = np.exp(a[None, None, :] * np.asarray(dist, np.float64)[:, :, None])
+    idx = np.arange(n)
+    T[idx, idx, :] = 1.0
+    return T
 
 
 def fw_minplus_f32(S):
