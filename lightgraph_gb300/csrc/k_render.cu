@@ -64,6 +64,15 @@ __device__ __forceinline__ void sample_scatter(const DevScatterGrid& sg, float w
 
 __device__ __forceinline__ float jitter_step(float step, float u) { return step * (1.f + (u - 0.5f) * 0.5f); }
 
+// jitter_step with u = (x >> 9) / 2^23 from a step-jitter stream state:
+// 1 + u is built from the bits directly, so (u - 0.5) = (1 + u) - 1.5 exactly.
+__device__ __forceinline__ float jitter_step_bits(float step, uint32_t x) {
+    const float f = __uint_as_float(0x3F800000u | (x >> 9));
+    // rounding spelled out (no contraction into the caller's additions): the
+    // two primary passes must step identically
+    return __fmul_rn(step, __fmaf_rn(__fsub_rn(f, 1.5f), 0.5f, 1.f));
+}
+
 // Primary ray of pixel (i, j), sample s: PerspectiveCamera::getRay with the
 // offset 0.5 + (u - 0.5) in each axis, mapped to the density's index space.
 __device__ __forceinline__ bool primary_ray(const DevScene& sc, const DevCamera& cam, int i, int j, Stream stream,
@@ -119,6 +128,7 @@ __device__ __forceinline__ uint32_t primary_sample(const DevScene& sc, const Dev
         dda_init(dda, pr, G);
         float ta, tb;
         uint32_t span_ord = 0, n_iter = 0;
+        uint32_t jit = step_seed_primary(stream);
         bool pdrop = false;
         int64_t base = kWrite ? offsets[ps] : 0;
         while (!pdrop && next_span(G, dda, ta, tb)) {
@@ -127,10 +137,11 @@ __device__ __forceinline__ uint32_t primary_sample(const DevScene& sc, const Dev
             // (pT + pStep > pT stops a march whose step underflows against pT)
             for (float pT = step0 * ceilf(ta / step0); pT <= tb && pT + pStep > pT;) {
                 const uint32_t n = n_iter++;
+                jit = step_next(jit);
                 ++n_primary;
                 const float p[3] = {__fmaf_rn(pT, pr.d[0], pr.e[0]), __fmaf_rn(pT, pr.d[1], pr.e[1]),
                                     __fmaf_rn(pT, pr.d[2], pr.e[2])};
-                const float rho = fminf(sample_index_t<DT>(G, p[0], p[1], p[2]) * sh.dS, sh.dMax);
+                const float rho = fminf(sample_span_t<DT>(G, p[0], p[1], p[2]) * sh.dS, sh.dMax);
                 if (rho < cutoff) { pT += pStep; continue; }
                 float omdT[3], dT[3];
 #pragma unroll
@@ -169,7 +180,7 @@ __device__ __forceinline__ uint32_t primary_sample(const DevScene& sc, const Dev
                     pdrop = true;
                     break;
                 }
-                pStep = jitter_step(step0, draw(stream, kTagPrimaryStep | n));
+                pStep = jitter_step_bits(step0, jit);
                 pT += pStep;
             }
         }
@@ -366,6 +377,7 @@ __global__ void __launch_bounds__(128, 8) k_shadow(DevScene sc, const ShadowTask
             dda_init(sd, srr, G);
             float sa, sb, tau = 0.f;
             uint32_t sspan = 0, siter = 0;
+            uint32_t jit = step_seed_shadow(sub);
             bool sdrop = false;
             while (!sdrop && next_span(G, sd, sa, sb)) {
                 float sStep = jitter_step(step1, draw_sub(sub, kTagShadowSpan | sspan));
@@ -374,14 +386,15 @@ __global__ void __launch_bounds__(128, 8) k_shadow(DevScene sc, const ShadowTask
                 // absorbed at sb, sT grows on every iteration up to sb
                 if (!(sb + 0.75f * step1 > sb)) continue;
                 for (float sT = step1 * ceilf(sa / step1); sT <= sb;) {
-                    const uint32_t q = siter++;
-                    const float rs = fminf(sample_index_t<DT>(G, srr.e[0] + sT * srr.d[0], srr.e[1] + sT * srr.d[1],
-                                                              srr.e[2] + sT * srr.d[2]) * scale,
+                    ++siter;
+                    jit = step_next(jit);
+                    const float rs = fminf(sample_span_t<DT>(G, srr.e[0] + sT * srr.d[0], srr.e[1] + sT * srr.d[1],
+                                                             srr.e[2] + sT * srr.d[2]) * scale,
                                            sh.dMax);
                     // a sample below the cutoff adds nothing and keeps its
                     // step (no re-jitter); branch-free, the warp stays converged
                     const bool take = rs >= cutoff;
-                    const float next = jitter_step(step1, draw_sub(sub, kTagShadowStep | q));
+                    const float next = jitter_step_bits(step1, jit);
                     tau = take ? fmaf(rs, sStep, tau) : tau;
                     if (tau > sh.tau_drop) { sdrop = true; break; }
                     sStep = take ? next : sStep;

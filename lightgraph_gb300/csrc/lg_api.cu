@@ -331,8 +331,14 @@ lg_status Ctx::upload_grid(int which, const lg_grid_desc* desc, const float* val
         g.vlo[a] = g.blo[a] * 8;
         g.vn[a] = (uint32_t)g.nb[a] * 8u;
     }
-    g.sy = (uint32_t)g.nb[0] * 512u;
-    g.sz = (uint32_t)g.nb[0] * (uint32_t)g.nb[1] * 512u;
+    g.sz = g.vn[0] * g.vn[1];
+    g.rec_last = g.sz * g.vn[2] - 1u;
+    {
+        // span_cell adds the three floor_bits words (floor + 0x4B400000)
+        const uint32_t bias = 0x4B400000u;
+        g.rec_off = 0u - ((uint32_t)g.vlo[0] + bias) - ((uint32_t)g.vlo[1] + bias) * g.vn[0] -
+                    ((uint32_t)g.vlo[2] + bias) * g.sz;
+    }
     const int64_t nvox = (int64_t)desc->dims[0] * desc->dims[1] * desc->dims[2];
     const int64_t nbt = (int64_t)g.nb[0] * g.nb[1] * g.nb[2];
     const size_t rec = (size_t)cell_record_bytes(dtype);

@@ -19,16 +19,17 @@ constexpr int kMaxRamp = 16;
 constexpr float kDelta = 1e-9f;
 
 // ---------------------------------------------------------------------------
-// Grid: one record per voxel cell (x, y, z) of a dense box that is tiled into
-// 8^3 bricks (x fastest inside a brick, bricks x fastest in the box) with one
-// brick of zero padding on every side. A cell's record holds the eight voxel
-// values of its trilinear footprint, v(x + a, y + b, z + c) at index
-// a + 2b + 4c, so one sample is one aligned 32-byte (FP32) or 16-byte
-// (FP16/BF16) load instead of eight gathers. Voxels outside the box read the
-// background value 0. The box's first cell lies in the padding corner brick,
-// so its eight values are 0; samplers redirect cells outside the box to it.
-// Records cost 8x the voxel storage, which HBM holds easily (a 512^3 box is
-// 4.6 GB in FP32); what matters for the marches is one L1 request per sample.
+// Grid: one record per voxel cell (x, y, z) of a dense box that covers the
+// grid's 8^3 leaf bricks plus one brick of zero padding on every side, x
+// fastest, then y, then z. A cell's record holds the eight voxel values of its
+// trilinear footprint, v(x + a, y + b, z + c) at index a + 2b + 4c, so one
+// sample is one aligned 32-byte (FP32) or 16-byte (FP16/BF16) load instead of
+// eight gathers, and a 128-byte line holds four neighbouring cells along x.
+// Voxels outside the box read the background value 0. The box's first and
+// last cells lie in padding corners, so their eight values are 0; the checked
+// sampler redirects cells outside the box to the first one. Records cost 8x
+// the voxel storage, which HBM holds easily (a 512^3 box is 4.7 GB in FP32);
+// what matters for the marches is one L1 request per sample.
 // ---------------------------------------------------------------------------
 struct DevGrid {
     const void* data = nullptr;
@@ -44,7 +45,9 @@ struct DevGrid {
     float bbmin[3] = {0.f, 0.f, 0.f};    // leaf bbox in index space (origin of min leaf)
     float bbmax[3] = {0.f, 0.f, 0.f};    // ... max leaf origin + 8
     int has_leaves = 0;
-    uint32_t sy = 0, sz = 0;             // record strides of one brick step in y and z
+    uint32_t sz = 0;                     // records per z slice (vn[0] * vn[1])
+    uint32_t rec_off = 0;                // record of cell (0, 0, 0): -(vlo . strides) mod 2^32
+    uint32_t rec_last = 0;               // last record (a padding cell)
     // The leaf bitmap covers the brick box plus a margin of one brick on
     // every side (bits 0), so a walker one cell off the box reads "no leaf"
     // without per-axis bounds checks: bit ((z + 1) * lby + y + 1) * lbx + x + 1
@@ -84,9 +87,35 @@ __device__ __forceinline__ void ld_cell(const void* data, uint32_t rec, float v[
 __device__ __forceinline__ uint32_t cell_record(const DevGrid& g, int ix, int iy, int iz) {
     const uint32_t rx = (uint32_t)(ix - g.vlo[0]), ry = (uint32_t)(iy - g.vlo[1]), rz = (uint32_t)(iz - g.vlo[2]);
     const bool in = rx < g.vn[0] && ry < g.vn[1] && rz < g.vn[2];
-    const uint32_t rec = (rx >> 3) * 512u + (ry >> 3) * g.sy + (rz >> 3) * g.sz +
-                         (((rz & 7u) << 6) | ((ry & 7u) << 3) | (rx & 7u));
+    const uint32_t rec = rx + ry * g.vn[0] + rz * g.sz;
     return in ? rec : 0u;
+}
+
+// Floor of an index-space coordinate (|p| < 2^22) without a float-to-int
+// conversion: adding 1.5 * 2^23 rounding down leaves floor(p) in the low
+// mantissa bits. Returns those bits (floor(p) + 0x4B400000) and floor(p) as
+// a float.
+__device__ __forceinline__ uint32_t floor_bits(float p, float& fl) {
+    const float r = __fadd_rd(p, 12582912.0f);
+    fl = __fsub_rn(r, 12582912.0f);
+    return __float_as_uint(r);
+}
+
+// Trilinear weights and record of the cell under an index-space position
+// inside a leaf span of g. Leaves lie inside the box with a brick of padding
+// around them, so such a cell is always inside the box and needs no per-axis
+// test; the index is clamped to the last (all-zero) record all the same, so
+// no position can address memory outside the records.
+__device__ __forceinline__ uint32_t span_cell(const DevGrid& g, float px, float py, float pz, float& wx,
+                                              float& wy, float& wz) {
+    float fx, fy, fz;
+    const uint32_t bx = floor_bits(px, fx), by = floor_bits(py, fy), bz = floor_bits(pz, fz);
+    wx = px - fx;
+    wy = py - fy;
+    wz = pz - fz;
+    // the 0x4B400000 bias of the three coordinates is folded into rec_off
+    const uint32_t rec = bx + by * g.vn[0] + bz * g.sz + g.rec_off;
+    return min(rec, g.rec_last);
 }
 
 // Trilinear sample at an index-space position for storage type DT: the eight
@@ -107,6 +136,22 @@ __device__ __forceinline__ float sample_index_t(const DevGrid& g, float px, floa
     const float2 z0 = __ffma2_rn(__fadd2_rn(b0, make_float2(-a0.x, -a0.y)), wz2, a0);
     const float2 z1 = __ffma2_rn(__fadd2_rn(b1, make_float2(-a1.x, -a1.y)), wz2, a1);
     // lanes (x0, x1) interpolated along y
+    const float2 y = __ffma2_rn(__fadd2_rn(z1, make_float2(-z0.x, -z0.y)), wy2, z0);
+    return fmaf(y.y - y.x, wx, y.x);
+}
+
+// sample_index_t for a position inside a leaf span of g (span_cell): the same
+// eight values and the same interpolation, without the box test.
+template <int DT>
+__device__ __forceinline__ float sample_span_t(const DevGrid& g, float px, float py, float pz) {
+    float wx, wy, wz;
+    float v[8];
+    ld_cell<DT>(g.data, span_cell(g, px, py, pz, wx, wy, wz), v);
+    const float2 wz2 = make_float2(wz, wz), wy2 = make_float2(wy, wy);
+    const float2 a0 = make_float2(v[0], v[1]), b0 = make_float2(v[4], v[5]);
+    const float2 a1 = make_float2(v[2], v[3]), b1 = make_float2(v[6], v[7]);
+    const float2 z0 = __ffma2_rn(__fadd2_rn(b0, make_float2(-a0.x, -a0.y)), wz2, a0);
+    const float2 z1 = __ffma2_rn(__fadd2_rn(b1, make_float2(-a1.x, -a1.y)), wz2, a1);
     const float2 y = __ffma2_rn(__fadd2_rn(z1, make_float2(-z0.x, -z0.y)), wy2, z0);
     return fmaf(y.y - y.x, wx, y.x);
 }

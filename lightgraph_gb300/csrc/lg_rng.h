@@ -89,4 +89,15 @@ LG_HD uint32_t shadow_key(Stream s, uint32_t n, uint32_t k, uint32_t ls) {
 
 LG_HD float draw_sub(uint32_t sub, uint32_t key) { return u01(hash32(sub ^ (key * 0x9E3779B9u))); }
 
+// Step-jitter stream of one march. The jitter drawn at loop iteration q is
+// the state after q + 1 steps of a full-period 32-bit linear congruential
+// generator seeded with a hash of the march's key. Every iteration advances
+// it, whether its sample is taken or not, so the number drawn at an
+// iteration does not depend on earlier skip decisions (which FP32 and FP64
+// can resolve differently). Its top 23 bits give u = (x >> 9) / 2^23.
+constexpr uint32_t kStepLcgA = 1664525u, kStepLcgC = 1013904223u;
+LG_HD uint32_t step_seed_primary(Stream s) { return hash32(s.a ^ (s.b + kTagPrimaryStep * 0x9E3779B9u)); }
+LG_HD uint32_t step_seed_shadow(uint32_t sub) { return hash32(sub ^ kTagShadowStep); }
+LG_HD uint32_t step_next(uint32_t x) { return x * kStepLcgA + kStepLcgC; }
+
 }  // namespace lg

@@ -70,6 +70,10 @@ uint32_t shadow_key(Stream s, uint32_t n, uint32_t k, uint32_t ls) {
     return hash32(s.a ^ hash32(s.b ^ (0x30000000u | (n & 0x0FFFFFFFu))) + k * 0x9E3779B9u + ls * 0x85EBCA6Bu);
 }
 float draw_sub(uint32_t sub, uint32_t key) { return u01(hash32(sub ^ (key * 0x9E3779B9u))); }
+// Step-jitter streams: a full-period 32-bit LCG advanced once per loop
+// iteration, seeded by a hash of the march's key; u = (x >> 9) / 2^23.
+uint32_t step_next(uint32_t x) { return x * 1664525u + 1013904223u; }
+double step_u(uint32_t x) { return (double)(x >> 9) * (1.0 / 8388608.0); }
 constexpr uint64_t kDomainPixel = 0x01ull << 56, kDomainVertex = 0x02ull << 56;
 constexpr uint32_t kTagJitterX = 0x00000000u, kTagJitterY = 0x00000001u, kTagPrimarySpan = 0x10000000u,
                    kTagPrimaryStep = 0x20000000u, kTagShadowSpan = 0x40000000u, kTagShadowStep = 0x50000000u,
@@ -1060,12 +1064,14 @@ static void render_rows(const lgo_grid* dens, const lgo_grid* temp, const lg_sha
                 SpanMarch pm(g, pr);
                 double pT0, pT1;
                 uint32_t span_ord = 0, n_iter = 0;
+                uint32_t pj = hash32(stream.a ^ (stream.b + kTagPrimaryStep * 0x9E3779B9u));
                 bool pDropout = false;
                 while (!pDropout && pm.next_span(pT0, pT1)) {
                     double pStep = step0 * (1.0 + ((double)draw(stream, kTagPrimarySpan | span_ord) - 0.5) * jit);
                     ++span_ord;
                     for (double pT = step0 * std::ceil(pT0 / step0); pT <= pT1; pT += pStep) {
                         const uint32_t n = n_iter++;
+                        pj = step_next(pj);
                         ++cnt_p;
                         const V3 pPos = g.index_to_world(pr.at(pT));
                         const double pDensity = std::min((double)g.sample_world(pPos) * sh->density_scale,
@@ -1096,12 +1102,14 @@ static void render_rows(const lgo_grid* dens, const lgo_grid* temp, const lg_sha
                                 SpanMarch sm(g, sr);
                                 double sT0, sT1;
                                 uint32_t sspan = 0, siter = 0;
+                                uint32_t sj = hash32(sub ^ kTagShadowStep);
                                 bool sDropout = false;
                                 while (!sDropout && sm.next_span(sT0, sT1)) {
                                     double sStep = step1 * (1.0 + ((double)draw_sub(sub, kTagShadowSpan | sspan) - 0.5) * jit);
                                     ++sspan;
                                     for (double sT = step1 * std::ceil(sT0 / step1); sT <= sT1; sT += sStep) {
-                                        const uint32_t q = siter++;
+                                        ++siter;
+                                        sj = step_next(sj);
                                         const double sDensity =
                                             std::min((double)g.sample_world(g.index_to_world(sr.at(sT))) *
                                                          sh->density_scale * sh->shadow_density_scale,
@@ -1113,7 +1121,7 @@ static void render_rows(const lgo_grid* dens, const lgo_grid* temp, const lg_sha
                                             sDropout = true;
                                             break;
                                         }
-                                        sStep = step1 * (1.0 + ((double)draw_sub(sub, kTagShadowStep | q) - 0.5) * jit);
+                                        sStep = step1 * (1.0 + (step_u(sj) - 0.5) * jit);
                                     }
                                 }
                                 cnt_s += siter;
@@ -1133,7 +1141,7 @@ static void render_rows(const lgo_grid* dens, const lgo_grid* temp, const lg_sha
                             pDropout = true;
                             break;
                         }
-                        pStep = step0 * (1.0 + ((double)draw(stream, kTagPrimaryStep | n) - 0.5) * jit);
+                        pStep = step0 * (1.0 + (step_u(pj) - 0.5) * jit);
                     }
                 }
                 pLumiAA += pLumi * ratioAA;
