@@ -307,6 +307,123 @@ __global__ void __launch_bounds__(256) k_ray_bins(const ShadowTask* __restrict__
     }
 }
 
+// --- occupancy bounds of the light-space bins -----------------------------
+
+// Cube-map face of direction w and its two face coordinates in [-1, 1]
+// (the same face choice and axis order as ray_key).
+__device__ __forceinline__ int cube_face(const float w[3], float& x, float& y) {
+    const float a0 = fabsf(w[0]), a1 = fabsf(w[1]), a2 = fabsf(w[2]);
+    int face;
+    float m;
+    if (a0 >= a1 && a0 >= a2) { face = w[0] < 0.f; m = a0; x = w[1]; y = w[2]; }
+    else if (a1 >= a2) { face = 2 + (w[1] < 0.f); m = a1; x = w[0]; y = w[2]; }
+    else { face = 4 + (w[2] < 0.f); m = a2; x = w[0]; y = w[1]; }
+    const float inv = m > 0.f ? 1.f / m : 0.f;
+    x *= inv;
+    y *= inv;
+    return face;
+}
+
+// One thread per leaf-bitmap cell; a leaf cell (an 8^3 index-space box)
+// raises the bound of every bin it overlaps, widened by a margin that covers
+// the rounding of the rays' own bin computation.
+__global__ void __launch_bounds__(256) k_ray_bounds(DevGrid g, RayBins rb) {
+    const uint32_t lin = blockIdx.x * blockDim.x + threadIdx.x;
+    if (lin >= g.nbits) return;
+    if (!((__ldg(g.leafbits + (lin >> 5)) >> (lin & 31u)) & 1u)) return;
+    const int cx = (int)(lin % (uint32_t)g.lbx), cy = (int)((lin / (uint32_t)g.lbx) % (uint32_t)g.lby),
+              cz = (int)(lin / ((uint32_t)g.lbx * (uint32_t)g.lby));
+    const float lo[3] = {(float)((g.blo[0] + cx - 1) * 8), (float)((g.blo[1] + cy - 1) * 8),
+                         (float)((g.blo[2] + cz - 1) * 8)};
+    for (int k = 0; k < rb.n; ++k) {
+        const RayBin& b = rb.b[k];
+        if (b.bound == nullptr) continue;
+        if (b.kind == 0) {
+            float umin = kInf, umax = -kInf, vmin = kInf, vmax = -kInf, dmax = -kInf;
+            for (int c = 0; c < 8; ++c) {
+                const float q[3] = {lo[0] + 8.f * (c & 1), lo[1] + 4.f * (c & 2), lo[2] + 2.f * (c & 4)};
+                const float u = q[0] * b.U[0] + q[1] * b.U[1] + q[2] * b.U[2] - b.u0;
+                const float v = q[0] * b.V[0] + q[1] * b.V[1] + q[2] * b.V[2] - b.v0;
+                const float d = q[0] * b.D[0] + q[1] * b.D[1] + q[2] * b.D[2] - b.d0;
+                umin = fminf(umin, u); umax = fmaxf(umax, u);
+                vmin = fminf(vmin, v); vmax = fmaxf(vmax, v);
+                dmax = fmaxf(dmax, d);
+            }
+            const float eps = 0.05f;  // index-space voxels
+            const int u0 = clamp_bin((umin - eps) * b.inv_bs, b.ns), u1 = clamp_bin((umax + eps) * b.inv_bs, b.ns);
+            const int v0 = clamp_bin((vmin - eps) * b.inv_bs, b.ns), v1 = clamp_bin((vmax + eps) * b.inv_bs, b.ns);
+            const int bits = __float_as_int(fmaxf(dmax, 0.f));
+            for (int v = v0; v <= v1; ++v)
+                for (int u = u0; u <= u1; ++u) atomicMax(reinterpret_cast<int*>(b.bound) + v * b.ns + u, bits);
+        } else if (b.kind == 1) {
+            // the box's distance from the light
+            float d2 = 0.f;
+            for (int a = 0; a < 3; ++a) {
+                const float e = fmaxf(fmaxf(lo[a] - b.O[a], b.O[a] - (lo[a] + 8.f)), 0.f);
+                d2 = fmaf(e, e, d2);
+            }
+            const int bits = __float_as_int(sqrtf(d2));
+            for (int f = 0; f < 6; ++f) {
+                const int a = f >> 1;
+                const float sg = (f & 1) ? -1.f : 1.f;
+                const int ax = a == 0 ? 1 : 0, ay = a == 2 ? 1 : 2;
+                int npos = 0;
+                float smin = kInf, smax = -kInf, tmin = kInf, tmax = -kInf;
+                for (int c = 0; c < 8; ++c) {
+                    const float q[3] = {lo[0] + 8.f * (c & 1), lo[1] + 4.f * (c & 2), lo[2] + 2.f * (c & 4)};
+                    const float w[3] = {q[0] - b.O[0], q[1] - b.O[1], q[2] - b.O[2]};
+                    const float m = sg * w[a];
+                    if (!(m > 0.f)) continue;
+                    ++npos;
+                    const float x = w[ax] / m, y = w[ay] / m;
+                    smin = fminf(smin, x); smax = fmaxf(smax, x);
+                    tmin = fminf(tmin, y); tmax = fmaxf(tmax, y);
+                }
+                if (npos == 0) continue;
+                int s0 = 0, s1 = b.ns - 1, t0 = 0, t1 = b.ns - 1;
+                if (npos == 8) {
+                    // the face's bins as ray_key computes them, widened by 1e-3 bin
+                    const float eps = 2e-3f / (float)b.ns;
+                    s0 = clamp_bin(((smin - eps) * 0.5f + 0.5f) * (float)b.ns, b.ns);
+                    s1 = clamp_bin(((smax + eps) * 0.5f + 0.5f) * (float)b.ns, b.ns);
+                    t0 = clamp_bin(((tmin - eps) * 0.5f + 0.5f) * (float)b.ns, b.ns);
+                    t1 = clamp_bin(((tmax + eps) * 0.5f + 0.5f) * (float)b.ns, b.ns);
+                }  // else the box straddles the plane through the light: every bin of the face
+                int* tb = reinterpret_cast<int*>(b.bound) + (int64_t)f * b.ns * b.ns;
+                for (int t = t0; t <= t1; ++t)
+                    for (int s = s0; s <= s1; ++s) atomicMin(tb + t * b.ns + s, bits);
+            }
+        }
+    }
+}
+
+cudaError_t launch_ray_bounds(const DevGrid& g, const RayBins& rb, cudaStream_t st) {
+    if (g.nbits == 0) return cudaSuccess;
+    k_ray_bounds<<<(g.nbits + 255) / 256, 256, 0, st>>>(g, rb);
+    ++g_launch_counter;
+    return cudaGetLastError();
+}
+
+// End time of a shadow ray from index-space position p past which no leaf of
+// its light-space bin lies (kInf without a bound table), plus a margin of two
+// voxels for the rounding of the bin and depth computations.
+__device__ __forceinline__ float shadow_ray_end(const RayBin& b, const float p[3]) {
+    if (b.bound == nullptr) return kInf;
+    if (b.kind == 0) {
+        const float u = p[0] * b.U[0] + p[1] * b.U[1] + p[2] * b.U[2] - b.u0;
+        const float v = p[0] * b.V[0] + p[1] * b.V[1] + p[2] * b.V[2] - b.v0;
+        const float d = p[0] * b.D[0] + p[1] * b.D[1] + p[2] * b.D[2] - b.d0;
+        const int ui = clamp_bin(u * b.inv_bs, b.ns), vi = clamp_bin(v * b.inv_bs, b.ns);
+        return __ldg(b.bound + vi * b.ns + ui) - d + 2.f;
+    }
+    const float w[3] = {p[0] - b.O[0], p[1] - b.O[1], p[2] - b.O[2]};
+    float x, y;
+    const int f = cube_face(w, x, y);
+    const int si = clamp_bin((x * 0.5f + 0.5f) * (float)b.ns, b.ns), ti = clamp_bin((y * 0.5f + 0.5f) * (float)b.ns, b.ns);
+    const float dmin = __ldg(b.bound + ((int64_t)f * b.ns + ti) * b.ns + si);
+    return sqrtf(w[0] * w[0] + w[1] * w[1] + w[2] * w[2]) - dmin + 2.f;
+}
+
 cudaError_t launch_ray_bins(const ShadowTask* tasks, const int32_t* total, int64_t task_cap, const RayBins& rb,
                             int32_t* counts, int32_t* order, int sms, cudaStream_t st) {
     k_ray_bins<<<(unsigned)sms * 8u, 256, 0, st>>>(tasks, total, task_cap, rb, counts, order);
@@ -325,7 +442,7 @@ cudaError_t launch_ray_bins(const ShadowTask* tasks, const int32_t* total, int64
 // kEnv = false leaves the environment-light branch out (no light of the
 // scene is an environment light), which frees registers for occupancy.
 template <int DT, bool kEnv>
-__global__ void __launch_bounds__(128, 8) k_shadow(DevScene sc, const ShadowTask* __restrict__ tasks,
+__global__ void __launch_bounds__(128, 8) k_shadow(DevScene sc, RayBins rb, const ShadowTask* __restrict__ tasks,
                                                 const int32_t* __restrict__ total_ptr, int64_t task_cap,
                                                 const int32_t* __restrict__ order, float4* __restrict__ direct,
                                                 unsigned long long* __restrict__ ctr) {
@@ -373,6 +490,9 @@ __global__ void __launch_bounds__(128, 8) k_shadow(DevScene sc, const ShadowTask
             make_iray(srr, tk.p[0], tk.p[1], tk.p[2], -ldir[0], -ldir[1], -ldir[2], kDelta * G.inv_h,
                       dist * G.inv_h);
             if (!clip_to_bbox(G, srr)) continue;  // the reference skips the light sample
+            // past the last leaf of the ray's light-space bin the walk finds no
+            // span: stop it there (spans and samples are unchanged)
+            srr.t1 = fminf(srr.t1, fmaxf(shadow_ray_end(rb.b[k], tk.p), srr.t0));
             LeafDDA sd;
             dda_init(sd, srr, G);
             float sa, sb, tau = 0.f;
@@ -596,13 +716,13 @@ cudaError_t launch_render_shade(const DevScene& sc, const DevCamera& cam, const 
     // one resident wave of CTAs; the threads stride over the rays
     const unsigned sblocks = (unsigned)sms * (unsigned)shadow_ctas_per_sm(sc.dens.dtype, env);
     if (env) {
-        if (sc.dens.dtype == 1) k_shadow<1, true><<<sblocks, 128, 0, st>>>(sc, tasks, total, task_cap, ro.order, direct, counters);
-        else if (sc.dens.dtype == 2) k_shadow<2, true><<<sblocks, 128, 0, st>>>(sc, tasks, total, task_cap, ro.order, direct, counters);
-        else k_shadow<0, true><<<sblocks, 128, 0, st>>>(sc, tasks, total, task_cap, ro.order, direct, counters);
+        if (sc.dens.dtype == 1) k_shadow<1, true><<<sblocks, 128, 0, st>>>(sc, ro.rb, tasks, total, task_cap, ro.order, direct, counters);
+        else if (sc.dens.dtype == 2) k_shadow<2, true><<<sblocks, 128, 0, st>>>(sc, ro.rb, tasks, total, task_cap, ro.order, direct, counters);
+        else k_shadow<0, true><<<sblocks, 128, 0, st>>>(sc, ro.rb, tasks, total, task_cap, ro.order, direct, counters);
     } else {
-        if (sc.dens.dtype == 1) k_shadow<1, false><<<sblocks, 128, 0, st>>>(sc, tasks, total, task_cap, ro.order, direct, counters);
-        else if (sc.dens.dtype == 2) k_shadow<2, false><<<sblocks, 128, 0, st>>>(sc, tasks, total, task_cap, ro.order, direct, counters);
-        else k_shadow<0, false><<<sblocks, 128, 0, st>>>(sc, tasks, total, task_cap, ro.order, direct, counters);
+        if (sc.dens.dtype == 1) k_shadow<1, false><<<sblocks, 128, 0, st>>>(sc, ro.rb, tasks, total, task_cap, ro.order, direct, counters);
+        else if (sc.dens.dtype == 2) k_shadow<2, false><<<sblocks, 128, 0, st>>>(sc, ro.rb, tasks, total, task_cap, ro.order, direct, counters);
+        else k_shadow<0, false><<<sblocks, 128, 0, st>>>(sc, ro.rb, tasks, total, task_cap, ro.order, direct, counters);
     }
     ++g_launch_counter;
     mark(2);

@@ -1545,6 +1545,26 @@ lg_status Ctx::render(const lg_camera* c) {
                d_ray_total.bytes < sizeof(int32_t) * 2) {
         return fail(LG_ERR_STATE, "render buffers changed size during graph capture");
     }
+    // occupancy bounds of the distant and point lights' bins (rebuilt every
+    // render: one short kernel over the leaf bitmap)
+    {
+        int64_t entries = 0;
+        for (int k = 0; k < ro.rb.n; ++k) entries += bound_entries(ro.rb.b[k]);
+        if (!capturing) CK(d_ray_bounds.reserve(sizeof(float) * (size_t)std::max<int64_t>(entries, 1)), "ray bound alloc");
+        else if (d_ray_bounds.bytes < sizeof(float) * (size_t)std::max<int64_t>(entries, 1))
+            return fail(LG_ERR_STATE, "render buffers changed size during graph capture");
+        int64_t off = 0;
+        for (int k = 0; k < ro.rb.n; ++k) {
+            RayBin& b = ro.rb.b[k];
+            const int64_t ne = bound_entries(b);
+            if (ne == 0) continue;
+            b.bound = d_ray_bounds.as<float>() + off;
+            off += ne;
+            if (b.kind == 0) CK(cudaMemsetAsync(b.bound, 0, sizeof(float) * (size_t)ne, st), "ray bound clear");
+            else CK(launch_fill(b.bound, ne, kInf, st), "ray bound clear");
+        }
+        if (off > 0) CK(launch_ray_bounds(sc.dens, ro.rb, st), "ray bounds");
+    }
     ro.key_counts = d_ray_counts.as<int32_t>();
     ro.key_offsets = d_ray_offsets.as<int32_t>();
     ro.key_scan = d_ray_scan.as<int32_t>();

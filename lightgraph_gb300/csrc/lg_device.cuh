@@ -179,12 +179,6 @@ __device__ __forceinline__ float sample_world(const DevGrid& g, float wx, float 
                         (wz - g.wo[2]) * g.inv_h);
 }
 
-// Leaf test for bitmap cell lin (false outside the bitmap).
-__device__ __forceinline__ bool is_leaf(const DevGrid& g, int lin) {
-    if ((unsigned)lin >= g.nbits) return false;
-    return (__ldg(g.leafbits + ((unsigned)lin >> 5)) >> ((unsigned)lin & 31u)) & 1u;
-}
-
 // ---------------------------------------------------------------------------
 // Index ray and the leaf-span march.
 // The reference marches a ray through maximal runs of existing leaf nodes
@@ -235,8 +229,6 @@ struct LeafDDA {
     float dx, dy, dz;   // crossing interval per axis
     int lin;            // current leaf cell (bitmap index)
     int ix, iy, iz;     // bitmap increment of one step per axis
-    bool open;          // a span has started
-    float start;        // its start time
     bool done;
 };
 
@@ -267,8 +259,6 @@ __device__ __forceinline__ int dda_axis(float e, float d, float inv, float t0, i
 __device__ __forceinline__ void dda_init(LeafDDA& s, const IRay& r, const DevGrid& g) {
     s.t = r.t0;
     s.tmax = r.t1;
-    s.open = false;
-    s.start = 0.f;
     s.done = false;
     int sx, sy, sz;
     const int cx = dda_axis(r.e[0], r.d[0], r.inv[0], r.t0, g.blo[0], sx, s.nx, s.dx);
@@ -284,29 +274,46 @@ __device__ __forceinline__ void dda_init(LeafDDA& s, const IRay& r, const DevGri
     s.iz = sz * g.lbx * g.lby;
 }
 
-// Next span [ta, tb] of consecutive leaf cells with tb - ta > kDelta.
+// Leaf test for a walker cell: the index is clamped to nbits (a zero bit: the
+// bitmap's last word has room for it), so no branch guards the load.
+__device__ __forceinline__ bool walker_leaf(const DevGrid& g, int lin) {
+    const uint32_t c = min((uint32_t)lin, g.nbits);
+    return (__ldg(g.leafbits + (c >> 5)) >> (c & 31u)) & 1u;
+}
+
+// One DDA step to the next cell (math::MinIndex tie order: x if strictly
+// smallest, else y if below z, else z); returns false once the crossing
+// lies past tmax.
+__device__ __forceinline__ bool walker_step(LeafDDA& s) {
+    const bool ax = (s.nx < s.ny) && (s.nx < s.nz);
+    const bool ay = !(s.nx < s.ny) && (s.ny < s.nz);
+    const bool az = !ax && !ay;
+    s.t = ax ? s.nx : (ay ? s.ny : s.nz);
+    if (ax) { s.nx += s.dx; s.lin += s.ix; }
+    if (ay) { s.ny += s.dy; s.lin += s.iy; }
+    if (az) { s.nz += s.dz; s.lin += s.iz; }
+    return s.t <= s.tmax;
+}
+
+// Next span [ta, tb] of consecutive leaf cells with tb - ta > kDelta: first
+// the cells up to the next leaf, then the run of leaves; a run cut by tmax
+// ends there.
 __device__ __forceinline__ bool next_span(const DevGrid& g, LeafDDA& s, float& ta, float& tb) {
     while (!s.done) {
-        const bool leaf = is_leaf(g, s.lin);
-        if (leaf) {
-            if (!s.open) { s.open = true; s.start = s.t; }
-        } else if (s.open) {
-            s.open = false;
-            if (s.t - s.start > kDelta) { ta = s.start; tb = s.t; return true; }
+        while (!walker_leaf(g, s.lin)) {
+            if (!walker_step(s)) { s.done = true; return false; }
         }
-        // step to the next cell (math::MinIndex tie order: x if strictly
-        // smallest, else y if below z, else z)
-        const bool ax = (s.nx < s.ny) && (s.nx < s.nz);
-        const bool ay = !(s.nx < s.ny) && (s.ny < s.nz);
-        const bool az = !ax && !ay;
-        s.t = ax ? s.nx : (ay ? s.ny : s.nz);
-        if (ax) { s.nx += s.dx; s.lin += s.ix; }
-        if (ay) { s.ny += s.dy; s.lin += s.iy; }
-        if (az) { s.nz += s.dz; s.lin += s.iz; }
-        if (!(s.t <= s.tmax)) {
+        const float start = s.t;
+        bool inside;
+        do {
+            inside = walker_step(s);
+        } while (inside && walker_leaf(g, s.lin));
+        if (!inside) {
             s.done = true;
-            if (s.open && s.tmax - s.start > kDelta) { ta = s.start; tb = s.tmax; return true; }
+            if (s.tmax - start > kDelta) { ta = start; tb = s.tmax; return true; }
+            return false;
         }
+        if (s.t - start > kDelta) { ta = start; tb = s.t; return true; }
     }
     return false;
 }

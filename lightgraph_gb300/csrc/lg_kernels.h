@@ -157,6 +157,13 @@ struct RayBin {
     float u0, v0, inv_bs;     // kind 0: projected origin, 1 / bin size
     float d0, inv_ds;         // depth origin, 1 / depth bin size
     int64_t key_off, nkeys;   // this light's keys in the combined histogram
+    // Occupancy bound per light-space bin (kinds 0 and 1; null: none). A
+    // distant light's shadow ray stays in its (u, v) column and a point
+    // light's in its cube-map cone, so no leaf lies on the ray past the
+    // column's largest leaf depth - d0 (kind 0, ns x ns, v major) or closer to
+    // the light than the cone's smallest leaf distance (kind 1, 6 x ns x ns,
+    // face major). k_shadow ends its walk there, past every leaf it can meet.
+    float* bound;
 };
 struct RayBins {
     RayBin b[kMaxLights];
@@ -167,6 +174,15 @@ constexpr int kRayUnit = 2;  // consecutive tasks ordered as one unit
 // holds the exclusive scan; order[counts[key]++] = task) over all lights.
 cudaError_t launch_ray_bins(const ShadowTask* tasks, const int32_t* total, int64_t task_cap, const RayBins& rb,
                             int32_t* counts, int32_t* order, int sms, cudaStream_t st);
+// Fills the occupancy bounds of every light of rb with a bound table (kind 0:
+// rb.b[k].ns^2 floats, kind 1: 6 * ns^2, zeroed or set to +inf first by the
+// caller as bound_init gives): one thread per leaf-bitmap cell.
+cudaError_t launch_ray_bounds(const DevGrid& g, const RayBins& rb, cudaStream_t st);
+// Initial value of a light's bound table entries (bits of a non-negative float).
+inline uint32_t bound_init(const RayBin& b) { return b.kind == 0 ? 0u : 0x7F800000u; }
+inline int64_t bound_entries(const RayBin& b) {
+    return b.kind == 0 ? (int64_t)b.ns * b.ns : b.kind == 1 ? 6 * (int64_t)b.ns * b.ns : 0;
+}
 // Wave 1: counts[ps] = shading samples of each pixel-sample.
 // claim: a zeroed counter the persistent grid's warps claim pixel samples
 // from.
