@@ -114,9 +114,12 @@ static void post_rotate(double M[3][3], int axis, double ang) {
 
 // PerspectiveCamera as main.cc:96-102 builds it (src/Renderer.h:148-171,232-239).
 // Shadow-ray ordering keys of every light of the scene (see RayBin): about
-// 8 x 8 voxel (u, v) bins for distant lights, a cube map of about 4 voxels per
+// 4 x 4 voxel (u, v) bins for distant lights (at most 256^2), a cube map of
+// about 4 voxels per
 // bin at the far side of the leaf bbox (at most 128^2 per face) for point
-// lights, and depth bins of about 16 voxels (at most 32).
+// lights, and depth bins of about 4 voxels (at most 128): the lanes of a warp
+// then start their rays at nearly the same depth and sample neighbouring
+// cells at the same time.
 static RayBins ray_bins(const DevScene& sc, int64_t cap) {
     RayBins rb{};
     rb.n = sc.n_lights;
@@ -127,7 +130,7 @@ static RayBins ray_bins(const DevScene& sc, int64_t cap) {
     auto dot = [](const double* x, const double* y) { return x[0] * y[0] + x[1] * y[1] + x[2] * y[2]; };
     auto depth_bins = [](RayBin& b, double lo, double hi) {
         const double range = std::max(hi - lo, 1e-3);
-        b.nd = (int)std::min(32.0, std::max(1.0, std::ceil(range / 16.0)));
+        b.nd = (int)std::min(128.0, std::max(1.0, std::ceil(range / 4.0)));
         b.d0 = (float)lo;
         b.inv_ds = (float)(b.nd / range);
     };
@@ -156,7 +159,7 @@ static RayBins ray_bins(const DevScene& sc, int64_t cap) {
             }
             const double range = std::max({hi[0] - lo[0], hi[1] - lo[1], 1e-3});
             b.ns = 1;
-            while (b.ns < 128 && b.ns * 8.0 < range) b.ns *= 2;
+            while (b.ns < 256 && b.ns * 4.0 < range) b.ns *= 2;
             b.inv_bs = (float)(b.ns / range);
             b.u0 = (float)lo[0];
             b.v0 = (float)lo[1];
