@@ -70,8 +70,9 @@ def parse():
     ap.add_argument("--image", type=int, default=0, help="override the square image size (profiling runs)")
     ap.add_argument("--spp", type=int, default=0, help="override the samples per pixel (profiling runs)")
     ap.add_argument("--res", type=int, default=0, help="override the production grid resolution (profiling runs)")
-    ap.add_argument("--serving", type=int, default=24, help="requests in the serving measurement (0: skip)")
-    ap.add_argument("--rate", type=float, default=50.0, help="Poisson arrival rate of the serving stream (req/s)")
+    ap.add_argument("--serving", type=int, default=48, help="requests in the serving measurement (0: skip)")
+    ap.add_argument("--rates", default="50", help="Poisson arrival rates of the serving stream (req/s, comma "
+                                                  "separated; the full sweep is 1,5,10,25,50)")
     ap.add_argument("--batched", type=int, default=1, help="run the 64-graph batched measurement (0: skip)")
     ap.add_argument("--fw-schedule", type=int, default=-1,
                     help="pin the Floyd-Warshall schedule (0-5; -1: autotuned). Profiling runs pin the "
@@ -197,44 +198,56 @@ def run_batched_graphs(local: int):
     return out
 
 
-def run_serving(n: int, rate: float):
+def run_serving(n: int, rates):
     """The mixed request stream (4 volumes 64^3..512^3, 512..8192 points,
-    128^2..1024^2 at 1-4 spp, 1-3 lights, Poisson arrivals, seed 4): served
-    by the server (volumes resident) one request at a time and with
-    continuous batching (8 slots), and through the plain drop-in path (each
-    request uploads its volume and renders alone)."""
+    128^2..1024^2 at 1-4 spp, 1-3 lights plus an environment light on a
+    quarter of the requests, seed 4). The same n requests are
+      * rendered each alone on an idle server (single-request latency);
+      * submitted all at once (capacity) to the batched server (8 slots,
+        volumes resident), to a one-slot resident server, and through the
+        plain drop-in path (one request at a time: volume load, then
+        lg_render_frame; Floyd-Warshall on the server's fixed schedule, the
+        load timed apart);
+      * replayed as a Poisson stream at each rate against the batched server
+        (p50/p99 latency, renders/s, p99 over the alone p99)."""
     from lightgraph_gb300 import serve
-    out = {"stream": f"{n} requests, Poisson {rate} req/s, seed 4, volumes 64^3-512^3, 512-8192 points, "
-                     "128^2-1024^2 at 1-4 spp, 1-3 lights"}
     vs = serve.make_volumes(None)
-    # single-request latency: each request alone on an idle server; "plain" and
-    # "batched" replay the Poisson arrivals; the *_capacity runs submit every
-    # request at once (throughput when the queue never drains)
-    runs = (("alone", 1, False), ("plain", 1, True), ("batched", 8, True), ("plain_capacity", 1, False),
-            ("batched_capacity", 8, False))
-    for label, slots, realtime in runs:
+    out = {"stream": f"{n} requests, Poisson arrivals, seed 4, volumes 64^3-512^3, 512-8192 points, "
+                     "128^2-1024^2 at 1-4 spp, 1-3 lights, a 2-sample env light on a quarter of them"}
+
+    def server(slots):
         srv = serve.Server(max_inflight=slots)
         vs.ids = [srv.add_volume(g) for g in vs.grids]
-        stream = serve.request_stream(vs, n, rate, seed=4)
-        if label == "alone":
-            lat = []
-            for _, req in stream:
-                _, _, l = srv.wait(srv.submit(req), -1, False)
-                lat.append(l / 1e3)
-            out["alone_p50_ms"] = float(np.percentile(lat, 50))
-            out["alone_p99_ms"] = float(np.percentile(lat, 99))
-        else:
-            stats, _ = serve.run_stream(srv, stream, want_images=False, realtime=realtime)
-            out[label] = stats
+        return srv
+
+    srv = server(1)
+    lat = []
+    for _, req in serve.request_stream(vs, n, 1.0, seed=4):
+        _, _, l = srv.wait(srv.submit(req), -1, False)
+        lat.append(l / 1e3)
+    srv.close()
+    out["alone_p50_ms"] = float(np.percentile(lat, 50))
+    out["alone_p99_ms"] = float(np.percentile(lat, 99))
+    cap = {}
+    for label, slots in (("batched_8_slots", 8), ("resident_1_slot", 1)):
+        srv = server(slots)
+        cap[label], _ = serve.run_stream(srv, serve.request_stream(vs, n, 1.0, seed=4), realtime=False)
         srv.close()
-    # the plain drop-in path: each request uploads its volume and renders alone
-    out["standalone_capacity"] = serve.run_standalone(vs, serve.request_stream(vs, n, rate, seed=4))
-    out["capacity_batched_over_standalone"] = (out["batched_capacity"]["renders_per_s"] /
-                                               out["standalone_capacity"]["renders_per_s"])
-    out["batched_over_plain_renders_per_s"] = out["batched"]["renders_per_s"] / out["plain"]["renders_per_s"]
-    out["capacity_batched_over_plain"] = (out["batched_capacity"]["renders_per_s"] /
-                                          out["plain_capacity"]["renders_per_s"])
-    out["batched_p99_over_alone_p99"] = out["batched"]["p99_ms"] / out["alone_p99_ms"]
+    cap["plain_fixed_schedule"] = serve.run_standalone(vs, serve.request_stream(vs, n, 1.0, seed=4))
+    b = cap["batched_8_slots"]["renders_per_s"]
+    cap["batched_over_resident_1_slot"] = b / cap["resident_1_slot"]["renders_per_s"]
+    cap["batched_over_plain"] = b / cap["plain_fixed_schedule"]["renders_per_s"]
+    cap["batched_over_plain_without_upload"] = b / cap["plain_fixed_schedule"]["renders_per_s_without_upload"]
+    out["capacity"] = cap
+    sweep = []
+    for rate in rates:
+        srv = server(8)
+        st, _ = serve.run_stream(srv, serve.request_stream(vs, n, rate, seed=4), realtime=True)
+        srv.close()
+        st["rate_req_per_s"] = rate
+        st["p99_over_alone_p99"] = st["p99_ms"] / out["alone_p99_ms"]
+        sweep.append(st)
+    out["rates"] = sweep
     return out
 
 
@@ -676,7 +689,7 @@ def run_ours(args):
                         "executed_frac_of_inner_loop_ceiling": fw_exec / (stage_ms[2] * 1e-3) / 1e12 / fw_ceiling},
     }
     if rank == 0 and args.serving > 0:
-        line["serving"] = run_serving(args.serving, args.rate)
+        line["serving"] = run_serving(args.serving, [float(r) for r in args.rates.split(",") if r])
     if rank == 0 and world == 1 and args.ref_iters > 0 and not args.small:
         line["reference_scale"] = run_reference_scale(args.ref_iters, local, not args.no_cpu_baseline)
     if rank == 0 and world == 1 and args.batched and not args.small:

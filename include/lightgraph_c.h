@@ -463,8 +463,9 @@ typedef struct lg_server_opts {
 
 /* A render request against a resident volume: one frame of the three stages
  * with its own graphs, lights, shader, settings (settings.seed keys its random
- * streams) and camera. Arrays are copied at submit time. Environment lights
- * are not accepted (no per-request map). */
+ * streams) and camera. An environment light (LG_LIGHT_ENV) needs the
+ * request's env map (env_rgb, env_h rows x env_w columns x RGB, at least
+ * 2 x 2). Arrays are copied at submit time. */
 typedef struct lg_request {
     int32_t volume;                /* id from lg_server_add_volume                */
     int32_t n_graphs;
@@ -478,6 +479,8 @@ typedef struct lg_request {
     lg_settings settings;
     lg_camera camera;
     double point_voxel_size;
+    const float* env_rgb;          /* env map of the request's env lights, or NULL */
+    int32_t env_w, env_h;
 } lg_request;
 
 /* Creates a server with max_inflight slots (one context, stream and worker

@@ -90,7 +90,8 @@ class RequestC(C.Structure):
     _fields_ = [("volume", C.c_int32), ("n_graphs", C.c_int32), ("points", C.c_void_p), ("offsets", C.c_void_p),
                 ("radius_sq", C.c_void_p), ("max_connect", C.c_int32), ("n_lights", C.c_int32),
                 ("lights", C.c_void_p), ("shader", ShaderC), ("settings", SettingsC), ("camera", CameraC),
-                ("point_voxel_size", C.c_double)]
+                ("point_voxel_size", C.c_double), ("env_rgb", C.c_void_p), ("env_w", C.c_int32),
+                ("env_h", C.c_int32)]
 
 
 P = C.c_void_p

@@ -58,6 +58,7 @@ struct Request {
     std::vector<int64_t> offs;
     std::vector<float> r2;
     std::vector<lg_light> lights;
+    std::vector<float> env;  // env map (h x w x 3) of the request's env lights
     uint64_t bytes = 0;
     double t_submit = 0, t_admit = 0, t_done = 0;
     bool done = false;
@@ -111,6 +112,8 @@ extern "C" uint64_t lg_request_bytes(const lg_request* q) {
     // tasks depend on the volume and are not counted)
     b += (uint64_t)q->camera.width * q->camera.height * (uint64_t)std::max(q->camera.samples, 1) * 44;
     b += 160ull * 160 * 160 * 12;                      // point bins (upper bound)
+    if (q->env_rgb && q->env_w > 1 && q->env_h > 1)  // env map and its CDFs
+        b += (uint64_t)q->env_w * q->env_h * 4 * 5 + (uint64_t)q->env_h * 4 * 262;
     return b;
 }
 
@@ -143,7 +146,8 @@ void lg_server::run(Slot* s, Request* q) {
     c.temp_ext_set = true;
     c.shader = r.shader;
     c.settings = r.settings;
-    lg_status st = c.set_lights(q->lights.data(), (int)q->lights.size(), nullptr, 0, 0);
+    lg_status st = c.set_lights(q->lights.data(), (int)q->lights.size(), q->env.empty() ? nullptr : q->env.data(),
+                                r.env_w, r.env_h);
     if (st == LG_OK) st = c.load_graphs(r.n_graphs, q->pts.data(), q->offs.data(), q->r2.data(), r.max_connect);
     // the symmetric persistent solve at 1 CTA per SM (leaves room for the
     // other slots' kernels; correct whatever the residency), its queue in
@@ -283,8 +287,8 @@ extern "C" lg_status lg_server_submit(lg_server* srv, const lg_request* req, int
         req->n_lights > LG_MAX_LIGHTS || (req->n_lights > 0 && !req->lights))
         return LG_ERR_INVALID;
     for (int k = 0; k < req->n_lights; ++k)
-        if (req->lights[k].type == LG_LIGHT_ENV) {
-            srv->err = "environment lights are not served (no per-request env map)";
+        if (req->lights[k].type == LG_LIGHT_ENV && (!req->env_rgb || req->env_w < 2 || req->env_h < 2)) {
+            srv->err = "an environment light needs the request's env map (at least 2 x 2)";
             return LG_ERR_INVALID;
         }
     auto q = std::make_unique<Request>();
@@ -294,6 +298,9 @@ extern "C" lg_status lg_server_submit(lg_server* srv, const lg_request* req, int
     q->offs.assign(req->offsets, req->offsets + req->n_graphs + 1);
     q->r2.assign(req->radius_sq, req->radius_sq + req->n_graphs);
     q->lights.assign(req->lights, req->lights + req->n_lights);
+    if (req->env_rgb && req->env_w > 1 && req->env_h > 1)
+        q->env.assign(req->env_rgb, req->env_rgb + (size_t)3 * req->env_w * req->env_h);
+    q->r.env_rgb = nullptr;
     q->r.points = nullptr;
     q->r.offsets = nullptr;
     q->r.radius_sq = nullptr;

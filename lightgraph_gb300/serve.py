@@ -4,7 +4,9 @@ request stream, and latency / throughput statistics.
 The workload stands in for a render service: four resident cumulus volumes
 (64^3, 128^3, 256^3, 512^3), requests drawn uniformly over them with a
 LightGraph of log-uniform [512, 8192] points, an image from {128^2, 256^2,
-512^2, 1024^2} at 1-4 spp and 1-3 lights, arriving as a Poisson process.
+512^2, 1024^2} at 1-4 spp and 1-3 lights (a quarter of the requests add a
+2-sample environment light on the synthetic 512x256 sky map), arriving as a
+Poisson process.
 """
 from __future__ import annotations
 
@@ -97,6 +99,7 @@ class Request:
     opts: SceneSettings
     max_connect: int = 12
     point_voxel_size: float = 0.0
+    env_map: np.ndarray | None = None
 
     def to_c(self) -> RequestC:
         arrs = [np.ascontiguousarray(p, np.float32).reshape(-1, 3) for p in self.points]
@@ -118,6 +121,10 @@ class Request:
         c.settings = self.opts.to_c()
         c.camera = self.opts.camera_c()
         c.point_voxel_size = self.point_voxel_size
+        if self.env_map is not None:
+            self._env = np.ascontiguousarray(self.env_map, np.float32)
+            c.env_rgb = ptr(self._env)
+            c.env_h, c.env_w = self._env.shape[0], self._env.shape[1]
         return c
 
 
@@ -129,6 +136,16 @@ VOLUME_RES = (64, 128, 256, 512)
 IMAGES = (128, 256, 512, 1024)
 LIGHT_SPECS = ("dir:0:1,0.89,0.79:1.2:-40,30,0", "point:0:0.4,0.6,1.0:30:0.6,0.5,0.9",
                "dir:0:0.3,0.4,0.5:0.5:20,-120,0")
+ENV_SPEC = "env:0:1,1,1:0.35:2:sky"
+_SKY = None
+
+
+def sky_map() -> np.ndarray:
+    """The synthetic 512x256 sky map the environment-lit requests share."""
+    global _SKY
+    if _SKY is None:
+        _SKY = scenes.envmap()
+    return _SKY
 
 
 @dataclass
@@ -159,13 +176,15 @@ def make_volumes(server: Server | None, resolutions=VOLUME_RES, pool: int = 8192
 
 
 def request_stream(vs: VolumeSet, n: int, rate: float, seed: int = 4, n_min: int = 512, n_max: int = 8192,
-                   images=IMAGES):
-    """(arrival time s, Request) pairs: Poisson arrivals at `rate` req/s."""
+                   images=IMAGES, env_fraction: float = 0.25):
+    """(arrival time s, Request) pairs: Poisson arrivals at `rate` req/s. The
+    requests themselves depend only on the seed, not on the rate."""
     rng = np.random.default_rng(seed)
     t = 0.0
     out = []
     for q in range(n):
-        t += rng.exponential(1.0 / rate) if rate > 0 else 0.0
+        gap = rng.exponential(1.0)  # drawn for every rate, so the requests do not depend on it
+        t += gap / rate if rate > 0 else 0.0
         v = int(rng.integers(len(vs.grids)))
         npts = int(np.exp(rng.uniform(np.log(n_min), np.log(n_max))))
         pool = vs.pools[v]
@@ -176,11 +195,16 @@ def request_stream(vs: VolumeSet, n: int, rate: float, seed: int = 4, n_min: int
         spp = int(rng.integers(1, 5))
         nl = int(rng.integers(1, 4))
         lights = [Light.parse(s) for s in LIGHT_SPECS[:nl]]
+        env = None
+        if env_fraction > 0 and rng.random() < env_fraction:
+            lights.append(Light.parse(ENV_SPEC))
+            env = sky_map()
         # connection radius: 1.7 x the mean point spacing of the request
         spacing = (0.3 / max(npts, 1)) ** (1.0 / 3.0)
         opts = SceneSettings(width=img, height=img, samples=spp, camTranslate=(0.0, 0.0, 2.2), iter=1,
                              seed=1000 + q)
-        out.append((t, Request(vs.ids[v] if vs.ids else v, [pts], [1.7 * spacing], lights, vs.shaders[v], opts)))
+        out.append((t, Request(vs.ids[v] if vs.ids else v, [pts], [1.7 * spacing], lights, vs.shaders[v], opts,
+                               env_map=env)))
     return out
 
 
@@ -209,29 +233,37 @@ def run_stream(server: Server, stream, want_images: bool = False, realtime: bool
     return stats, imgs
 
 
-def run_standalone(vs: VolumeSet, stream, device: int = 0):
+def run_standalone(vs: VolumeSet, stream, device: int = 0, fw_schedule: int = 3):
     """The plain drop-in path, one request at a time, as the reference runs one
-    render per invocation: upload the request's volume, then lg_render_frame
-    with the request's points and lights (host buffers in, the four films
-    out). One context is reused, so no CUDA context is created per request.
-    All requests are taken at once (throughput when the queue never drains)."""
+    render per invocation: load the request's volume, then lg_render_frame with
+    the request's points and lights (host buffers in, the four films out). One
+    context is reused (no CUDA context per request) and the Floyd-Warshall
+    schedule is fixed to the server's (no autotuning per size). The volume
+    load (lg_upload_grid and the scene settings) is timed apart from the
+    render. All requests are taken at once (throughput when the queue never
+    drains)."""
     from .lightgraph import Context
     ctx = Context(device)
+    ctx.set_fw_schedule(fw_schedule)
     t0 = time.perf_counter()
-    lat = []
+    lat, up = [], []
     for _, req in stream:
         t = time.perf_counter()
         ctx.upload_density(vs.grids[vs.ids.index(req.volume) if vs.ids else req.volume])
         ctx.set_shader(req.shader)
         ctx.set_settings(req.opts)
-        ctx.set_lights(req.lights)
+        ctx.set_lights(req.lights, req.env_map)
+        t1 = time.perf_counter()
         r2 = [np.float32(r) * np.float32(r) for r in req.radius]
         ctx.render_frame(req.points, r2, req.opts, req.max_connect, req.point_voxel_size)
-        lat.append((time.perf_counter() - t) * 1e3)
+        t2 = time.perf_counter()
+        up.append((t1 - t) * 1e3)
+        lat.append((t2 - t1) * 1e3)
     wall = time.perf_counter() - t0
     ctx.close()
-    lat = np.array(lat)
+    lat, up = np.array(lat), np.array(up)
+    render_s = float(lat.sum()) / 1e3
     return {"requests": len(stream), "wall_s": wall, "renders_per_s": len(stream) / wall,
-            "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
-            "mean_ms": float(lat.mean())}
-
+            "renders_per_s_without_upload": len(stream) / render_s, "upload_ms_mean": float(up.mean()),
+            "fw_schedule": fw_schedule, "p50_ms": float(np.percentile(lat, 50)),
+            "p99_ms": float(np.percentile(lat, 99)), "mean_ms": float(lat.mean())}

@@ -16,13 +16,17 @@ def small_stream():
 
 
 def test_mixed_equals_alone(small_stream):
+    """Every result, environment-lit requests included, is bit-identical alone
+    and in the mix."""
     vs = small_stream
     alone_srv = serve.Server(max_inflight=1)
     mix_srv = serve.Server(max_inflight=4)
     try:
         for srv in (alone_srv, mix_srv):
             vs.ids = [srv.add_volume(g) for g in vs.grids]
-            stream = serve.request_stream(vs, 8, rate=0, seed=4, n_min=64, n_max=600, images=(32, 48, 64))
+            stream = serve.request_stream(vs, 8, rate=0, seed=4, n_min=64, n_max=600, images=(32, 48, 64),
+                                          env_fraction=0.5)
+            assert any(req.env_map is not None for _, req in stream)
             stats, imgs = serve.run_stream(srv, stream, want_images=True, realtime=False)
             assert stats["requests"] == 8
             if srv is alone_srv:
@@ -90,5 +94,19 @@ def test_queue_capacity(small_stream):
         for t in tickets:
             srv.wait(t, -1, False)
         assert busy > 0 and len(tickets) + busy == 12
+    finally:
+        srv.close()
+
+
+def test_env_light_needs_its_map(small_stream):
+    vs = small_stream
+    srv = serve.Server(max_inflight=1)
+    try:
+        vs.ids = [srv.add_volume(g) for g in vs.grids]
+        req = serve.request_stream(vs, 1, rate=0, seed=2, n_min=64, n_max=64, images=(32,), env_fraction=1.0)[0][1]
+        req.env_map = None
+        with pytest.raises(LightGraphError) as e:
+            srv.submit(req)
+        assert e.value.status == _capi.LG_ERR_INVALID
     finally:
         srv.close()
