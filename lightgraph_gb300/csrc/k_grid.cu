@@ -19,17 +19,20 @@
 
 namespace lg {
 
-// One thread per cell record (x fastest over the padded box): gathers the
-// cell's eight voxel values from the dense staging array (0 outside it) and
-// writes them as one record.
+// One thread per cell record: gathers the cell's eight voxel values from the
+// dense staging array (0 outside it) and writes them as one record.
 __global__ void k_pack_bricks(const float* __restrict__ dense, int dx, int dy, int dz, int ox, int oy,
                               int oz, DevGrid g, void* __restrict__ bricks) {
-    const int64_t total = (int64_t)g.sz * g.vn[2];
+    const int64_t total = (int64_t)g.nb[0] * g.nb[1] * g.nb[2] * 512;
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= total) return;
-    const int x = g.vlo[0] + (int)(t % g.vn[0]) - ox;
-    const int y = g.vlo[1] + (int)((t / g.vn[0]) % g.vn[1]) - oy;
-    const int z = g.vlo[2] + (int)(t / g.sz) - oz;
+    const int64_t b = t >> 9;
+    const int l = (int)(t & 511);
+    const int bx = (int)(b % g.nb[0]), by = (int)((b / g.nb[0]) % g.nb[1]),
+              bz = (int)(b / ((int64_t)g.nb[0] * g.nb[1]));
+    const int x = (g.blo[0] + bx) * 8 + (l & 7) - ox;
+    const int y = (g.blo[1] + by) * 8 + ((l >> 3) & 7) - oy;
+    const int z = (g.blo[2] + bz) * 8 + (l >> 6) - oz;
     float v[8];
 #pragma unroll
     for (int c = 0; c < 8; ++c) {
@@ -60,7 +63,7 @@ __global__ void k_pack_bricks(const float* __restrict__ dense, int dx, int dy, i
 
 cudaError_t launch_pack_bricks(const float* dense, const int dims[3], const int origin[3],
                                const DevGrid& g, void* bricks, cudaStream_t st) {
-    const int64_t total = (int64_t)g.sz * g.vn[2];
+    const int64_t total = (int64_t)g.nb[0] * g.nb[1] * g.nb[2] * 512;
     k_pack_bricks<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(
         dense, dims[0], dims[1], dims[2], origin[0], origin[1], origin[2], g, bricks);
     ++g_launch_counter;

@@ -334,13 +334,15 @@ lg_status Ctx::upload_grid(int which, const lg_grid_desc* desc, const float* val
         g.vlo[a] = g.blo[a] * 8;
         g.vn[a] = (uint32_t)g.nb[a] * 8u;
     }
-    g.sz = g.vn[0] * g.vn[1];
-    g.rec_last = g.sz * g.vn[2] - 1u;
+    g.sy = (uint32_t)g.nb[0] * 512u;
+    g.sz = (uint32_t)g.nb[0] * (uint32_t)g.nb[1] * 512u;
+    g.rec_last = g.sz * (uint32_t)g.nb[2] - 1u;
     {
-        // span_cell adds the three floor_bits words (floor + 0x4B400000)
-        const uint32_t bias = 0x4B400000u;
-        g.rec_off = 0u - ((uint32_t)g.vlo[0] + bias) - ((uint32_t)g.vlo[1] + bias) * g.vn[0] -
-                    ((uint32_t)g.vlo[2] + bias) * g.sz;
+        // span_cell's brick coordinates carry 0x4B400000 / 8 each (the floor
+        // bits' bias); brick_off removes it and the box's first brick
+        const uint32_t b8 = 0x4B400000u >> 3;
+        g.brick_off = 0u - ((uint32_t)g.blo[0] + b8) - ((uint32_t)g.blo[1] + b8) * (uint32_t)g.nb[0] -
+                      ((uint32_t)g.blo[2] + b8) * (uint32_t)g.nb[0] * (uint32_t)g.nb[1];
     }
     const int64_t nvox = (int64_t)desc->dims[0] * desc->dims[1] * desc->dims[2];
     const int64_t nbt = (int64_t)g.nb[0] * g.nb[1] * g.nb[2];

@@ -19,17 +19,19 @@ constexpr int kMaxRamp = 16;
 constexpr float kDelta = 1e-9f;
 
 // ---------------------------------------------------------------------------
-// Grid: one record per voxel cell (x, y, z) of a dense box that covers the
-// grid's 8^3 leaf bricks plus one brick of zero padding on every side, x
-// fastest, then y, then z. A cell's record holds the eight voxel values of its
-// trilinear footprint, v(x + a, y + b, z + c) at index a + 2b + 4c, so one
-// sample is one aligned 32-byte (FP32) or 16-byte (FP16/BF16) load instead of
-// eight gathers, and a 128-byte line holds four neighbouring cells along x.
-// Voxels outside the box read the background value 0. The box's first and
-// last cells lie in padding corners, so their eight values are 0; the checked
-// sampler redirects cells outside the box to the first one. Records cost 8x
-// the voxel storage, which HBM holds easily (a 512^3 box is 4.7 GB in FP32);
-// what matters for the marches is one L1 request per sample.
+// Grid: one record per voxel cell (x, y, z) of a dense box that is tiled into
+// 8^3 bricks (x fastest inside a brick, bricks x fastest in the box) with one
+// brick of zero padding on every side. A cell's record holds the eight voxel
+// values of its trilinear footprint, v(x + a, y + b, z + c) at index
+// a + 2b + 4c, so one sample is one aligned 32-byte (FP32) or 16-byte
+// (FP16/BF16) load instead of eight gathers. A brick's 512 records are one
+// contiguous 16 KB block, so a ray crossing a brick in any direction stays in
+// one block (rays that run along z would otherwise touch a new page at every
+// voxel). Voxels outside the box read the background value 0. The box's first
+// and last cells lie in padding corner bricks, so their eight values are 0;
+// the checked sampler redirects cells outside the box to the first one.
+// Records cost 8x the voxel storage, which HBM holds easily (a 512^3 box is
+// 4.6 GB in FP32); what matters for the marches is one L1 request per sample.
 // ---------------------------------------------------------------------------
 struct DevGrid {
     const void* data = nullptr;
@@ -45,8 +47,8 @@ struct DevGrid {
     float bbmin[3] = {0.f, 0.f, 0.f};    // leaf bbox in index space (origin of min leaf)
     float bbmax[3] = {0.f, 0.f, 0.f};    // ... max leaf origin + 8
     int has_leaves = 0;
-    uint32_t sz = 0;                     // records per z slice (vn[0] * vn[1])
-    uint32_t rec_off = 0;                // record of cell (0, 0, 0): -(vlo . strides) mod 2^32
+    uint32_t sy = 0, sz = 0;             // record strides of one brick step in y and z
+    uint32_t brick_off = 0;              // span_cell's brick index offset (mod 2^32)
     uint32_t rec_last = 0;               // last record (a padding cell)
     // The leaf bitmap covers the brick box plus a margin of one brick on
     // every side (bits 0), so a walker one cell off the box reads "no leaf"
@@ -87,7 +89,8 @@ __device__ __forceinline__ void ld_cell(const void* data, uint32_t rec, float v[
 __device__ __forceinline__ uint32_t cell_record(const DevGrid& g, int ix, int iy, int iz) {
     const uint32_t rx = (uint32_t)(ix - g.vlo[0]), ry = (uint32_t)(iy - g.vlo[1]), rz = (uint32_t)(iz - g.vlo[2]);
     const bool in = rx < g.vn[0] && ry < g.vn[1] && rz < g.vn[2];
-    const uint32_t rec = rx + ry * g.vn[0] + rz * g.sz;
+    const uint32_t rec = (rx >> 3) * 512u + (ry >> 3) * g.sy + (rz >> 3) * g.sz +
+                         (((rz & 7u) << 6) | ((ry & 7u) << 3) | (rx & 7u));
     return in ? rec : 0u;
 }
 
@@ -113,8 +116,12 @@ __device__ __forceinline__ uint32_t span_cell(const DevGrid& g, float px, float 
     wx = px - fx;
     wy = py - fy;
     wz = pz - fz;
-    // the 0x4B400000 bias of the three coordinates is folded into rec_off
-    const uint32_t rec = bx + by * g.vn[0] + bz * g.sz + g.rec_off;
+    // The bias 0x4B400000 is a multiple of 8: the low three bits are the
+    // offsets inside the brick, and bits >> 3 are the brick coordinates plus
+    // 0x4B400000 / 8, which brick_off cancels together with the box's first
+    // brick.
+    const uint32_t brick = (bx >> 3) + (by >> 3) * (uint32_t)g.nb[0] + (bz >> 3) * (g.sz >> 9) + g.brick_off;
+    const uint32_t rec = brick * 512u + (((bz & 7u) << 6) | ((by & 7u) << 3) | (bx & 7u));
     return min(rec, g.rec_last);
 }
 
