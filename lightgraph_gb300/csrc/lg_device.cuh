@@ -236,6 +236,8 @@ struct LeafDDA {
     float dx, dy, dz;   // crossing interval per axis
     int lin;            // current leaf cell (bitmap index)
     int ix, iy, iz;     // bitmap increment of one step per axis
+    bool open;          // next_span_flat: a span has started
+    float start;        // next_span_flat: its start time
     bool done;
 };
 
@@ -267,6 +269,8 @@ __device__ __forceinline__ void dda_init(LeafDDA& s, const IRay& r, const DevGri
     s.t = r.t0;
     s.tmax = r.t1;
     s.done = false;
+    s.open = false;
+    s.start = 0.f;
     int sx, sy, sz;
     const int cx = dda_axis(r.e[0], r.d[0], r.inv[0], r.t0, g.blo[0], sx, s.nx, s.dx);
     const int cy = dda_axis(r.e[1], r.d[1], r.inv[1], r.t0, g.blo[1], sy, s.ny, s.dy);
@@ -321,6 +325,27 @@ __device__ __forceinline__ bool next_span(const DevGrid& g, LeafDDA& s, float& t
             return false;
         }
         if (s.t - start > kDelta) { ta = start; tb = s.t; return true; }
+    }
+    return false;
+}
+
+// next_span in one loop that examines a cell and steps on every pass (the
+// same spans). Marches whose lanes run unrelated rays (graph edges, vertex
+// shadow rays) stay converged better with it than with next_span's two inner
+// loops, which the render's ordered, neighbouring rays favour.
+__device__ __forceinline__ bool next_span_flat(const DevGrid& g, LeafDDA& s, float& ta, float& tb) {
+    while (!s.done) {
+        const bool leaf = walker_leaf(g, s.lin);
+        if (leaf) {
+            if (!s.open) { s.open = true; s.start = s.t; }
+        } else if (s.open) {
+            s.open = false;
+            if (s.t - s.start > kDelta) { ta = s.start; tb = s.t; return true; }
+        }
+        if (!walker_step(s)) {
+            s.done = true;
+            if (s.open && s.tmax - s.start > kDelta) { ta = s.start; tb = s.tmax; return true; }
+        }
     }
     return false;
 }
@@ -499,7 +524,7 @@ __device__ __forceinline__ bool march_fixed(const DevGrid& g, IRay r, float step
     LeafDDA s;
     dda_init(s, r, g);
     float ta, tb;
-    while (next_span(g, s, ta, tb)) {
+    while (next_span_flat(g, s, ta, tb)) {
         for (float t = step * ceilf(ta / step); t <= tb && t + step > t; t += step) {
             const float rho = fminf(
                 sample_index_t<DT>(g, r.e[0] + t * r.d[0], r.e[1] + t * r.d[1], r.e[2] + t * r.d[2]) * scale,
