@@ -335,7 +335,11 @@ __device__ __forceinline__ bool next_span(const DevGrid& g, LeafDDA& s, float& t
 // loops, which the render's ordered, neighbouring rays favour.
 __device__ __forceinline__ bool next_span_flat(const DevGrid& g, LeafDDA& s, float& ta, float& tb) {
     while (!s.done) {
-        const bool leaf = walker_leaf(g, s.lin);
+        // the bounds test skips the bitmap load for cells off the bitmap
+        // (measured: the clamped load of walker_leaf makes these marches
+        // several times slower)
+        const bool leaf = (unsigned)s.lin < g.nbits &&
+                          ((__ldg(g.leafbits + ((unsigned)s.lin >> 5)) >> ((unsigned)s.lin & 31u)) & 1u);
         if (leaf) {
             if (!s.open) { s.open = true; s.start = s.t; }
         } else if (s.open) {
