@@ -154,7 +154,11 @@ __device__ __forceinline__ uint32_t primary_sample(const DevScene& sc, const Dev
                     const float pw[3] = {p[0] * G.h + G.wo[0], p[1] * G.h + G.wo[1], p[2] * G.h + G.wo[2]};
                     float sgv[3], em[3];
                     sample_scatter(sg, pw[0], pw[1], pw[2], sgv);
-                    const float mask = powf(fminf(fmaxf(rho, 0.f), 1.f), sh.mask_power) * sh.scatter_scale;
+                    // clamp(rho, 0, 1)^maskPower (src/Renderer.h:584-588) as 2^(p log2 x);
+                    // x = 0 gives what pow gives: 1 for p = 0, 0 for p > 0, inf for p < 0
+                    const float rc = fminf(fmaxf(rho, 0.f), 1.f), mp = sh.mask_power;
+                    const float mask = (rc > 0.f ? exp2f(mp * __log2f(rc)) : (mp == 0.f ? 1.f : mp > 0.f ? 0.f : kInf)) *
+                                       sh.scatter_scale;
                     const float temp = sc.has_temp ? sample_world(sc.temp, pw[0], pw[1], pw[2]) : 0.f;
                     ramp_color(sh, temp, em);
                     const int64_t t = base + shading;
