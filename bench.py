@@ -70,7 +70,7 @@ def parse():
     ap.add_argument("--image", type=int, default=0, help="override the square image size (profiling runs)")
     ap.add_argument("--spp", type=int, default=0, help="override the samples per pixel (profiling runs)")
     ap.add_argument("--res", type=int, default=0, help="override the production grid resolution (profiling runs)")
-    ap.add_argument("--serving", type=int, default=48, help="requests in the serving measurement (0: skip)")
+    ap.add_argument("--serving", type=int, default=200, help="requests in the serving measurement (0: skip)")
     ap.add_argument("--rates", default="50", help="Poisson arrival rates of the serving stream (req/s, comma "
                                                   "separated; the full sweep is 1,5,10,25,50)")
     ap.add_argument("--batched", type=int, default=1, help="run the 64-graph batched measurement (0: skip)")
