@@ -149,10 +149,11 @@ void lg_server::run(Slot* s, Request* q) {
     lg_status st = c.set_lights(q->lights.data(), (int)q->lights.size(), q->env.empty() ? nullptr : q->env.data(),
                                 r.env_w, r.env_h);
     if (st == LG_OK) st = c.load_graphs(r.n_graphs, q->pts.data(), q->offs.data(), q->r2.data(), r.max_connect);
-    // the symmetric persistent solve at 1 CTA per SM (leaves room for the
-    // other slots' kernels; correct whatever the residency), its queue in
+    // the symmetric persistent solve at 2 CTAs per SM (correct whatever the
+    // residency, so the slots' solves may share the SMs; measured 11% more
+    // renders/s than 1 CTA per SM on the mixed stream), its queue in
     // structural order (one-off sizes do not pay for the list scheduling)
-    if (st == LG_OK) c.fw_choice = 3;
+    if (st == LG_OK) c.fw_choice = 4;
     if (st == LG_OK) st = c.build_edges();
     if (st == LG_OK) st = c.solve_all();
     if (st == LG_OK) st = c.splat(r.point_voxel_size);

@@ -233,7 +233,7 @@ def run_stream(server: Server, stream, want_images: bool = False, realtime: bool
     return stats, imgs
 
 
-def run_standalone(vs: VolumeSet, stream, device: int = 0, fw_schedule: int = 3):
+def run_standalone(vs: VolumeSet, stream, device: int = 0, fw_schedule: int = 4):
     """The plain drop-in path, one request at a time, as the reference runs one
     render per invocation: load the request's volume, then lg_render_frame with
     the request's points and lights (host buffers in, the four films out). One
