@@ -204,7 +204,9 @@ def run_serving(n: int, rates):
     quarter of the requests, seed 4). The same n requests are
       * rendered each alone on an idle server (single-request latency);
       * submitted all at once (capacity) to the batched server (8 slots,
-        volumes resident), to a one-slot resident server, and through the
+        volumes resident, path solves of requests in flight sharing
+        Floyd-Warshall launches), to the same server with every request
+        solving its paths alone, to a one-slot resident server, and through the
         plain drop-in path (one request at a time: volume load, then
         lg_render_frame; Floyd-Warshall on the server's fixed schedule, the
         load timed apart);
@@ -215,8 +217,8 @@ def run_serving(n: int, rates):
     out = {"stream": f"{n} requests, Poisson arrivals, seed 4, volumes 64^3-512^3, 512-8192 points, "
                      "128^2-1024^2 at 1-4 spp, 1-3 lights, a 2-sample env light on a quarter of them"}
 
-    def server(slots):
-        srv = serve.Server(max_inflight=slots)
+    def server(slots, solo_paths=False):
+        srv = serve.Server(max_inflight=slots, solo_paths=solo_paths)
         vs.ids = [srv.add_volume(g) for g in vs.grids]
         return srv
 
@@ -229,13 +231,15 @@ def run_serving(n: int, rates):
     out["alone_p50_ms"] = float(np.percentile(lat, 50))
     out["alone_p99_ms"] = float(np.percentile(lat, 99))
     cap = {}
-    for label, slots in (("batched_8_slots", 8), ("resident_1_slot", 1)):
-        srv = server(slots)
+    for label, slots, solo in (("batched_8_slots", 8, False), ("batched_8_slots_solo_paths", 8, True),
+                               ("resident_1_slot", 1, True)):
+        srv = server(slots, solo)
         cap[label], _ = serve.run_stream(srv, serve.request_stream(vs, n, 1.0, seed=4), realtime=False)
         srv.close()
     cap["plain_fixed_schedule"] = serve.run_standalone(vs, serve.request_stream(vs, n, 1.0, seed=4))
     b = cap["batched_8_slots"]["renders_per_s"]
     cap["batched_over_resident_1_slot"] = b / cap["resident_1_slot"]["renders_per_s"]
+    cap["shared_paths_over_solo_paths"] = b / cap["batched_8_slots_solo_paths"]["renders_per_s"]
     cap["batched_over_plain"] = b / cap["plain_fixed_schedule"]["renders_per_s"]
     cap["batched_over_plain_without_upload"] = b / cap["plain_fixed_schedule"]["renders_per_s_without_upload"]
     out["capacity"] = cap

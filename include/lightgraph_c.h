@@ -457,7 +457,9 @@ typedef struct lg_server_opts {
     int32_t device;
     int32_t max_inflight;          /* requests on the device at once (slots)    */
     int32_t queue_capacity;        /* waiting requests before LG_ERR_BUSY        */
-    int32_t _pad0;
+    int32_t solo_paths;            /* 0: the Floyd-Warshall solves of requests in
+                                      flight share persistent launches; 1: each
+                                      request solves its own graphs alone       */
     uint64_t hbm_budget_bytes;     /* device bytes admitted at once (0: 64 GiB)  */
 } lg_server_opts;
 
@@ -486,7 +488,11 @@ typedef struct lg_request {
 /* Creates a server with max_inflight slots (one context, stream and worker
  * thread each). Admission is FIFO: the head request is admitted when a slot is
  * free and its lg_request_bytes fit in hbm_budget_bytes next to the requests
- * in flight; admitted requests run concurrently. */
+ * in flight; admitted requests run concurrently. Unless solo_paths is set,
+ * the requests whose edges are marched at about the same time (within a
+ * fraction of a millisecond of each other) have their all-pairs path solves
+ * batched into one persistent Floyd-Warshall launch; every result is the
+ * same, bit for bit, as the request's alone. */
 lg_status lg_server_create(const lg_server_opts* opts, lg_server** out);
 lg_status lg_server_destroy(lg_server* srv);
 const char* lg_server_last_error(const lg_server* srv);
@@ -512,6 +518,10 @@ lg_status lg_server_wait(lg_server* srv, int64_t ticket, int timeout_ms,
                          float* rgba, double* queue_us, double* latency_us);
 /* Device bytes a request is charged against the HBM budget. */
 uint64_t lg_request_bytes(const lg_request* req);
+/* Floyd-Warshall launches the server has made for its requests and the
+ * graphs they solved (more graphs than launches: requests shared a launch).
+ * No counterpart in the reference. */
+lg_status lg_server_stats(lg_server* srv, uint64_t* path_launches, uint64_t* path_graphs);
 
 /* ------------------------------------------------------------------------- */
 /* Host helpers: the reference's scene description (no device work)          */

@@ -83,7 +83,7 @@ class ScatterOptsC(C.Structure):
 
 class ServerOptsC(C.Structure):
     _fields_ = [("device", C.c_int32), ("max_inflight", C.c_int32), ("queue_capacity", C.c_int32),
-                ("_pad0", C.c_int32), ("hbm_budget_bytes", C.c_uint64)]
+                ("solo_paths", C.c_int32), ("hbm_budget_bytes", C.c_uint64)]
 
 
 class RequestC(C.Structure):
@@ -153,6 +153,7 @@ SIGNATURES = {
     "lg_server_poll": (I32, [P, I64, C.POINTER(C.c_int)]),
     "lg_server_wait": (I32, [P, I64, C.c_int, P, C.POINTER(D), C.POINTER(D)]),
     "lg_request_bytes": (U64, [C.POINTER(RequestC)]),
+    "lg_server_stats": (I32, [P, C.POINTER(U64), C.POINTER(U64)]),
 }
 
 # liblightgraph_host.so: scene description helpers, EXR files, synthetic scenes

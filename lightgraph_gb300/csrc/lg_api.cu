@@ -1048,6 +1048,26 @@ lg_status Ctx::solve_paths() {
     return LG_OK;
 }
 
+lg_status Ctx::fw_solve_on(float* base, int choice) {
+    if (choice < 3 || choice > 5) return fail(LG_ERR_INVALID, "batched path solves use a symmetric schedule");
+    lg_status s = solve_paths_batched(choice);
+    if (s != LG_OK) return s;
+    return run_fw_schedule(this, base, choice);
+}
+
+lg_status Ctx::solve_rest() {
+    Ctx* ctx = this;
+    CK(launch_set_diag(d_S.as<float>(), d_graphs.as<GraphInfo>(), n_graphs, max_n, st), "diagonal");
+    paths_solved = true;
+    lg_status s = vertex_light();
+    if (s != LG_OK) return s;
+    light_done = true;
+    s = diffuse();
+    if (s != LG_OK) return s;
+    diffuse_done = true;
+    return LG_OK;
+}
+
 lg_status Ctx::vertex_light() {
     Ctx* ctx = this;
     if (!D().valid) return fail(LG_ERR_STATE, "no density grid uploaded");

@@ -186,6 +186,12 @@ struct Ctx {
     lg_status vertex_light();
     lg_status diffuse();
     lg_status solve_all();
+    // The path solve split for a caller that batches several contexts'
+    // matrices into one launch: fw_solve_on runs this context's queue (its
+    // h_graphs' s_off relative to base) on its own stream; solve_rest is
+    // what follows the solve (diagonal, vertex light, diffusion).
+    lg_status fw_solve_on(float* base, int choice);
+    lg_status solve_rest();
     lg_status splat(double point_voxel_size);
     lg_status render(const lg_camera* c);
     lg_status download_films(float* rgba, float* direct, float* scatter, float* emission);

@@ -9,9 +9,17 @@
 //   - each slot is a context with its own stream and worker thread, bound to
 //     the volume's resident grids, so the kernels of admitted requests
 //     overlap on the device; a slot is taken again as soon as it finishes;
+//   - the all-pairs path solves of requests in flight are batched: a slot
+//     that has marched its edges hands its matrices to a path batcher, and
+//     the slots that arrive within a fraction of a millisecond of each other
+//     share one persistent Floyd-Warshall launch over all their graphs (the
+//     batched solve's queue interleaves the graphs round by round; each
+//     matrix stays in its slot's buffers and the launch addresses them from
+//     the lowest of them). CUDA events order the launch after every member's
+//     edge march and each member's later kernels after the launch;
 //   - every kernel is deterministic and every random number is keyed by the
 //     request's own seed, so a request's films are the same alone or in the
-//     mix.
+//     mix, batched or not.
 #include <algorithm>
 #include <chrono>
 #include <condition_variable>
@@ -73,7 +81,31 @@ struct Slot {
     Request* cur = nullptr;
     float* pinned = nullptr;
     size_t pinned_bytes = 0;
+    cudaEvent_t marched = nullptr;  // the slot's edge march is done
+    cudaEvent_t solved = nullptr;   // the batched path solve holding its graphs is done
 };
+
+// One slot's matrices waiting for, or in, a batched path solve.
+struct PathJob {
+    Slot* slot = nullptr;
+    lg_status status = LG_OK;
+    std::string err;
+    bool finished = false;
+};
+
+// Batches the path solves of the slots in flight (see the file comment).
+struct PathBatcher {
+    std::mutex mu;
+    std::condition_variable cv;
+    std::vector<PathJob*> pending;
+    bool leading = false;     // a slot thread is forming or running a batch
+    int marching = 0;         // slots admitted that have not handed over their matrices yet
+    std::unique_ptr<Ctx> ctx; // the batch's queue buffers and stream
+    uint64_t launches = 0, graphs = 0;
+};
+
+// How long a batch waits for slots still marching their edges.
+constexpr double kPathWaitUs = 300.0;
 
 }  // namespace
 
@@ -90,10 +122,13 @@ struct lg_server {
     bool stop = false;
     std::string err;
     std::unique_ptr<Ctx> upload_ctx;
+    PathBatcher paths;
 
     void admit_locked();
     void slot_loop(Slot* s);
     void run(Slot* s, Request* q);
+    lg_status solve_paths_shared(Slot* s);
+    void run_path_batch(std::vector<PathJob*>& batch);
 };
 
 extern "C" uint64_t lg_request_bytes(const lg_request* q) {
@@ -133,6 +168,86 @@ void lg_server::admit_locked() {
     }
 }
 
+// One persistent launch over the graphs of every job of the batch, on the
+// batcher's stream: it waits for each member's edge march and each member's
+// stream waits for it.
+void lg_server::run_path_batch(std::vector<PathJob*>& batch) {
+    Ctx& b = *paths.ctx;
+    lg_status st = LG_OK;
+    float* base = nullptr;
+    for (PathJob* j : batch) {
+        float* S = j->slot->ctx->d_S.as<float>();
+        if (!base || S < base) base = S;
+    }
+    b.h_graphs.clear();
+    b.max_n = 0;
+    for (PathJob* j : batch) {
+        const Ctx& c = *j->slot->ctx;
+        const int64_t shift = c.d_S.as<float>() - base;
+        for (GraphInfo g : c.h_graphs) {
+            g.s_off += shift;
+            b.h_graphs.push_back(g);
+            b.max_n = std::max(b.max_n, g.n);
+        }
+        if (cudaStreamWaitEvent(b.st, j->slot->marched, 0) != cudaSuccess) st = b.fail(LG_ERR_CUDA, "path batch wait");
+    }
+    b.n_graphs = (int)b.h_graphs.size();
+    if (st == LG_OK) st = b.fw_solve_on(base, 4);
+    for (PathJob* j : batch) {
+        if (st == LG_OK && cudaEventRecord(j->slot->solved, b.st) != cudaSuccess)
+            st = b.fail(LG_ERR_CUDA, "path batch record");
+    }
+    for (PathJob* j : batch) {
+        j->status = st;
+        if (st != LG_OK) j->err = b.err;
+    }
+    paths.launches += 1;
+    paths.graphs += (uint64_t)b.n_graphs;
+}
+
+// Hands the slot's marched matrices to the batcher and returns once a batched
+// launch holding them is enqueued (the slot's stream then waits for it). The
+// first slot to find no batch forming leads the next one: it waits up to
+// kPathWaitUs for the slots still marching, takes every job waiting and runs
+// the launch; later arrivals wait for the next leader.
+lg_status lg_server::solve_paths_shared(Slot* s) {
+    Ctx& c = *s->ctx;
+    PathJob job;
+    job.slot = s;
+    if (cudaEventRecord(s->marched, c.st) != cudaSuccess) {
+        std::lock_guard<std::mutex> lk(paths.mu);
+        --paths.marching;
+        paths.cv.notify_all();
+        return c.fail(LG_ERR_CUDA, "edge march event");
+    }
+    std::unique_lock<std::mutex> lk(paths.mu);
+    --paths.marching;
+    paths.pending.push_back(&job);
+    paths.cv.notify_all();
+    while (!job.finished) {
+        if (!paths.leading) {
+            paths.leading = true;
+            const double t0 = now_us();
+            while (paths.marching > 0 && now_us() - t0 < kPathWaitUs)
+                paths.cv.wait_for(lk, std::chrono::microseconds(50));
+            std::vector<PathJob*> batch;
+            batch.swap(paths.pending);
+            lk.unlock();
+            run_path_batch(batch);
+            lk.lock();
+            for (PathJob* j : batch) j->finished = true;
+            paths.leading = false;
+            paths.cv.notify_all();
+            continue;
+        }
+        paths.cv.wait(lk);
+    }
+    lk.unlock();
+    if (job.status != LG_OK) return c.fail(job.status, "%s", job.err.c_str());
+    if (cudaStreamWaitEvent(c.st, s->solved, 0) != cudaSuccess) return c.fail(LG_ERR_CUDA, "path solve wait");
+    return LG_OK;
+}
+
 void lg_server::run(Slot* s, Request* q) {
     Ctx& c = *s->ctx;
     const lg_request& r = q->r;
@@ -140,6 +255,12 @@ void lg_server::run(Slot* s, Request* q) {
         q->status = st;
         q->err = c.err;
     };
+    if (!opts.solo_paths) {
+        // counted until the slot hands its matrices to the path batcher, so
+        // a forming batch can wait for it
+        std::lock_guard<std::mutex> lk(paths.mu);
+        ++paths.marching;
+    }
     const Volume* v = volumes[r.volume].get();
     c.dens_ext = &v->dens;
     c.temp_ext = &v->temp;
@@ -155,7 +276,19 @@ void lg_server::run(Slot* s, Request* q) {
     // structural order (one-off sizes do not pay for the list scheduling)
     if (st == LG_OK) c.fw_choice = 4;
     if (st == LG_OK) st = c.build_edges();
-    if (st == LG_OK) st = c.solve_all();
+    if (opts.solo_paths) {
+        if (st == LG_OK) st = c.solve_all();
+    } else {
+        if (st == LG_OK) st = c.march_edges();
+        if (st == LG_OK) {
+            st = solve_paths_shared(s);  // leaves the marching count
+        } else {
+            std::lock_guard<std::mutex> lk(paths.mu);
+            --paths.marching;
+            paths.cv.notify_all();
+        }
+        if (st == LG_OK) st = c.solve_rest();
+    }
     if (st == LG_OK) st = c.splat(r.point_voxel_size);
     if (st == LG_OK) st = c.render(&r.camera);
     if (st == LG_OK) {
@@ -204,16 +337,22 @@ extern "C" lg_status lg_server_create(const lg_server_opts* opts, lg_server** ou
     auto srv = std::make_unique<lg_server>();
     srv->opts = *opts;
     if (srv->opts.hbm_budget_bytes == 0) srv->opts.hbm_budget_bytes = 64ull << 30;
-    for (int k = 0; k <= opts->max_inflight; ++k) {
+    for (int k = 0; k <= opts->max_inflight + 1; ++k) {
         lg_ctx* h = nullptr;
         const lg_status st = lg_create(opts->device, &h);
         if (st != LG_OK) return st;
         std::unique_ptr<Ctx> c(reinterpret_cast<Ctx*>(h));
         if (k == 0) {
             srv->upload_ctx = std::move(c);
+        } else if (k == 1) {
+            srv->paths.ctx = std::move(c);
         } else {
             auto s = std::make_unique<Slot>();
             s->ctx = std::move(c);
+            cudaSetDevice(opts->device);
+            if (cudaEventCreateWithFlags(&s->marched, cudaEventDisableTiming) != cudaSuccess ||
+                cudaEventCreateWithFlags(&s->solved, cudaEventDisableTiming) != cudaSuccess)
+                return LG_ERR_CUDA;
             srv->slots.push_back(std::move(s));
         }
     }
@@ -236,11 +375,22 @@ extern "C" lg_status lg_server_destroy(lg_server* srv) {
     for (auto& s : srv->slots) {
         if (s->th.joinable()) s->th.join();
         if (s->pinned) cudaFreeHost(s->pinned);
+        if (s->marched) cudaEventDestroy(s->marched);
+        if (s->solved) cudaEventDestroy(s->solved);
         // the slot contexts are destroyed through the C ABI (stream, events)
         lg_destroy(reinterpret_cast<lg_ctx*>(s->ctx.release()));
     }
+    lg_destroy(reinterpret_cast<lg_ctx*>(srv->paths.ctx.release()));
     lg_destroy(reinterpret_cast<lg_ctx*>(srv->upload_ctx.release()));
     delete srv;
+    return LG_OK;
+}
+
+extern "C" lg_status lg_server_stats(lg_server* srv, uint64_t* path_launches, uint64_t* path_graphs) {
+    if (!srv) return LG_ERR_INVALID;
+    std::lock_guard<std::mutex> lk(srv->paths.mu);
+    if (path_launches) *path_launches = srv->paths.launches;
+    if (path_graphs) *path_graphs = srv->paths.graphs;
     return LG_OK;
 }
 

@@ -23,9 +23,9 @@ from .lightgraph import Grid, Light, SceneSettings, Shader
 
 class Server:
     def __init__(self, device: int = 0, max_inflight: int = 4, queue_capacity: int = 1024,
-                 hbm_budget_bytes: int = 64 << 30):
+                 hbm_budget_bytes: int = 64 << 30, solo_paths: bool = False):
         self.lib = _capi.load()
-        o = ServerOptsC(device, max_inflight, queue_capacity, 0, hbm_budget_bytes)
+        o = ServerOptsC(device, max_inflight, queue_capacity, 1 if solo_paths else 0, hbm_budget_bytes)
         h = C.c_void_p()
         st = self.lib.lg_server_create(C.byref(o), C.byref(h))
         if st != _capi.LG_OK:
@@ -66,6 +66,12 @@ class Server:
             self._err(st)
         self._keep[tk.value] = req
         return tk.value
+
+    def stats(self):
+        """(Floyd-Warshall launches, graphs they solved) so far."""
+        a, b = C.c_uint64(), C.c_uint64()
+        self._err(self.lib.lg_server_stats(self.h, C.byref(a), C.byref(b)))
+        return a.value, b.value
 
     def poll(self, ticket: int) -> bool:
         """True once the request has finished (its result stays for wait)."""
@@ -230,6 +236,9 @@ def run_stream(server: Server, stream, want_images: bool = False, realtime: bool
     stats = {"requests": len(stream), "wall_s": wall, "renders_per_s": len(stream) / wall,
              "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
              "mean_ms": float(lat.mean()), "queue_p50_ms": float(np.percentile(que, 50))}
+    launches, graphs = server.stats()
+    stats["path_launches"] = launches
+    stats["path_graphs"] = graphs
     return stats, imgs
 
 

@@ -17,9 +17,10 @@ def small_stream():
 
 def test_mixed_equals_alone(small_stream):
     """Every result, environment-lit requests included, is bit-identical alone
-    and in the mix."""
+    (one slot, its own path solve) and in the mix (four slots whose path
+    solves share Floyd-Warshall launches)."""
     vs = small_stream
-    alone_srv = serve.Server(max_inflight=1)
+    alone_srv = serve.Server(max_inflight=1, solo_paths=True)
     mix_srv = serve.Server(max_inflight=4)
     try:
         for srv in (alone_srv, mix_srv):
@@ -29,6 +30,10 @@ def test_mixed_equals_alone(small_stream):
             assert any(req.env_map is not None for _, req in stream)
             stats, imgs = serve.run_stream(srv, stream, want_images=True, realtime=False)
             assert stats["requests"] == 8
+            if srv is mix_srv:
+                # every request's graph went through a shared launch, and at
+                # least one launch held more than one request's graph
+                assert stats["path_graphs"] == 8 and stats["path_launches"] < 8
             if srv is alone_srv:
                 alone = imgs
             else:
