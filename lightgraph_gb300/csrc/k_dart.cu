@@ -280,7 +280,7 @@ cudaError_t launch_dart(const DevGrid& g, const DartParams& prm, int n_iter, con
     if (n_iter <= 0) return cudaSuccess;
     const size_t smem = sizeof(float) * 3 * prm.hard_limit;
     if (smem > 32 * 1024) {  // with the static arrays, past the default 48 KB
-        cudaError_t e = cudaFuncSetAttribute(k_dart, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        const cudaError_t e = raise_smem_limit(reinterpret_cast<const void*>(k_dart));
         if (e != cudaSuccess) return e;
     }
     k_dart<<<n_iter, kDartThreads, smem, st>>>(g, prm, expected, out_pts, out_count, out_last_m2);

@@ -11,6 +11,10 @@
 //      reference's FP64) are re-tested with FP64 arithmetic.
 //   2. k_greedy (one CTA per graph, rows in order): a warp takes the first
 //      (max_connect - cnt[i]) candidates whose partner count is below the cap.
+#include <algorithm>
+#include <mutex>
+#include <vector>
+
 #include "lg_kernels.h"
 
 namespace lg {
@@ -189,14 +193,29 @@ cudaError_t launch_candidates(const float* pts, const GraphInfo* graphs, const i
     return cudaGetLastError();
 }
 
+cudaError_t raise_smem_limit(const void* func) {
+    static std::mutex mu;
+    static std::vector<const void*> done;
+    std::lock_guard<std::mutex> lk(mu);
+    if (std::find(done.begin(), done.end(), func) != done.end()) return cudaSuccess;
+    int dev = 0, optin = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    cudaFuncAttributes fa{};
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, func);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes);
+    if (e == cudaSuccess) done.push_back(func);
+    return e;
+}
+
 cudaError_t launch_greedy(const float* pts, const GraphInfo* graphs, int n_graphs, int max_n,
                           const uint16_t* cand, const int32_t* cand_cnt, int max_connect,
                           int2* edges, int32_t* edge_cnt, cudaStream_t st) {
     if (n_graphs == 0) return cudaSuccess;
     const size_t smem = 2 * kGreedyChunk * kCandCap * sizeof(uint16_t) + 2 * kGreedyChunk * sizeof(int32_t) +
                         (size_t)max_n;
-    cudaError_t e = cudaFuncSetAttribute(k_greedy, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)smem);
+    const cudaError_t e = raise_smem_limit(reinterpret_cast<const void*>(k_greedy));
     if (e != cudaSuccess) return e;
     k_greedy<<<n_graphs, 256, smem, st>>>(pts, graphs, cand, cand_cnt, max_connect, edges, edge_cnt);
     ++g_launch_counter;
