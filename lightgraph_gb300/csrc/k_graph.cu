@@ -13,6 +13,7 @@
 //      (max_connect - cnt[i]) candidates whose partner count is below the cap.
 #include <algorithm>
 #include <mutex>
+#include <utility>
 #include <vector>
 
 #include "lg_kernels.h"
@@ -194,18 +195,21 @@ cudaError_t launch_candidates(const float* pts, const GraphInfo* graphs, const i
 }
 
 cudaError_t raise_smem_limit(const void* func) {
+    // the limit belongs to the current device's context: one entry per
+    // (device, kernel)
     static std::mutex mu;
-    static std::vector<const void*> done;
-    std::lock_guard<std::mutex> lk(mu);
-    if (std::find(done.begin(), done.end(), func) != done.end()) return cudaSuccess;
+    static std::vector<std::pair<int, const void*>> done;
     int dev = 0, optin = 0;
     cudaError_t e = cudaGetDevice(&dev);
-    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    if (e != cudaSuccess) return e;
+    std::lock_guard<std::mutex> lk(mu);
+    if (std::find(done.begin(), done.end(), std::make_pair(dev, func)) != done.end()) return cudaSuccess;
+    e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
     cudaFuncAttributes fa{};
     if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, func);
     if (e == cudaSuccess)
         e = cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes);
-    if (e == cudaSuccess) done.push_back(func);
+    if (e == cudaSuccess) done.push_back(std::make_pair(dev, func));
     return e;
 }
 

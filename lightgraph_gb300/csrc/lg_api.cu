@@ -1313,7 +1313,7 @@ int64_t occupied_voxels(int64_t n, const float* pts, const double lo[3], const d
         dim[a] = (int64_t)std::floor(hi[a] * inv + 0.5) - c0[a] + 1;
         cells = (cells > (int64_t)1 << 40) ? cells : cells * dim[a];
     }
-    if (cells <= ((int64_t)1 << 28)) {
+    if (cells <= ((int64_t)1 << 25)) {  // a byte map of at most 32 MB, else a sort of the keys
         std::vector<uint8_t> seen((size_t)cells, 0);
         int64_t count = 0;
         for (int64_t i = 0; i < n; ++i) {
