@@ -402,10 +402,15 @@ class CpuFrameSample:
         sparsity pattern after the same rounds;
       * render: the rows (r + 1/2) H / R, R = H / SAMPLE_FRACTION, in one call
         parallel over their pixels, scaled x SAMPLE_FRACTION.
-    setup() does the untimed preparation once; step() times one sample."""
+    setup() does the untimed preparation once; step() times one sample.
+    calibrate() measures, against a whole frame timed in the same run, the
+    ratio of each sampled stage's whole-frame time to its scaled sample
+    (rows rendered apart lose the cache reuse neighbouring rows get in a
+    whole frame); later steps multiply the sampled stages by it."""
 
     def __init__(self, sc):
         self.sc = sc
+        self.factors = {}
 
     def setup(self):
         import ctypes as C
@@ -450,11 +455,24 @@ class CpuFrameSample:
         self.lib.lgo_transmittance_of(n * n, S64.ctypes.data, self.ext.ctypes.data, out.ctypes.data)
         return out
 
+    def calibrate(self, full_stages):
+        """Per sampled stage, whole-frame ms / scaled sample ms, from the mean
+        of two warm samples against the whole frame's stage times."""
+        self.factors = {}
+        dets = [self.step()[1] for _ in range(2)]
+        for k in ("floyd_warshall", "render"):
+            self.factors[k] = full_stages[k] / (0.5 * (dets[0][k] + dets[1][k]))
+        return self.factors
+
     def describe(self):
-        return (f"build/march/light/diffuse/splat whole; Floyd-Warshall {FW_WINDOWS} windows of {self.K} rounds "
-                f"spread over {self.n} (each from the matrix's state at its round) scaled x{self.fw_scale:g}; "
-                f"render rows (r+1/2)H/{len(self.rows)} ({len(self.rows)} of {self.sc.opts.height}) in one "
-                f"pixel-parallel call scaled x{self.row_scale:g}")
+        d = (f"build/march/light/diffuse/splat whole; Floyd-Warshall {FW_WINDOWS} windows of {self.K} rounds "
+             f"spread over {self.n} (each from the matrix's state at its round) scaled x{self.fw_scale:g}; "
+             f"render rows (r+1/2)H/{len(self.rows)} ({len(self.rows)} of {self.sc.opts.height}) in one "
+             f"pixel-parallel call scaled x{self.row_scale:g}")
+        if self.factors:
+            d += ("; both sampled stages then scaled by their whole-frame/sample ratio measured once in this run "
+                  f"(Floyd-Warshall x{self.factors['floyd_warshall']:.3f}, render x{self.factors['render']:.3f})")
+        return d
 
     def step(self):
         """One timed sample: (ms per frame, per-stage ms)."""
@@ -473,7 +491,7 @@ class CpuFrameSample:
             t = time.perf_counter()
             lib.lgo_fw_maxtimes_rounds(n, self.T_window.ctypes.data, k0, k0 + self.K)
             fw += time.perf_counter() - t
-        det["floyd_warshall"] = fw * 1e3 * self.fw_scale
+        det["floyd_warshall"] = fw * 1e3 * self.fw_scale * self.factors.get("floyd_warshall", 1.0)
         t = time.perf_counter()
         L = o.vertex_light(pts)
         det["vertex_light"] = (time.perf_counter() - t) * 1e3
@@ -495,7 +513,7 @@ class CpuFrameSample:
                             C.c_double(sc.density.voxel_size * sc.opts.scatterGridResFactor),
                             C.c_void_p(vals.ctypes.data), C.c_void_p(self.rows.ctypes.data), C.c_int(len(self.rows)),
                             *[C.c_void_p(f.ctypes.data) for f in films], None)
-        det["render"] = (time.perf_counter() - t) * 1e3 * self.row_scale
+        det["render"] = (time.perf_counter() - t) * 1e3 * self.row_scale * self.factors.get("render", 1.0)
         return sum(det.values()), det
 
 
@@ -524,15 +542,13 @@ def cpu_full_frame(sc):
     return sum(det.values()), det
 
 
-def sampler_error(sc, full_ms=None):
-    """The sampling rule checked against the whole frame of the same
-    workload, timed complete on the host cores (once), beside one sampled
-    estimate after a warm-up sample."""
-    if full_ms is None:
-        full_ms, _ = cpu_full_frame(sc)
-    smp = CpuFrameSample(sc).setup()
+def sampler_error(smp, full_ms):
+    """The uncalibrated sampling rule against the whole frame of the same
+    workload timed complete on the host cores: one sample after a warm-up."""
+    saved, smp.factors = smp.factors, {}
     smp.step()
     est = smp.step()[0]
+    smp.factors = saved
     return {"full_frame_ms": full_ms, "sampled_estimate_ms": est, "relative_error": (est - full_ms) / full_ms}
 
 
@@ -541,8 +557,11 @@ def run_reference(args):
     if rank != 0:
         return 0
     sc = make_scene(args.small, args.image, args.spp, args.res)
-    check = sampler_error(sc)
+    full, full_det = cpu_full_frame(sc)
     smp = CpuFrameSample(sc).setup()
+    check = sampler_error(smp, full)
+    check["factors"] = smp.calibrate(full_det)
+    check["full_frame_stages_ms"] = {k: round(x, 3) for k, x in full_det.items()}
     for _ in range(args.warmup):
         smp.step()
     vals, det_acc = [], {}
@@ -712,10 +731,11 @@ def run_ours(args):
         # --impl reference arm uses checked against it
         from oracle import pyoracle as po
         full, det = cpu_full_frame(sc)
+        smp = CpuFrameSample(sc).setup()
         line["cpu_baseline"] = {"value": full, "unit": "ms/frame", "cores": int(po.load().lgo_threads()),
                                 "kind": "port", "sample": "the whole frame, timed once (nothing sampled or scaled)",
                                 "stages_ms": {k: round(x, 3) for k, x in det.items()},
-                                "sampler_check": sampler_error(sc, full)}
+                                "sampler_check": sampler_error(smp, full)}
     if rank == 0:
         print(json.dumps(line), flush=True)
     ctx.close()
