@@ -11,7 +11,10 @@ Compiles, in parallel and only when sources changed:
     (links both libraries);
   * oracle/_build/liblg_oracle.so                   -- the CPU oracle used by the
     tests and the CPU baseline (test infrastructure, never linked into the
-    product library).
+    product library);
+  * oracle/_ref/libref_randgen.so                   -- where the reference source
+    tree is present, its RandGen compiled from it (oracle/build_ref.py), which
+    the tests use to pin the oracle's random sequence.
 No CMake; nvcc and g++ only, so the same recipe runs on x86-64 and aarch64.
 """
 from __future__ import annotations
@@ -142,12 +145,21 @@ def build_oracle(verbose: bool = False) -> str:
     return out
 
 
+def build_reference_part(verbose: bool = False) -> None:
+    """oracle/_ref: the part of the reference that compiles here (its RandGen),
+    built by oracle/build_ref.py when the reference source tree is present
+    (test infrastructure; nothing is built without the tree)."""
+    _run([sys.executable, os.path.join(ORACLE_DIR, "build_ref.py")] + (["-v"] if verbose else []), verbose)
+
+
 def build_all(verbose: bool = False) -> None:
-    with cf.ThreadPoolExecutor(max_workers=2) as ex:
+    with cf.ThreadPoolExecutor(max_workers=3) as ex:
         a = ex.submit(build_library, verbose)
         b = ex.submit(build_oracle, verbose)
+        c = ex.submit(build_reference_part, verbose)
         a.result()
         b.result()
+        c.result()
 
 
 if __name__ == "__main__":

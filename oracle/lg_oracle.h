@@ -24,7 +24,10 @@
  * PARITY UNPINNED: the reference ships no tests, fixtures or golden vectors,
  * and cannot be built here (it needs OpenVDB, TBB, OpenEXR 2.x and Boost).
  * This restatement is pinned instead by known-answer tests (tests/test_oracle.py)
- * and by the golden fixtures it generates (tests/golden/).
+ * and by the golden fixtures it generates (tests/golden/). Its random
+ * sequence alone is pinned to the reference's code: src/RandGen.h, which
+ * needs none of those libraries, is compiled from the reference tree
+ * (oracle/build_ref.py) and compared draw for draw (tests/test_ref_randgen.py).
  *
  * OpenVDB behaviour the reference leans on is restated from its documented
  * semantics (OpenVDB 7/8 era; the reference pins no version):

@@ -6,7 +6,8 @@ compared with, or as the timed CPU baseline. The product package
 (lightgraph_gb300) never imports it.
 
 PARITY UNPINNED: the reference has no tests or fixtures and cannot be built
-here; see lg_oracle.h.
+here, except its RandGen, against which the random sequence is pinned; see
+lg_oracle.h.
 """
 from __future__ import annotations
 
