@@ -74,7 +74,10 @@ typedef struct lg_grid_desc {
 /* Uploads a grid once into the device brick layout (8^3 bricks, one padding
  * brick on every side, stored as storage_dtype; FP32 math on read). Replaces
  * the openvdb::io::File::readGrid + GridSampler set-up at src/main.cc:486-502.
- * Re-uploading replaces the previous grid of that kind. */
+ * Re-uploading replaces the previous grid of that kind. The padded box must
+ * lie within +-(2^22 - 64) voxels of index 0 on every axis (the marches work
+ * in FP32 index space) and hold fewer than 2^32 voxels; LG_ERR_INVALID
+ * otherwise. */
 lg_status lg_upload_grid(lg_ctx* ctx, int which, const lg_grid_desc* desc,
                          const float* values, int storage_dtype);
 
@@ -381,6 +384,11 @@ lg_status lg_fw_schedule(lg_ctx* ctx, int* schedule, double* tuned_ms, int n);
  * dependency waits, no stores), 2 CTAs per SM. Enqueued on the context's
  * stream and waited for. */
 lg_status lg_fw_inner_loop_rate(lg_ctx* ctx, double* tflops);
+/* Accuracy check of the primary wave's e^x - 1 (a Taylor series below
+ * |x| = 1/16, __expf(x) - 1 above): approx[i] is its value at x[i] and ref[i]
+ * the CUDA library's expm1f there, both computed on the device (host
+ * buffers, n entries). Enqueued on the context's stream and waited for. */
+lg_status lg_expm1_check(lg_ctx* ctx, const float* x, float* approx, float* ref, int32_t n);
 /* Host-only check of the persistent schedules' work queue for graphs of the
  * given point counts (no device work). Builds the queue the solve would use
  * (sym != 0: the symmetric solve of schedules 3 to 5, in its structural

@@ -73,6 +73,133 @@ __device__ __forceinline__ float jitter_step_bits(float step, uint32_t x) {
     return __fmul_rn(step, __fmaf_rn(__fsub_rn(f, 1.5f), 0.5f, 1.f));
 }
 
+// The same jittered step for the shadow rays in one rounding:
+// step * (0.75 + 0.5 u) = fma(1 + u, step / 2, step / 4), half = step / 2 and
+// quarter = step / 4 (both exact).
+__device__ __forceinline__ float jitter_step_fma(float half, float quarter, uint32_t x) {
+    return __fmaf_rn(__uint_as_float(0x3F800000u | (x >> 9)), half, quarter);
+}
+
+// Light::illuminate for the shadow rays: the point light's distance and
+// direction from one approximate reciprocal square root and its falloff from
+// one approximate reciprocal (within a few ulp of illuminate's IEEE forms).
+__device__ __forceinline__ void illuminate_shadow(const DevLight& L, const float p[3], float dir[3], float I[3],
+                                                  float& dist) {
+    if (L.type == 1) {
+        const float d[3] = {p[0] - L.pos[0], p[1] - L.pos[1], p[2] - L.pos[2]};
+        const float r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+        const float ri = rsqrtf(r2);
+        dist = r2 > 0.f ? r2 * ri : 0.f;
+        const float fall = __fdividef(1.f, 1.f + 4.f * 3.14159265358979323846f * r2);
+#pragma unroll
+        for (int c = 0; c < 3; ++c) { dir[c] = d[c] * ri; I[c] = L.I[c] * fall; }
+    } else {
+#pragma unroll
+        for (int c = 0; c < 3; ++c) { dir[c] = L.dir[c]; I[c] = L.I[c]; }
+        dist = kInf;
+    }
+}
+
+// make_iray with approximate reciprocals of the direction (exact at +-0,
+// where they give +-inf like the IEEE quotient).
+__device__ __forceinline__ void make_iray_approx(IRay& r, float ex, float ey, float ez, float dx, float dy, float dz,
+                                                 float t0, float t1) {
+    r.e[0] = ex; r.e[1] = ey; r.e[2] = ez;
+    r.d[0] = dx; r.d[1] = dy; r.d[2] = dz;
+    r.inv[0] = __fdividef(1.f, dx); r.inv[1] = __fdividef(1.f, dy); r.inv[2] = __fdividef(1.f, dz);
+    r.t0 = t0; r.t1 = t1;
+}
+
+// clip_to_bbox without branches: the same slab times per axis, t0 raised to
+// the near one and t1 lowered to the far one, the test once at the end (t0
+// only grows and t1 only shrinks, so it fails there exactly when it fails
+// after some axis). A NaN slab time (a zero direction component starting on
+// a slab plane) leaves its bound alone, as the slab test's comparisons do.
+__device__ __forceinline__ bool clip_to_bbox_flat(const DevGrid& g, IRay& r) {
+    float t0 = r.t0, t1 = r.t1;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        const float a = (g.bbmin[i] - r.e[i]) * r.inv[i];
+        const float b = (g.bbmax[i] - r.e[i]) * r.inv[i];
+        const bool sw = a > b;
+        t0 = fmaxf(t0, sw ? b : a);
+        t1 = fminf(t1, sw ? a : b);
+    }
+    r.t0 = t0;
+    r.t1 = t1;
+    return g.has_leaves && t0 <= t1;
+}
+
+// dda_axis from the floor bits of the start coordinate (|p| < 2^22, which
+// the grid upload guarantees): the same cell and first crossing, since the
+// bits with their low three cleared are ca * 8 (plus the bias). bias =
+// 0x4B400000 / 8 + blo - 1 turns bits >> 3 into the bitmap coordinate.
+__device__ __forceinline__ int dda_axis_bits(float e, float d, float inv, float t0, uint32_t bias, int& step,
+                                             float& next, float& delta) {
+    const float p = __fmaf_rn(t0, d, e);
+    float fl;
+    const uint32_t bits = floor_bits(p, fl);
+    const float c8 = __fsub_rn(__uint_as_float(bits & ~7u), 12582912.0f);  // ca * 8
+    const bool up = inv > 0.f;
+    const float plane = up ? __fadd_rn(c8, 8.f) : c8;
+    step = d == 0.f ? 0 : (up ? 1 : -1);
+    next = d == 0.f ? kInf : __fmaf_rn(__fsub_rn(plane, p), inv, t0);
+    delta = d == 0.f ? kInf : 8.f * fabsf(inv);
+    return (int)((bits >> 3) - bias);
+}
+
+// dda_init over dda_axis_bits.
+__device__ __forceinline__ void dda_init_bits(LeafDDA& s, const IRay& r, const DevGrid& g) {
+    s.t = r.t0;
+    s.tmax = r.t1;
+    s.done = false;
+    s.open = false;
+    s.start = 0.f;
+    constexpr uint32_t b8 = 0x4B400000u >> 3;
+    int sx, sy, sz;
+    const int cx = dda_axis_bits(r.e[0], r.d[0], r.inv[0], r.t0, b8 + (uint32_t)g.blo[0] - 1u, sx, s.nx, s.dx);
+    const int cy = dda_axis_bits(r.e[1], r.d[1], r.inv[1], r.t0, b8 + (uint32_t)g.blo[1] - 1u, sy, s.ny, s.dy);
+    const int cz = dda_axis_bits(r.e[2], r.d[2], r.inv[2], r.t0, b8 + (uint32_t)g.blo[2] - 1u, sz, s.nz, s.dz);
+    const bool in = (unsigned)cx < (unsigned)g.lbx && (unsigned)cy < (unsigned)g.lby &&
+                    (unsigned)cz < (unsigned)(g.nb[2] + 2);
+    s.lin = in ? cz * g.lbxy + cy * g.lbx + cx : (int)g.nbits;
+    s.ix = sx;
+    s.iy = sy * g.lbx;
+    s.iz = sz * g.lbxy;
+}
+
+// e^x - 1 for the primary wave's transmittance steps: for |x| < 1/16 the
+// Taylor series x + x^2/2! + ... + x^6/6! (the next term is below 2^-30 of
+// the result), beyond it __expf(x) - 1 (a few ulp of e^x, which at |x| = 1/16
+// is a relative error of about 2e-6 of the result). lg_expm1_check measures
+// it against the library's expm1f.
+__device__ __forceinline__ float expm1_approx(float x) {
+    if (fabsf(x) < 0.0625f) {
+        float q = __fmaf_rn(x, 1.f / 720.f, 1.f / 120.f);
+        q = __fmaf_rn(x, q, 1.f / 24.f);
+        q = __fmaf_rn(x, q, 1.f / 6.f);
+        q = __fmaf_rn(x, q, 0.5f);
+        return __fmaf_rn(__fmul_rn(x, x), q, x);
+    }
+    return __fsub_rn(__expf(x), 1.f);
+}
+
+__global__ void k_expm1_check(const float* __restrict__ x, float* __restrict__ approx, float* __restrict__ ref,
+                              int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) {
+        approx[i] = expm1_approx(x[i]);
+        ref[i] = expm1f(x[i]);
+    }
+}
+
+cudaError_t launch_expm1_check(const float* x, float* approx, float* ref, int n, cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    k_expm1_check<<<(n + 255) / 256, 256, 0, st>>>(x, approx, ref, n);
+    ++g_launch_counter;
+    return cudaGetLastError();
+}
+
 // Primary ray of pixel (i, j), sample s: PerspectiveCamera::getRay with the
 // offset 0.5 + (u - 0.5) in each axis, mapped to the density's index space.
 __device__ __forceinline__ bool primary_ray(const DevScene& sc, const DevCamera& cam, int i, int j, Stream stream,
@@ -93,7 +220,7 @@ __device__ __forceinline__ bool primary_ray(const DevScene& sc, const DevCamera&
     make_iray(pr, (cam.eye[0] - G.wo[0]) * G.inv_h, (cam.eye[1] - G.wo[1]) * G.inv_h,
               (cam.eye[2] - G.wo[2]) * G.inv_h, d[0], d[1], d[2], cam.znear * tscale * G.inv_h,
               cam.zfar * tscale * G.inv_h);
-    return clip_to_bbox(G, pr);
+    return clip_to_bbox_flat(G, pr);
 }
 
 // Per pixel-sample results of the primary wave.
@@ -125,7 +252,7 @@ __device__ __forceinline__ uint32_t primary_sample(const DevScene& sc, const Dev
     IRay pr;
     if (primary_ray(sc, cam, i, j, stream, pr)) {
         LeafDDA dda;
-        dda_init(dda, pr, G);
+        dda_init_bits(dda, pr, G);
         float ta, tb;
         uint32_t span_ord = 0, n_iter = 0;
         uint32_t jit = step_seed_primary(stream);
@@ -146,7 +273,7 @@ __device__ __forceinline__ uint32_t primary_sample(const DevScene& sc, const Dev
                 float omdT[3], dT[3];
 #pragma unroll
                 for (int c = 0; c < 3; ++c) {
-                    const float e1 = expm1f(-sh.a[c] * rho * pStep);
+                    const float e1 = expm1_approx(-sh.a[c] * rho * pStep);
                     dT[c] = 1.f + e1;
                     omdT[c] = -e1;
                 }
@@ -322,7 +449,9 @@ __device__ __forceinline__ int cube_face(const float w[3], float& x, float& y) {
     if (a0 >= a1 && a0 >= a2) { face = w[0] < 0.f; m = a0; x = w[1]; y = w[2]; }
     else if (a1 >= a2) { face = 2 + (w[1] < 0.f); m = a1; x = w[0]; y = w[2]; }
     else { face = 4 + (w[2] < 0.f); m = a2; x = w[0]; y = w[1]; }
-    const float inv = m > 0.f ? 1.f / m : 0.f;
+    // an approximate reciprocal: the bound tables' bins are widened by 1e-3
+    // of a bin, far more than its error
+    const float inv = m > 0.f ? __fdividef(1.f, m) : 0.f;
     x *= inv;
     y *= inv;
     return face;
@@ -425,7 +554,10 @@ __device__ __forceinline__ float shadow_ray_end(const RayBin& b, const float p[3
     const int f = cube_face(w, x, y);
     const int si = clamp_bin((x * 0.5f + 0.5f) * (float)b.ns, b.ns), ti = clamp_bin((y * 0.5f + 0.5f) * (float)b.ns, b.ns);
     const float dmin = __ldg(b.bound + ((int64_t)f * b.ns + ti) * b.ns + si);
-    return sqrtf(w[0] * w[0] + w[1] * w[1] + w[2] * w[2]) - dmin + 2.f;
+    // the distance from one approximate reciprocal square root (well inside
+    // the two-voxel margin)
+    const float r2 = w[0] * w[0] + w[1] * w[1] + w[2] * w[2];
+    return (r2 > 0.f ? r2 * rsqrtf(r2) : 0.f) - dmin + 2.f;
 }
 
 cudaError_t launch_ray_bins(const ShadowTask* tasks, const int32_t* total, int64_t task_cap, const RayBins& rb,
@@ -437,6 +569,30 @@ cudaError_t launch_ray_bins(const ShadowTask* tasks, const int32_t* total, int64
 
 // --- shadow rays -------------------------------------------------------------
 
+// The samples of one leaf span of a shadow ray, from t0 (a multiple of the
+// step) while they stay at or before sb and tau at or below the dropout
+// depth: tau += rho * step for each sample with rho at or above the cutoff,
+// rho = min(raw * scale, dmax) (kUnit: min(raw, dmax / scale), tau then in
+// units of 1 / scale; ShadowMarch). A sample below the cutoff adds nothing
+// and keeps its step (no re-jitter); the loop is branch-free, so the warp
+// stays converged. The step that the last sample still advances is not used.
+template <int DT, bool kUnit>
+__device__ __forceinline__ void shadow_span_samples(const DevGrid& G, const IRay& r, float t0, float sb, float half_step,
+                                                    float quarter_step, const ShadowMarch& sm, float& sStep,
+                                                    uint32_t& jit, uint32_t& siter, float& tau) {
+    for (float sT = t0; sT <= sb && tau <= sm.drop;) {
+        ++siter;
+        jit = step_next(jit);
+        const float raw = sample_span_t<DT>(G, r.e[0] + sT * r.d[0], r.e[1] + sT * r.d[1], r.e[2] + sT * r.d[2]);
+        const float rs = fminf(kUnit ? raw : raw * sm.scale, sm.dmax);
+        const bool take = rs >= sm.cut;
+        const float next = jitter_step_fma(half_step, quarter_step, jit);
+        tau = take ? fmaf(rs, sStep, tau) : tau;
+        sStep = take ? next : sStep;
+        sT += sStep;
+    }
+}
+
 // One thread per (light k, ordered slot r): the shadow rays of light k (all
 // its samples) from task kRayUnit * order[k * n_units + r / kRayUnit] +
 // r % kRayUnit; warps claim 32 consecutive (light, slot) pairs at a time from
@@ -445,7 +601,9 @@ cudaError_t launch_ray_bins(const ShadowTask* tasks, const int32_t* total, int64
 // direct[k * task_cap + t] = albedo * (sum_ls I * T / ns) * w.
 // kEnv = false leaves the environment-light branch out (no light of the
 // scene is an environment light), which frees registers for occupancy.
-template <int DT, bool kEnv>
+// kUnit = sc.smarch.unit: the density scale folded into the march constants
+// (ShadowMarch), one multiply per ray instead of one per sample.
+template <int DT, bool kEnv, bool kUnit>
 __global__ void __launch_bounds__(128, 8) k_shadow(DevScene sc, RayBins rb, const ShadowTask* __restrict__ tasks,
                                                 const int32_t* __restrict__ total_ptr, int64_t task_cap,
                                                 const int32_t* __restrict__ order, float4* __restrict__ direct,
@@ -455,8 +613,9 @@ __global__ void __launch_bounds__(128, 8) k_shadow(DevScene sc, RayBins rb, cons
     const uint64_t per_light = n_units * kRayUnit;
     const DevGrid& G = sc.dens;
     const DevShader& sh = sc.sh;
-    const float step1 = sc.step1, cutoff = sc.cutoff;
-    const float scale = sh.dS * sh.shadowDS;
+    const float step1 = sc.step1;
+    const float inv_step1 = 1.f / step1, half_step1 = 0.5f * step1, quarter_step1 = 0.25f * step1;
+    const ShadowMarch& sm = sc.smarch;
     uint32_t n_shadow = 0;
     // each warp claims the next 32 (light, ordered slot) pairs, lights in
     // order, until none are left: the warps stay busy to the end whatever
@@ -477,28 +636,32 @@ __global__ void __launch_bounds__(128, 8) k_shadow(DevScene sc, RayBins rb, cons
         }
         const int64_t t = (int64_t)order[k * n_units + rr / kRayUnit] * kRayUnit + (int64_t)(rr % kRayUnit);
         if (t >= total) continue;
-        const ShadowTask tk = tasks[t];
+        // the task's start point and stream words now, its weights after the
+        // march (not held in registers across it)
+        const float4 tk0 = __ldg(reinterpret_cast<const float4*>(tasks + t));
+        const uint2 tkw = __ldg(reinterpret_cast<const uint2*>(tasks + t) + 3);
+        const float tp[3] = {tk0.x, tk0.y, tk0.z};
         const DevLight& Lk = sc.lights[k];
         float lum[3] = {0.f, 0.f, 0.f};
         for (int ls = 0; ls < Lk.samples; ++ls) {
-            const uint32_t sub = shadow_key_from(tk.sa, tk.iw, (uint32_t)k, (uint32_t)ls);
+            const uint32_t sub = shadow_key_from(tkw.x, tkw.y, (uint32_t)k, (uint32_t)ls);
             float ldir[3], I[3], dist;
             if (kEnv && Lk.type == 2) {
                 env_illuminate(sc.env, Lk, draw_sub(sub, kTagEnvU), draw_sub(sub, kTagEnvV), ldir, I);
                 dist = kInf;
             } else {
-                const float pw[3] = {tk.p[0] * G.h + G.wo[0], tk.p[1] * G.h + G.wo[1], tk.p[2] * G.h + G.wo[2]};
-                illuminate(Lk, pw, ldir, I, dist);
+                const float pw[3] = {tp[0] * G.h + G.wo[0], tp[1] * G.h + G.wo[1], tp[2] * G.h + G.wo[2]};
+                illuminate_shadow(Lk, pw, ldir, I, dist);
             }
             IRay srr;
-            make_iray(srr, tk.p[0], tk.p[1], tk.p[2], -ldir[0], -ldir[1], -ldir[2], kDelta * G.inv_h,
-                      dist * G.inv_h);
-            if (!clip_to_bbox(G, srr)) continue;  // the reference skips the light sample
+            make_iray_approx(srr, tp[0], tp[1], tp[2], -ldir[0], -ldir[1], -ldir[2], kDelta * G.inv_h,
+                             dist * G.inv_h);
+            if (!clip_to_bbox_flat(G, srr)) continue;  // the reference skips the light sample
             // past the last leaf of the ray's light-space bin the walk finds no
             // span: stop it there (spans and samples are unchanged)
-            srr.t1 = fminf(srr.t1, fmaxf(shadow_ray_end(rb.b[k], tk.p), srr.t0));
+            srr.t1 = fminf(srr.t1, fmaxf(shadow_ray_end(rb.b[k], tp), srr.t0));
             LeafDDA sd;
-            dda_init(sd, srr, G);
+            dda_init_bits(sd, srr, G);
             float sa, sb, tau = 0.f;
             uint32_t sspan = 0, siter = 0;
             uint32_t jit = step_seed_shadow(sub);
@@ -509,31 +672,22 @@ __global__ void __launch_bounds__(128, 8) k_shadow(DevScene sc, RayBins rb, cons
                 // every jittered step is >= 0.75 step1: if that is not
                 // absorbed at sb, sT grows on every iteration up to sb
                 if (!(sb + 0.75f * step1 > sb)) continue;
-                for (float sT = step1 * ceilf(sa / step1); sT <= sb;) {
-                    ++siter;
-                    jit = step_next(jit);
-                    const float rs = fminf(sample_span_t<DT>(G, srr.e[0] + sT * srr.d[0], srr.e[1] + sT * srr.d[1],
-                                                             srr.e[2] + sT * srr.d[2]) * scale,
-                                           sh.dMax);
-                    // a sample below the cutoff adds nothing and keeps its
-                    // step (no re-jitter); branch-free, the warp stays converged
-                    const bool take = rs >= cutoff;
-                    const float next = jitter_step_bits(step1, jit);
-                    tau = take ? fmaf(rs, sStep, tau) : tau;
-                    if (tau > sh.tau_drop) { sdrop = true; break; }
-                    sStep = take ? next : sStep;
-                    sT += sStep;
-                }
+                shadow_span_samples<DT, kUnit>(G, srr, step1 * ceilf(sa * inv_step1), sb, half_step1, quarter_step1, sm,
+                                               sStep, jit, siter, tau);
+                sdrop = tau > sm.drop;
             }
             n_shadow += siter;
             if (sdrop) continue;
+            if (kUnit) tau *= sm.scale;
 #pragma unroll
             for (int c = 0; c < 3; ++c) lum[c] += I[c] * __expf(-sh.a[c] * tau);
         }
-        const float inv_ns = 1.f / (float)Lk.samples;
+        const float inv_ns = __fdividef(1.f, (float)Lk.samples);
+        const float2 w12 = __ldg(reinterpret_cast<const float2*>(tasks + t) + 2);
+        const float tw[3] = {tk0.w, w12.x, w12.y};
         float o[3];
 #pragma unroll
-        for (int c = 0; c < 3; ++c) o[c] = sh.albedo[c] * (lum[c] * inv_ns) * tk.w[c];
+        for (int c = 0; c < 3; ++c) o[c] = sh.albedo[c] * (lum[c] * inv_ns) * tw[c];
         direct[(int64_t)k * task_cap + t] = make_float4(o[0], o[1], o[2], 0.f);
     }
     {
@@ -654,24 +808,27 @@ cudaError_t launch_render_count(const DevScene& sc, const DevCamera& cam, const 
     return cudaGetLastError();
 }
 
-// Resident CTAs per SM of the k_shadow instance for (dtype, env), from the
-// occupancy calculator (once per instance; it enqueues no work, so it may run
-// while a stream is being captured).
-static int shadow_ctas_per_sm(int dtype, bool env) {
-    static std::atomic<int> cache[3][2];
-    std::atomic<int>& c = cache[dtype < 0 || dtype > 2 ? 0 : dtype][env ? 1 : 0];
+// The k_shadow instance for (dtype, env, unit).
+template <int DT>
+static const void* shadow_kernel_dt(bool env, bool unit) {
+    if (env) return unit ? (const void*)k_shadow<DT, true, true> : (const void*)k_shadow<DT, true, false>;
+    return unit ? (const void*)k_shadow<DT, false, true> : (const void*)k_shadow<DT, false, false>;
+}
+static const void* shadow_kernel(int dtype, bool env, bool unit) {
+    return dtype == 1 ? shadow_kernel_dt<1>(env, unit) : dtype == 2 ? shadow_kernel_dt<2>(env, unit)
+                                                                    : shadow_kernel_dt<0>(env, unit);
+}
+
+// Resident CTAs per SM of the k_shadow instance for (dtype, env, unit), from
+// the occupancy calculator (once per instance; it enqueues no work, so it
+// may run while a stream is being captured).
+static int shadow_ctas_per_sm(int dtype, bool env, bool unit) {
+    static std::atomic<int> cache[3][2][2];
+    if (dtype < 0 || dtype > 2) dtype = 0;
+    std::atomic<int>& c = cache[dtype][env ? 1 : 0][unit ? 1 : 0];
     if (c.load() == 0) {
         int n = 0;
-        cudaError_t e;
-        if (env) {
-            e = dtype == 1   ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_shadow<1, true>, 128, 0)
-                : dtype == 2 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_shadow<2, true>, 128, 0)
-                             : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_shadow<0, true>, 128, 0);
-        } else {
-            e = dtype == 1   ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_shadow<1, false>, 128, 0)
-                : dtype == 2 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_shadow<2, false>, 128, 0)
-                             : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_shadow<0, false>, 128, 0);
-        }
+        const cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, shadow_kernel(dtype, env, unit), 128, 0);
         c.store((e == cudaSuccess && n > 0) ? n : 8);
     }
     return c.load();
@@ -718,15 +875,17 @@ cudaError_t launch_render_shade(const DevScene& sc, const DevCamera& cam, const 
     bool env = false;
     for (int k = 0; k < sc.n_lights; ++k) env = env || sc.lights[k].type == 2;
     // one resident wave of CTAs; the threads stride over the rays
-    const unsigned sblocks = (unsigned)sms * (unsigned)shadow_ctas_per_sm(sc.dens.dtype, env);
-    if (env) {
-        if (sc.dens.dtype == 1) k_shadow<1, true><<<sblocks, 128, 0, st>>>(sc, ro.rb, tasks, total, task_cap, ro.order, direct, counters);
-        else if (sc.dens.dtype == 2) k_shadow<2, true><<<sblocks, 128, 0, st>>>(sc, ro.rb, tasks, total, task_cap, ro.order, direct, counters);
-        else k_shadow<0, true><<<sblocks, 128, 0, st>>>(sc, ro.rb, tasks, total, task_cap, ro.order, direct, counters);
-    } else {
-        if (sc.dens.dtype == 1) k_shadow<1, false><<<sblocks, 128, 0, st>>>(sc, ro.rb, tasks, total, task_cap, ro.order, direct, counters);
-        else if (sc.dens.dtype == 2) k_shadow<2, false><<<sblocks, 128, 0, st>>>(sc, ro.rb, tasks, total, task_cap, ro.order, direct, counters);
-        else k_shadow<0, false><<<sblocks, 128, 0, st>>>(sc, ro.rb, tasks, total, task_cap, ro.order, direct, counters);
+    const bool unit = sc.smarch.unit != 0;
+    const unsigned sblocks = (unsigned)sms * (unsigned)shadow_ctas_per_sm(sc.dens.dtype, env, unit);
+    {
+        DevScene scv = sc;
+        RayBins rbv = ro.rb;
+        const ShadowTask* tasks_c = tasks;
+        const int32_t* order_c = ro.order;
+        void* args[] = {&scv, &rbv, &tasks_c, (void*)&total, &task_cap, &order_c, &direct, &counters};
+        if ((e = cudaLaunchKernel(shadow_kernel(sc.dens.dtype, env, unit), dim3(sblocks), dim3(128), args, 0, st)) !=
+            cudaSuccess)
+            return e;
     }
     ++g_launch_counter;
     mark(2);

@@ -330,6 +330,11 @@ lg_status Ctx::upload_grid(int which, const lg_grid_desc* desc, const float* val
     // the samplers address cell records with 32-bit indices
     if ((uint64_t)g.nb[0] * g.nb[1] * g.nb[2] * 512ull >= (1ull << 32))
         return fail(LG_ERR_INVALID, "grid too large: the padded brick box must hold fewer than 2^32 voxels");
+    // the marches take floors of index-space coordinates from float bits
+    // (floor_bits), exact for |p| < 2^22: the padded box must lie inside that
+    for (int a = 0; a < 3; ++a)
+        if ((int64_t)g.blo[a] * 8 < -(int64_t)(1 << 22) + 64 || ((int64_t)g.blo[a] + g.nb[a]) * 8 > (1 << 22) - 64)
+            return fail(LG_ERR_INVALID, "grid index box must lie within +-2^22 voxels of the origin");
     for (int a = 0; a < 3; ++a) {
         g.vlo[a] = g.blo[a] * 8;
         g.vn[a] = (uint32_t)g.nb[a] * 8u;
@@ -337,12 +342,16 @@ lg_status Ctx::upload_grid(int which, const lg_grid_desc* desc, const float* val
     g.sy = (uint32_t)g.nb[0] * 512u;
     g.sz = (uint32_t)g.nb[0] * (uint32_t)g.nb[1] * 512u;
     g.rec_last = g.sz * (uint32_t)g.nb[2] - 1u;
+    g.ky = g.sy - 64u;
+    g.kz = g.sz - 512u;
     {
-        // span_cell's brick coordinates carry 0x4B400000 / 8 each (the floor
-        // bits' bias); brick_off removes it and the box's first brick
+        // span_cell's axis terms carry the floor bits' bias 0x4B400000 as
+        // 512 * (0x4B400000 / 8) per brick coordinate; rec_off removes it and
+        // the box's first brick (arithmetic mod 2^32)
         const uint32_t b8 = 0x4B400000u >> 3;
-        g.brick_off = 0u - ((uint32_t)g.blo[0] + b8) - ((uint32_t)g.blo[1] + b8) * (uint32_t)g.nb[0] -
-                      ((uint32_t)g.blo[2] + b8) * (uint32_t)g.nb[0] * (uint32_t)g.nb[1];
+        g.rec_off = 0u - ((uint32_t)g.blo[0] + b8 + ((uint32_t)g.blo[1] + b8) * (uint32_t)g.nb[0] +
+                          ((uint32_t)g.blo[2] + b8) * (uint32_t)g.nb[0] * (uint32_t)g.nb[1]) *
+                             512u;
     }
     const int64_t nvox = (int64_t)desc->dims[0] * desc->dims[1] * desc->dims[2];
     const int64_t nbt = (int64_t)g.nb[0] * g.nb[1] * g.nb[2];
@@ -352,6 +361,7 @@ lg_status Ctx::upload_grid(int which, const lg_grid_desc* desc, const float* val
     CK(gs.bricks.reserve(rec * nbt * 512), "brick alloc");
     g.lbx = g.nb[0] + 2;
     g.lby = g.nb[1] + 2;
+    g.lbxy = g.lbx * g.lby;
     g.nbits = (uint32_t)((int64_t)g.lbx * g.lby * (g.nb[2] + 2));
     const size_t bit_words = (size_t)g.nbits / 32 + 1;
     CK(gs.bits.reserve(sizeof(uint32_t) * bit_words), "leaf bitmap alloc");
@@ -550,6 +560,14 @@ DevScene Ctx::scene() const {
     sc.step0 = (float)settings.step[0];
     sc.step1 = (float)settings.step[1];
     sc.seed = settings.seed;
+    {
+        ShadowMarch& m = sc.smarch;
+        m.scale = d.dS * d.shadowDS;
+        m.unit = m.scale > 0.f && std::isfinite(m.scale) ? 1 : 0;
+        m.dmax = m.unit ? d.dMax / m.scale : d.dMax;
+        m.cut = m.unit ? sc.cutoff / m.scale : sc.cutoff;
+        m.drop = m.unit ? d.tau_drop / m.scale : d.tau_drop;
+    }
     return sc;
 }
 
@@ -1795,6 +1813,22 @@ extern "C" lg_status lg_fw_inner_loop_rate(lg_ctx* handle, double* tflops) {
     DevBuf scratch;
     CK(scratch.reserve(sizeof(float) * 2 * sms * 256), "scratch alloc");
     CK(fw_inner_loop_rate(scratch.as<float>(), sms, tflops, ctx->st), "inner loop rate");
+    return LG_OK;
+}
+
+extern "C" lg_status lg_expm1_check(lg_ctx* handle, const float* x, float* approx, float* ref, int32_t n) {
+    Ctx* ctx = reinterpret_cast<Ctx*>(handle);
+    GUARD(ctx);
+    if (n < 0 || (n > 0 && (!x || !approx || !ref))) return ctx->fail(LG_ERR_INVALID, "bad expm1 check arguments");
+    if (n == 0) return LG_OK;
+    DevBuf buf;
+    CK(buf.reserve(sizeof(float) * 3 * (size_t)n), "expm1 check alloc");
+    float* dx = buf.as<float>();
+    CK(cudaMemcpyAsync(dx, x, sizeof(float) * n, cudaMemcpyHostToDevice, ctx->st), "expm1 check upload");
+    CK(launch_expm1_check(dx, dx + n, dx + 2 * (size_t)n, n, ctx->st), "expm1 check");
+    CK(cudaMemcpyAsync(approx, dx + n, sizeof(float) * n, cudaMemcpyDeviceToHost, ctx->st), "expm1 check read");
+    CK(cudaMemcpyAsync(ref, dx + 2 * (size_t)n, sizeof(float) * n, cudaMemcpyDeviceToHost, ctx->st), "expm1 check read");
+    CK(cudaStreamSynchronize(ctx->st), "sync");
     return LG_OK;
 }
 

@@ -48,13 +48,15 @@ struct DevGrid {
     float bbmax[3] = {0.f, 0.f, 0.f};    // ... max leaf origin + 8
     int has_leaves = 0;
     uint32_t sy = 0, sz = 0;             // record strides of one brick step in y and z
-    uint32_t brick_off = 0;              // span_cell's brick index offset (mod 2^32)
+    uint32_t ky = 0, kz = 0;             // sy - 64 and sz - 512 (span_cell)
+    uint32_t rec_off = 0;                // span_cell's record index offset (mod 2^32)
     uint32_t rec_last = 0;               // last record (a padding cell)
     // The leaf bitmap covers the brick box plus a margin of one brick on
     // every side (bits 0), so a walker one cell off the box reads "no leaf"
     // without per-axis bounds checks: bit ((z + 1) * lby + y + 1) * lbx + x + 1
     // for box brick (x, y, z).
     int lbx = 0, lby = 0;                // bitmap cells per row and per column (nb + 2)
+    int lbxy = 0;                        // lbx * lby
     uint32_t nbits = 0;                  // bitmap cells
 };
 
@@ -116,26 +118,23 @@ __device__ __forceinline__ uint32_t span_cell(const DevGrid& g, float px, float 
     wx = px - fx;
     wy = py - fy;
     wz = pz - fz;
-    // The bias 0x4B400000 is a multiple of 8: the low three bits are the
-    // offsets inside the brick, and bits >> 3 are the brick coordinates plus
-    // 0x4B400000 / 8, which brick_off cancels together with the box's first
-    // brick.
-    const uint32_t brick = (bx >> 3) + (by >> 3) * (uint32_t)g.nb[0] + (bz >> 3) * (g.sz >> 9) + g.brick_off;
-    const uint32_t rec = brick * 512u + (((bz & 7u) << 6) | ((by & 7u) << 3) | (bx & 7u));
+    // Record of cell (x, y, z): brick (x >> 3, y >> 3, z >> 3) times 512 plus
+    // the offset (z & 7) * 64 + (y & 7) * 8 + (x & 7) inside it. With
+    // x & 7 = x - 8 (x >> 3) it is linear per axis:
+    //   x + 504 (x >> 3) + 8 y + (sy - 64) (y >> 3) + 64 z + (sz - 512) (z >> 3)
+    // The bits carry the bias B = 0x4B400000, a multiple of 8, so bits >> 3
+    // carry B / 8 and the terms carry (512 + sy + sz) B / 8 in all; rec_off
+    // removes that and moves the box's first brick to record 0 (mod 2^32).
+    const uint32_t rec = bx + 504u * (bx >> 3) + 8u * by + g.ky * (by >> 3) + 64u * bz + g.kz * (bz >> 3) + g.rec_off;
     return min(rec, g.rec_last);
 }
 
-// Trilinear sample at an index-space position for storage type DT: the eight
-// voxels around floor(p), interpolated along z, then y, then x (the order of
-// OpenVDB's BoxSampler::trilinearInterpolation), each step
-// fmaf(b - a, w, a). The z and y steps run two lanes at a time in packed
-// FP32 (same rounding per lane as the scalar form).
-template <int DT>
-__device__ __forceinline__ float sample_index_t(const DevGrid& g, float px, float py, float pz) {
-    const float fx = floorf(px), fy = floorf(py), fz = floorf(pz);
-    const float wx = px - fx, wy = py - fy, wz = pz - fz;
-    float v[8];
-    ld_cell<DT>(g.data, cell_record(g, (int)fx, (int)fy, (int)fz), v);
+// The interpolation of a cell record's eight values (a + 2b + 4c order) at
+// weights (wx, wy, wz): along z, then y, then x (the order of OpenVDB's
+// BoxSampler::trilinearInterpolation), each step fmaf(b - a, w, a). The z and
+// y steps run two lanes at a time in packed FP32 (same rounding per lane as
+// the scalar form).
+__device__ __forceinline__ float trilinear8(const float v[8], float wx, float wy, float wz) {
     const float2 wz2 = make_float2(wz, wz), wy2 = make_float2(wy, wy);
     // lanes (x0, x1) at y0 and at y1, interpolated along z
     const float2 a0 = make_float2(v[0], v[1]), b0 = make_float2(v[4], v[5]);
@@ -147,6 +146,16 @@ __device__ __forceinline__ float sample_index_t(const DevGrid& g, float px, floa
     return fmaf(y.y - y.x, wx, y.x);
 }
 
+// Trilinear sample at an index-space position for storage type DT: the eight
+// voxels around floor(p), interpolated by trilinear8.
+template <int DT>
+__device__ __forceinline__ float sample_index_t(const DevGrid& g, float px, float py, float pz) {
+    const float fx = floorf(px), fy = floorf(py), fz = floorf(pz);
+    float v[8];
+    ld_cell<DT>(g.data, cell_record(g, (int)fx, (int)fy, (int)fz), v);
+    return trilinear8(v, px - fx, py - fy, pz - fz);
+}
+
 // sample_index_t for a position inside a leaf span of g (span_cell): the same
 // eight values and the same interpolation, without the box test.
 template <int DT>
@@ -154,13 +163,7 @@ __device__ __forceinline__ float sample_span_t(const DevGrid& g, float px, float
     float wx, wy, wz;
     float v[8];
     ld_cell<DT>(g.data, span_cell(g, px, py, pz, wx, wy, wz), v);
-    const float2 wz2 = make_float2(wz, wz), wy2 = make_float2(wy, wy);
-    const float2 a0 = make_float2(v[0], v[1]), b0 = make_float2(v[4], v[5]);
-    const float2 a1 = make_float2(v[2], v[3]), b1 = make_float2(v[6], v[7]);
-    const float2 z0 = __ffma2_rn(__fadd2_rn(b0, make_float2(-a0.x, -a0.y)), wz2, a0);
-    const float2 z1 = __ffma2_rn(__fadd2_rn(b1, make_float2(-a1.x, -a1.y)), wz2, a1);
-    const float2 y = __ffma2_rn(__fadd2_rn(z1, make_float2(-z0.x, -z0.y)), wy2, z0);
-    return fmaf(y.y - y.x, wx, y.x);
+    return trilinear8(v, wx, wy, wz);
 }
 
 // Value of voxel (x, y, z): the first entry of its cell's record (0 outside
@@ -296,10 +299,13 @@ __device__ __forceinline__ bool walker_leaf(const DevGrid& g, int lin) {
 // smallest, else y if below z, else z); returns false once the crossing
 // lies past tmax.
 __device__ __forceinline__ bool walker_step(LeafDDA& s) {
-    const bool ax = (s.nx < s.ny) && (s.nx < s.nz);
-    const bool ay = !(s.nx < s.ny) && (s.ny < s.nz);
+    // x strictly first: nx < min(ny, nz); else y if ny < nz (then nx >= ny);
+    // else z. The crossing taken is the smallest of the three either way.
+    const float myz = fminf(s.ny, s.nz);
+    const bool ax = s.nx < myz;
+    const bool ay = !ax && (s.ny < s.nz);
     const bool az = !ax && !ay;
-    s.t = ax ? s.nx : (ay ? s.ny : s.nz);
+    s.t = fminf(s.nx, myz);
     if (ax) { s.nx += s.dx; s.lin += s.ix; }
     if (ay) { s.ny += s.dy; s.lin += s.iy; }
     if (az) { s.nz += s.dz; s.lin += s.iz; }
@@ -396,6 +402,17 @@ struct DevEnv {
     int w = 0, h = 0;
 };
 
+// Constants of the shadow-ray march (k_shadow). A sample's density is
+// min(raw * scale, dMax), scale = dS * shadowDS; it counts when at or above
+// the cutoff, and the ray drops once tau passes tau_drop. With unit set
+// (scale positive and finite) the march accumulates raw density x step
+// against dmax, cut and drop divided by scale and multiplies tau by scale
+// once per ray; otherwise dmax, cut and drop are the plain values.
+struct ShadowMarch {
+    int unit;
+    float scale, dmax, cut, drop;
+};
+
 struct DevScene {
     DevGrid dens, temp;
     int has_temp;
@@ -405,6 +422,7 @@ struct DevScene {
     DevEnv env;
     float cutoff, step0, step1;
     uint64_t seed;
+    ShadowMarch smarch;
 };
 
 // ColorRamp::getColor (src/Shader.h:63-92), including its edge behaviour.

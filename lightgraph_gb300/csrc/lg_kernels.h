@@ -178,6 +178,9 @@ cudaError_t launch_ray_bins(const ShadowTask* tasks, const int32_t* total, int64
 // rb.b[k].ns^2 floats, kind 1: 6 * ns^2, zeroed or set to +inf first by the
 // caller as bound_init gives): one thread per leaf-bitmap cell.
 cudaError_t launch_ray_bounds(const DevGrid& g, const RayBins& rb, cudaStream_t st);
+// expm1_approx (the primary wave's e^x - 1) and expm1f at n points, for the
+// accuracy check behind lg_expm1_check.
+cudaError_t launch_expm1_check(const float* x, float* approx, float* ref, int n, cudaStream_t st);
 // Initial value of a light's bound table entries (bits of a non-negative float).
 inline uint32_t bound_init(const RayBin& b) { return b.kind == 0 ? 0u : 0x7F800000u; }
 inline int64_t bound_entries(const RayBin& b) {

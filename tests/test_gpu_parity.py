@@ -249,3 +249,39 @@ def test_render_wave_times_after_lg_render(gpu_ctx, small_scene, small_solved):
         gpu_ctx.lib.lg_set_profiling(gpu_ctx.h, 0)
     assert all(w > 0 for w in waves), waves
     assert sum(waves) < wall_ms
+
+
+def test_grid_index_box_limit():
+    """The marches take floors of index-space coordinates from float bits,
+    exact below 2^22 voxels: a grid whose padded brick box (one brick of
+    margin) reaches past +-(2^22 - 64) is refused, one just inside is taken."""
+    from lightgraph_gb300 import Context, Grid, LightGraphError
+    ctx = Context(0)
+    try:
+        vals = np.ones((8, 8, 8), np.float32)
+        lim = 1 << 22
+        for origin in [(lim - 128, 0, 0), (-lim + 128, 0, 0), (0, lim - 128, 0), (0, 0, -lim + 128)]:
+            ctx.upload_density(Grid(vals, origin, 0.01))
+        for origin in [(lim - 64, 0, 0), (-lim + 64, 0, 0), (0, lim, 0), (0, 0, -lim)]:
+            with pytest.raises(LightGraphError):
+                ctx.upload_density(Grid(vals, origin, 0.01))
+    finally:
+        ctx.close()
+
+
+def test_expm1_approx_vs_library(gpu_ctx):
+    """The primary wave's e^x - 1 (the Taylor series below |x| = 1/16,
+    __expf(x) - 1 above) against the CUDA library's expm1f on the device,
+    over the arguments its transmittance steps take (x <= 0, -extinction x
+    density x step): relative error <= 4e-6."""
+    from lightgraph_gb300 import _capi
+    x = np.concatenate([-np.logspace(-10, np.log10(60.0), 40000),
+                        [0.0, -0.0625, np.nextafter(np.float32(-0.0625), np.float32(0)),
+                         np.nextafter(np.float32(-0.0625), np.float32(-1))]]).astype(np.float32)
+    a = np.empty_like(x)
+    r = np.empty_like(x)
+    st = gpu_ctx.lib.lg_expm1_check(gpu_ctx.h, _capi.ptr(x), _capi.ptr(a), _capi.ptr(r), len(x))
+    assert st == _capi.LG_OK
+    ref = r.astype(np.float64)
+    rel = np.abs(a.astype(np.float64) - ref) / np.maximum(np.abs(ref), 1e-38)
+    assert rel.max() <= 4e-6, (float(rel.max()), float(x[np.argmax(rel)]))
