@@ -31,7 +31,11 @@
 
 namespace lg {
 
-// Trilinear Vec3 sample of the coarse scatter grid (0 outside the box).
+// Trilinear Vec3 sample of the coarse scatter grid (0 outside the box). A
+// footprint wholly inside the box (the common case) loads its eight corners
+// from one base index; one that reaches past a face tests every corner. The
+// lerps run the R and G channels as one packed pair (the same rounding per
+// channel as fmaf(b - a, w, a)).
 __device__ __forceinline__ void sample_scatter(const DevScatterGrid& sg, float wx, float wy, float wz,
                                                float out[3]) {
     const float px = wx * sg.inv_H, py = wy * sg.inv_H, pz = wz * sg.inv_H;
@@ -39,21 +43,37 @@ __device__ __forceinline__ void sample_scatter(const DevScatterGrid& sg, float w
     const int ix = (int)fx - sg.lo[0], iy = (int)fy - sg.lo[1], iz = (int)fz - sg.lo[2];
     const float u = px - fx, v = py - fy, w = pz - fz;
     float4 c[2][2][2];
+    if ((unsigned)ix < (unsigned)max(sg.dims[0] - 1, 0) && (unsigned)iy < (unsigned)max(sg.dims[1] - 1, 0) &&
+        (unsigned)iz < (unsigned)max(sg.dims[2] - 1, 0)) {
+        const int64_t sy = sg.dims[0], sz = (int64_t)sg.dims[0] * sg.dims[1];
+        const float4* b = sg.v + ((int64_t)iz * sz + (int64_t)iy * sy + ix);
 #pragma unroll
-    for (int a = 0; a < 2; ++a)
+        for (int d = 0; d < 2; ++d)
 #pragma unroll
-        for (int b = 0; b < 2; ++b)
-#pragma unroll
-            for (int d = 0; d < 2; ++d) {
-                const int x = ix + a, y = iy + b, z = iz + d;
-                if ((unsigned)x < (unsigned)sg.dims[0] && (unsigned)y < (unsigned)sg.dims[1] &&
-                    (unsigned)z < (unsigned)sg.dims[2])
-                    c[a][b][d] = __ldg(sg.v + ((int64_t)z * sg.dims[1] + y) * sg.dims[0] + x);
-                else
-                    c[a][b][d] = make_float4(0.f, 0.f, 0.f, 0.f);
+            for (int bb = 0; bb < 2; ++bb) {
+                const float4* row = b + d * sz + bb * sy;
+                c[0][bb][d] = __ldg(row);
+                c[1][bb][d] = __ldg(row + 1);
             }
+    } else {
+#pragma unroll
+        for (int a = 0; a < 2; ++a)
+#pragma unroll
+            for (int bb = 0; bb < 2; ++bb)
+#pragma unroll
+                for (int d = 0; d < 2; ++d) {
+                    const int x = ix + a, y = iy + bb, z = iz + d;
+                    if ((unsigned)x < (unsigned)sg.dims[0] && (unsigned)y < (unsigned)sg.dims[1] &&
+                        (unsigned)z < (unsigned)sg.dims[2])
+                        c[a][bb][d] = __ldg(sg.v + ((int64_t)z * sg.dims[1] + y) * sg.dims[0] + x);
+                    else
+                        c[a][bb][d] = make_float4(0.f, 0.f, 0.f, 0.f);
+                }
+    }
     auto l = [](float4 p, float4 q, float t) {
-        return make_float4(lerpf(p.x, q.x, t), lerpf(p.y, q.y, t), lerpf(p.z, q.z, t), 0.f);
+        const float2 rg = __ffma2_rn(__fadd2_rn(make_float2(q.x, q.y), make_float2(-p.x, -p.y)), make_float2(t, t),
+                                     make_float2(p.x, p.y));
+        return make_float4(rg.x, rg.y, lerpf(p.z, q.z, t), 0.f);
     };
     const float4 r = l(l(l(c[0][0][0], c[0][0][1], w), l(c[0][1][0], c[0][1][1], w), v),
                        l(l(c[1][0][0], c[1][0][1], w), l(c[1][1][0], c[1][1][1], w), v), u);
@@ -701,10 +721,14 @@ __global__ void __launch_bounds__(128, 8) k_shadow(DevScene sc, RayBins rb, cons
 // One warp per pixel. Its samples run side by side, G lanes each (G a power
 // of two, spp * G <= 32, so 32 / G samples per pass): lane l of a sample's
 // group sums the sample's tasks l, l + G, ... (a task's direct light is the
-// sum of its lights' contributions in light order), a butterfly inside the
-// group combines the lanes, and lane 0 (whose summation order is fixed)
-// takes the samples in order to form the antialiasing averages.
-__global__ void __launch_bounds__(128) k_resolve(DevCamera cam, const int32_t* __restrict__ offsets,
+// sum of its lights' contributions in light order; two tasks' loads are
+// issued before either is added), a butterfly inside the group combines the
+// lanes, and lane 0 (whose summation order is fixed) takes the samples in
+// order to form the antialiasing averages. Each group's first lane loads its
+// sample's primary-wave results up front, in parallel with the task loads,
+// and hands them to lane 0 by shuffles. 8 CTAs per SM (64 registers, a few
+// bytes spilled) hide the loads' latency better than 7 without spills.
+__global__ void __launch_bounds__(128, 8) k_resolve(DevCamera cam, const int32_t* __restrict__ offsets,
                                                  const int32_t* __restrict__ counts,
                                                  const PixelSample* __restrict__ pss,
                                                  const float4* __restrict__ direct, int n_lights, int64_t task_cap,
@@ -723,20 +747,40 @@ __global__ void __launch_bounds__(128) k_resolve(DevCamera cam, const int32_t* _
     for (int s0 = 0; s0 < spp; s0 += per_pass) {
         const int s = s0 + lane / G;
         float d[3] = {0.f, 0.f, 0.f};
+        float o[9] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};  // scat, emis, trans
         if (s < spp) {
             const int64_t ps = pix * spp + s;
-            const int64_t b = offsets[ps], e = min((int64_t)b + counts[ps], task_cap);
-            for (int64_t t = b + gl; t < e; t += G) {
-                float acc[3] = {0.f, 0.f, 0.f};
-                for (int k = 0; k < n_lights; ++k) {
-                    const float4 v = direct[(int64_t)k * task_cap + t];
-                    acc[0] += v.x;
-                    acc[1] += v.y;
-                    acc[2] += v.z;
+            if (gl == 0) {
+                const PixelSample q = pss[ps];
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    o[c] = q.scat[c];
+                    o[3 + c] = q.emis[c];
+                    o[6 + c] = q.trans[c];
                 }
-                d[0] += acc[0];
-                d[1] += acc[1];
-                d[2] += acc[2];
+            }
+            const int64_t b = offsets[ps], e = min((int64_t)b + counts[ps], task_cap);
+            for (int64_t t = b + gl; t < e; t += 2 * G) {
+                const bool two = t + G < e;
+                float acc0[3] = {0.f, 0.f, 0.f}, acc1[3] = {0.f, 0.f, 0.f};
+                for (int k = 0; k < n_lights; ++k) {
+                    const float4 v0 = direct[(int64_t)k * task_cap + t];
+                    const float4 v1 = two ? direct[(int64_t)k * task_cap + t + G] : make_float4(0.f, 0.f, 0.f, 0.f);
+                    acc0[0] += v0.x;
+                    acc0[1] += v0.y;
+                    acc0[2] += v0.z;
+                    acc1[0] += v1.x;
+                    acc1[1] += v1.y;
+                    acc1[2] += v1.z;
+                }
+                d[0] += acc0[0];
+                d[1] += acc0[1];
+                d[2] += acc0[2];
+                if (two) {
+                    d[0] += acc1[0];
+                    d[1] += acc1[1];
+                    d[2] += acc1[2];
+                }
             }
         }
         for (int off = G >> 1; off > 0; off >>= 1)
@@ -744,18 +788,19 @@ __global__ void __launch_bounds__(128) k_resolve(DevCamera cam, const int32_t* _
             for (int c = 0; c < 3; ++c) d[c] += __shfl_xor_sync(0xffffffffu, d[c], off);
         const int ns = min(per_pass, spp - s0);
         for (int jj = 0; jj < ns; ++jj) {
-            float dj[3];
+            float dj[3], oj[9];
 #pragma unroll
             for (int c = 0; c < 3; ++c) dj[c] = __shfl_sync(0xffffffffu, d[c], jj * G);
+#pragma unroll
+            for (int c = 0; c < 9; ++c) oj[c] = __shfl_sync(0xffffffffu, o[c], jj * G);
             if (lane == 0) {
-                const PixelSample o = pss[pix * spp + s0 + jj];
 #pragma unroll
                 for (int c = 0; c < 3; ++c) {
-                    lAA[c] += (dj[c] + o.scat[c] + o.emis[c]) * ratio;
+                    lAA[c] += (dj[c] + oj[c] + oj[3 + c]) * ratio;
                     dAA[c] += dj[c] * ratio;
-                    sAA[c] += o.scat[c] * ratio;
-                    eAA[c] += o.emis[c] * ratio;
-                    tAA[c] += o.trans[c] * ratio;
+                    sAA[c] += oj[c] * ratio;
+                    eAA[c] += oj[3 + c] * ratio;
+                    tAA[c] += oj[6 + c] * ratio;
                 }
             }
         }
