@@ -47,10 +47,17 @@ __device__ float sample_exact(const DevGrid& g, double px, double py, double pz)
     const double fx = floor(px), fy = floor(py), fz = floor(pz);
     const double u = px - fx, w = py - fy, t = pz - fz;
     float v[8];
-    const uint32_t rec = cell_record(g, (int)fx, (int)fy, (int)fz);
-    if (g.dtype == 1) ld_cell<1>(g.data, rec, v);
-    else if (g.dtype == 2) ld_cell<2>(g.data, rec, v);
-    else ld_cell<0>(g.data, rec, v);
+    const int ix = (int)fx, iy = (int)fy, iz = (int)fz;
+    if (g.dtype == 0) {
+        // FP32 records hold the polynomial: each corner is the first entry
+        // (the voxel itself) of its own cell's record
+#pragma unroll
+        for (int c = 0; c < 8; ++c) v[c] = voxel(g, ix + (c & 1), iy + ((c >> 1) & 1), iz + (c >> 2));
+    } else {
+        const uint32_t rec = cell_record(g, ix, iy, iz);
+        if (g.dtype == 1) ld_cell<1>(g.data, rec, v);
+        else ld_cell<2>(g.data, rec, v);
+    }
     auto lerp = [](float a, float b, double wt) {
         const double tmp = __dmul_rn((double)__fsub_rn(b, a), wt);
         return __fadd_rn(a, __double2float_rn(tmp));
@@ -68,7 +75,11 @@ __device__ float sample_exact(const DevGrid& g, double px, double py, double pz)
 // cell the trilinear sample moves by at most 3 * (max tap - min tap) per voxel
 // of position error index_err (FP32 rounding of wo, of 1 / h and of the
 // subtraction and product); the seven FP32 interpolations add under 2^-19 of
-// the largest tap.
+// the largest tap. For an FP32 record (the polynomial k0 + ...) S = sum of
+// |k| over the non-constant terms stands in for the taps' spread: every
+// partial derivative is at most S and every tap lies within S of k0; its
+// coefficients (rounded once) and their four FP32 steps add under 2^-21 of
+// |k0| + S.
 __device__ __forceinline__ bool density_passes(const DevGrid& g, const float p[3], const DartParams& prm) {
     const float ix = (p[0] - prm.wo_f[0]) * prm.inv_h_f, iy = (p[1] - prm.wo_f[1]) * prm.inv_h_f,
                 iz = (p[2] - prm.wo_f[2]) * prm.inv_h_f;
@@ -76,19 +87,31 @@ __device__ __forceinline__ bool density_passes(const DevGrid& g, const float p[3
     const float u = ix - fx, w = iy - fy, t = iz - fz;
     float v[8];
     const uint32_t rec = cell_record(g, (int)fx, (int)fy, (int)fz);
-    if (g.dtype == 1) ld_cell<1>(g.data, rec, v);
-    else if (g.dtype == 2) ld_cell<2>(g.data, rec, v);
-    else ld_cell<0>(g.data, rec, v);
-    float lo = v[0], hi = v[0];
+    float val, spread, mag;
+    if (g.dtype == 0) {
+        ld_cell<0>(g.data, rec, v);
+        val = trilinear_coefs(v, u, w, t);
+        float sum = 0.f;
 #pragma unroll
-    for (int k = 1; k < 8; ++k) { lo = fminf(lo, v[k]); hi = fmaxf(hi, v[k]); }
-    auto lerp = [](float a, float b, float wt) { return fmaf(b - a, wt, a); };
-    const float x0 = lerp(lerp(v[0], v[4], t), lerp(v[2], v[6], t), w);
-    const float x1 = lerp(lerp(v[1], v[5], t), lerp(v[3], v[7], t), w);
-    const float val = lerp(x0, x1, u);
+        for (int k = 1; k < 8; ++k) sum += fabsf(v[k]);
+        spread = sum * (1.f + 1e-6f);
+        mag = fabsf(v[0]) + spread;
+    } else {
+        if (g.dtype == 1) ld_cell<1>(g.data, rec, v);
+        else ld_cell<2>(g.data, rec, v);
+        float lo = v[0], hi = v[0];
+#pragma unroll
+        for (int k = 1; k < 8; ++k) { lo = fminf(lo, v[k]); hi = fmaxf(hi, v[k]); }
+        auto lerp = [](float a, float b, float wt) { return fmaf(b - a, wt, a); };
+        const float x0 = lerp(lerp(v[0], v[4], t), lerp(v[2], v[6], t), w);
+        const float x1 = lerp(lerp(v[1], v[5], t), lerp(v[3], v[7], t), w);
+        val = lerp(x0, x1, u);
+        spread = hi - lo;
+        mag = fmaxf(fabsf(hi), fabsf(lo));
+    }
     const float e2 = 2.f * prm.index_err;
     const bool near_face = u < e2 || u > 1.f - e2 || w < e2 || w > 1.f - e2 || t < e2 || t > 1.f - e2;
-    const float bound = 3.f * (hi - lo) * prm.index_err + fmaxf(fabsf(hi), fabsf(lo)) * 2e-6f + 1e-30f;
+    const float bound = 3.f * spread * prm.index_err + mag * 2e-6f + 1e-30f;
     if (!near_face) {
         if (val < prm.cutoff - bound) return false;
         if (val > prm.cutoff + bound) return true;

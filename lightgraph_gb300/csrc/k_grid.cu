@@ -42,9 +42,12 @@ __global__ void k_pack_bricks(const float* __restrict__ dense, int dx, int dy, i
                    : 0.f;
     }
     if (g.dtype == 0) {
+        // FP32 records hold the cell's trilinear polynomial (cell_coefs)
+        float c[8];
+        cell_coefs(v, c);
         float4* o = reinterpret_cast<float4*>(bricks) + 2 * t;
-        o[0] = make_float4(v[0], v[1], v[2], v[3]);
-        o[1] = make_float4(v[4], v[5], v[6], v[7]);
+        o[0] = make_float4(c[0], c[1], c[2], c[3]);
+        o[1] = make_float4(c[4], c[5], c[6], c[7]);
     } else {
         uint32_t w[4];
 #pragma unroll

@@ -23,8 +23,9 @@ constexpr float kDelta = 1e-9f;
 // 8^3 bricks (x fastest inside a brick, bricks x fastest in the box) with one
 // brick of zero padding on every side. A cell's record holds the eight voxel
 // values of its trilinear footprint, v(x + a, y + b, z + c) at index
-// a + 2b + 4c, so one sample is one aligned 32-byte (FP32) or 16-byte
-// (FP16/BF16) load instead of eight gathers. A brick's 512 records are one
+// a + 2b + 4c (FP16/BF16), or the eight coefficients of its trilinear
+// polynomial (FP32, cell_coefs), so one sample is one aligned 32-byte (FP32)
+// or 16-byte (FP16/BF16) load instead of eight gathers. A brick's 512 records are one
 // contiguous 16 KB block, so a ray crossing a brick in any direction stays in
 // one block (rays that run along z would otherwise touch a new page at every
 // voxel). Voxels outside the box read the background value 0. The box's first
@@ -63,7 +64,28 @@ struct DevGrid {
 // Bytes of one cell record for storage type dtype.
 __host__ __device__ constexpr int cell_record_bytes(int dtype) { return dtype == 0 ? 32 : 16; }
 
-// The eight values of record rec, decoded to FP32 (a + 2b + 4c order).
+// Coefficients of a cell's trilinear polynomial from its eight voxel values
+// v[a + 2b + 4c] = v(x + a, y + b, z + c), in the FP32 record order
+//   c[0..7] = {k0, kx, kz, kxz, ky, kxy, kyz, kxyz}
+// where v(wx, wy, wz) = (k0 + kz wz) + (ky + kyz wz) wy
+//                     + ((kx + kxz wz) + (kxy + kxyz wz) wy) wx.
+// The sums are exact in FP64 for float inputs of like magnitude and are
+// rounded once; k0 is the voxel v(x, y, z) itself.
+__host__ __device__ inline void cell_coefs(const float v[8], float c[8]) {
+    const double v000 = v[0], v100 = v[1], v010 = v[2], v110 = v[3];
+    const double v001 = v[4], v101 = v[5], v011 = v[6], v111 = v[7];
+    c[0] = (float)v000;
+    c[1] = (float)(v100 - v000);
+    c[2] = (float)(v001 - v000);
+    c[3] = (float)((v101 - v100) - (v001 - v000));
+    c[4] = (float)(v010 - v000);
+    c[5] = (float)((v110 - v100) - (v010 - v000));
+    c[6] = (float)((v011 - v010) - (v001 - v000));
+    c[7] = (float)(((v111 - v110) - (v101 - v100)) - ((v011 - v010) - (v001 - v000)));
+}
+
+// The raw eight values of record rec, decoded to FP32 (FP16/BF16: voxel
+// values in a + 2b + 4c order; FP32: cell_coefs).
 template <int DT>
 __device__ __forceinline__ void ld_cell(const void* data, uint32_t rec, float v[8]) {
     if (DT == 0) {
@@ -146,28 +168,45 @@ __device__ __forceinline__ float trilinear8(const float v[8], float wx, float wy
     return fmaf(y.y - y.x, wx, y.x);
 }
 
-// Trilinear sample at an index-space position for storage type DT: the eight
-// voxels around floor(p), interpolated by trilinear8.
+// The trilinear polynomial of an FP32 record (cell_coefs) at weights (wx,
+// wy, wz): the z terms of both wx halves as one packed pair, then y, then x.
+__device__ __forceinline__ float trilinear_coefs(const float c[8], float wx, float wy, float wz) {
+    const float2 wz2 = make_float2(wz, wz), wy2 = make_float2(wy, wy);
+    // lanes (without wx, with wx)
+    const float2 a = __ffma2_rn(make_float2(c[2], c[3]), wz2, make_float2(c[0], c[1]));  // (k0, kx) + (kz, kxz) wz
+    const float2 b = __ffma2_rn(make_float2(c[6], c[7]), wz2, make_float2(c[4], c[5]));  // (ky, kxy) + (kyz, kxyz) wz
+    const float2 y = __ffma2_rn(b, wy2, a);
+    return fmaf(y.y, wx, y.x);
+}
+
+// The interpolation of record values for storage type DT.
+template <int DT>
+__device__ __forceinline__ float record_sample(const float v[8], float wx, float wy, float wz) {
+    return DT == 0 ? trilinear_coefs(v, wx, wy, wz) : trilinear8(v, wx, wy, wz);
+}
+
+// Trilinear sample at an index-space position for storage type DT: the cell
+// record at floor(p) (the eight voxels around it, or their polynomial).
 template <int DT>
 __device__ __forceinline__ float sample_index_t(const DevGrid& g, float px, float py, float pz) {
     const float fx = floorf(px), fy = floorf(py), fz = floorf(pz);
     float v[8];
     ld_cell<DT>(g.data, cell_record(g, (int)fx, (int)fy, (int)fz), v);
-    return trilinear8(v, px - fx, py - fy, pz - fz);
+    return record_sample<DT>(v, px - fx, py - fy, pz - fz);
 }
 
 // sample_index_t for a position inside a leaf span of g (span_cell): the same
-// eight values and the same interpolation, without the box test.
+// record and the same interpolation, without the box test.
 template <int DT>
 __device__ __forceinline__ float sample_span_t(const DevGrid& g, float px, float py, float pz) {
     float wx, wy, wz;
     float v[8];
     ld_cell<DT>(g.data, span_cell(g, px, py, pz, wx, wy, wz), v);
-    return trilinear8(v, wx, wy, wz);
+    return record_sample<DT>(v, wx, wy, wz);
 }
 
-// Value of voxel (x, y, z): the first entry of its cell's record (0 outside
-// the box).
+// Value of voxel (x, y, z): the first entry of its cell's record (the voxel
+// itself in both record forms; 0 outside the box).
 __device__ __forceinline__ float voxel(const DevGrid& g, int x, int y, int z) {
     const size_t off = (size_t)cell_record(g, x, y, z) * 8;
     if (g.dtype == 0) return __ldg(reinterpret_cast<const float*>(g.data) + off);
