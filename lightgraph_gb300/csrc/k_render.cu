@@ -11,10 +11,13 @@
 //   (exclusive scan of the counts)
 //   k_primary<true>  : march again, accumulate the scatter and emission AOVs
 //                      and write one shadow task per shading sample
-//                      (position, pTrans * (1 - dT), stream words);
-//   k_ray_bins       : order each light's shadow rays by a light-space key
-//                      (counting sort: count, scan, scatter), so the rays in
-//                      flight are neighbouring, parallel rays;
+//                      (position, pTrans * (1 - dT), stream words), and the
+//                      light-space order key of each pair of tasks per light
+//                      with a count per key;
+//   (exclusive scan of the key counts)
+//   k_ray_scatter    : order each light's shadow rays by their keys (the
+//                      counting sort's scatter), so the rays in flight are
+//                      neighbouring, parallel rays;
 //   k_shadow         : one thread per (light, ordered pair of tasks) marches
 //                      that light's shadow rays (all its samples) and writes
 //                      the light's contribution to the task's slot;
@@ -243,6 +246,46 @@ __device__ __forceinline__ bool primary_ray(const DevScene& sc, const DevCamera&
     return clip_to_bbox_flat(G, pr);
 }
 
+// The low 16 bits of v spread to the even bits (Morton order of two bin
+// indices).
+__device__ __forceinline__ uint32_t spread_bits16(uint32_t v) {
+    v &= 0xFFFFu;
+    v = (v | (v << 8)) & 0x00FF00FFu;
+    v = (v | (v << 4)) & 0x0F0F0F0Fu;
+    v = (v | (v << 2)) & 0x33333333u;
+    v = (v | (v << 1)) & 0x55555555u;
+    return v;
+}
+__device__ __forceinline__ int clamp_bin(float x, int n) { return min(max((int)x, 0), n - 1); }
+
+// Key of the shadow ray of light b for the task at index-space position p.
+__device__ __forceinline__ int64_t ray_key(const RayBin& b, const float p[3], int64_t t) {
+    if (b.kind == 2) return b.key_off + (t >> b.shift);
+    int64_t uv;
+    float depth;
+    if (b.kind == 0) {
+        const float u = p[0] * b.U[0] + p[1] * b.U[1] + p[2] * b.U[2] - b.u0;
+        const float v = p[0] * b.V[0] + p[1] * b.V[1] + p[2] * b.V[2] - b.v0;
+        uv = spread_bits16((uint32_t)clamp_bin(u * b.inv_bs, b.ns)) |
+             (spread_bits16((uint32_t)clamp_bin(v * b.inv_bs, b.ns)) << 1);
+        depth = p[0] * b.D[0] + p[1] * b.D[1] + p[2] * b.D[2] - b.d0;
+    } else {
+        const float w0 = p[0] - b.O[0], w1 = p[1] - b.O[1], w2 = p[2] - b.O[2];
+        const float a0 = fabsf(w0), a1 = fabsf(w1), a2 = fabsf(w2);
+        int face;
+        float m, x, y;
+        if (a0 >= a1 && a0 >= a2) { face = w0 < 0.f; m = a0; x = w1; y = w2; }
+        else if (a1 >= a2) { face = 2 + (w1 < 0.f); m = a1; x = w0; y = w2; }
+        else { face = 4 + (w2 < 0.f); m = a2; x = w0; y = w1; }
+        const float inv = m > 0.f ? 0.5f / m : 0.f;
+        uv = (int64_t)face * b.ns * b.ns +
+             (spread_bits16((uint32_t)clamp_bin((x * inv + 0.5f) * (float)b.ns, b.ns)) |
+              (spread_bits16((uint32_t)clamp_bin((y * inv + 0.5f) * (float)b.ns, b.ns)) << 1));
+        depth = sqrtf(w0 * w0 + w1 * w1 + w2 * w2) - b.d0;
+    }
+    return b.key_off + uv * b.nd + clamp_bin(depth * b.inv_ds, b.nd);
+}
+
 // Per pixel-sample results of the primary wave.
 struct PixelSample {
     float scat[3], emis[3], trans[3];
@@ -259,7 +302,8 @@ template <bool kWrite, int DT>
 __device__ __forceinline__ uint32_t primary_sample(const DevScene& sc, const DevCamera& cam, const DevScatterGrid& sg,
                                                    int64_t ps, int32_t* __restrict__ counts,
                                                    const int32_t* __restrict__ offsets, ShadowTask* __restrict__ tasks,
-                                                   int64_t task_cap, PixelSample* __restrict__ out) {
+                                                   int64_t task_cap, PixelSample* __restrict__ out,
+                                                   const RayOrder& ko) {
     uint32_t n_primary = 0;
     const int64_t pix = ps / cam.spp;
     const int i = (int)(pix % cam.width), j = (int)(pix / cam.width);
@@ -317,6 +361,16 @@ __device__ __forceinline__ uint32_t primary_sample(const DevScene& sc, const Dev
                         tk.sa = stream.a;
                         tk.iw = shadow_iter_word(stream, n);
                         tasks[t] = tk;
+                        // the first task of a unit files the unit under each
+                        // light's order key (the shadow-ray ordering's count)
+                        if ((t & (kRayUnit - 1)) == 0) {
+                            const int64_t u = t / kRayUnit;
+                            for (int k = 0; k < ko.rb.n; ++k) {
+                                const uint32_t key = (uint32_t)ray_key(ko.rb.b[k], p, t);
+                                ko.keys[k * ko.unit_cap + u] = key;
+                                atomicAdd(ko.key_counts + key, 1);
+                            }
+                        }
                     }
 #pragma unroll
                     for (int c = 0; c < 3; ++c) {
@@ -355,7 +409,7 @@ __global__ void __launch_bounds__(128, kWrite ? 5 : 6) k_primary(DevScene sc, De
                                                  int32_t* __restrict__ counts, const int32_t* __restrict__ offsets,
                                                  ShadowTask* __restrict__ tasks, int64_t task_cap,
                                                  PixelSample* __restrict__ out, unsigned long long* __restrict__ ctr,
-                                                 unsigned long long* __restrict__ claim) {
+                                                 unsigned long long* __restrict__ claim, RayOrder ko) {
     const int64_t n_ps = (int64_t)cam.width * cam.height * cam.spp;
     const int lane = threadIdx.x & 31;
     uint32_t n_primary = 0;
@@ -366,7 +420,7 @@ __global__ void __launch_bounds__(128, kWrite ? 5 : 6) k_primary(DevScene sc, De
         if ((int64_t)claimed >= n_ps) break;
         const int64_t ps = (int64_t)claimed + lane;
         if (ps < n_ps)
-            n_primary += primary_sample<kWrite, DT>(sc, cam, sg, ps, counts, offsets, tasks, task_cap, out);
+            n_primary += primary_sample<kWrite, DT>(sc, cam, sg, ps, counts, offsets, tasks, task_cap, out, ko);
     }
     if (kWrite && ctr) {
         unsigned long long q = n_primary;
@@ -378,82 +432,36 @@ __global__ void __launch_bounds__(128, kWrite ? 5 : 6) k_primary(DevScene sc, De
 
 // --- shadow-ray ordering ---------------------------------------------------
 
-__device__ __forceinline__ uint32_t spread_bits16(uint32_t v) {
-    v &= 0xFFFFu;
-    v = (v | (v << 8)) & 0x00FF00FFu;
-    v = (v | (v << 4)) & 0x0F0F0F0Fu;
-    v = (v | (v << 2)) & 0x33333333u;
-    v = (v | (v << 1)) & 0x55555555u;
-    return v;
-}
-__device__ __forceinline__ int clamp_bin(float x, int n) { return min(max((int)x, 0), n - 1); }
-
-// Key of the shadow ray of light b for the task at index-space position p.
-__device__ __forceinline__ int64_t ray_key(const RayBin& b, const float p[3], int64_t t) {
-    if (b.kind == 2) return b.key_off + (t >> b.shift);
-    int64_t uv;
-    float depth;
-    if (b.kind == 0) {
-        const float u = p[0] * b.U[0] + p[1] * b.U[1] + p[2] * b.U[2] - b.u0;
-        const float v = p[0] * b.V[0] + p[1] * b.V[1] + p[2] * b.V[2] - b.v0;
-        uv = spread_bits16((uint32_t)clamp_bin(u * b.inv_bs, b.ns)) |
-             (spread_bits16((uint32_t)clamp_bin(v * b.inv_bs, b.ns)) << 1);
-        depth = p[0] * b.D[0] + p[1] * b.D[1] + p[2] * b.D[2] - b.d0;
-    } else {
-        const float w0 = p[0] - b.O[0], w1 = p[1] - b.O[1], w2 = p[2] - b.O[2];
-        const float a0 = fabsf(w0), a1 = fabsf(w1), a2 = fabsf(w2);
-        int face;
-        float m, x, y;
-        if (a0 >= a1 && a0 >= a2) { face = w0 < 0.f; m = a0; x = w1; y = w2; }
-        else if (a1 >= a2) { face = 2 + (w1 < 0.f); m = a1; x = w0; y = w2; }
-        else { face = 4 + (w2 < 0.f); m = a2; x = w0; y = w1; }
-        const float inv = m > 0.f ? 0.5f / m : 0.f;
-        uv = (int64_t)face * b.ns * b.ns +
-             (spread_bits16((uint32_t)clamp_bin((x * inv + 0.5f) * (float)b.ns, b.ns)) |
-              (spread_bits16((uint32_t)clamp_bin((y * inv + 0.5f) * (float)b.ns, b.ns)) << 1));
-        depth = sqrtf(w0 * w0 + w1 * w1 + w2 * w2) - b.d0;
-    }
-    return b.key_off + uv * b.nd + clamp_bin(depth * b.inv_ds, b.nd);
-}
-
-// Warp-aggregated counting sort passes over units of kRayUnit consecutive
-// tasks (neighbouring shading samples of one primary ray, keyed by the first
-// one), so lanes with equal keys share one atomic. Within a key the order is
-// whatever the atomics give; every ray's result goes to its own slot, so
-// results do not depend on it.
-__global__ void __launch_bounds__(256) k_ray_bins(const ShadowTask* __restrict__ tasks,
-                                                  const int32_t* __restrict__ total_ptr, int64_t task_cap,
-                                                  RayBins rb, int32_t* __restrict__ counts,
-                                                  int32_t* __restrict__ order) {
+// Scatter pass of the warp-aggregated counting sort over units of kRayUnit
+// consecutive tasks (neighbouring shading samples of one primary ray, keyed
+// by the first one): the shading pass has filed every unit under each
+// light's key and counted the keys, the counts have been scanned into
+// offsets, and here lanes with equal keys share one atomic. Within a key the
+// order is whatever the atomics give; every ray's result goes to its own
+// slot, so results do not depend on it.
+__global__ void __launch_bounds__(256) k_ray_scatter(const uint32_t* __restrict__ keys, int64_t unit_cap,
+                                                     int n_lights, const int32_t* __restrict__ total_ptr,
+                                                     int64_t task_cap, int32_t* __restrict__ offsets,
+                                                     int32_t* __restrict__ order) {
     const int64_t total = min((int64_t)*total_ptr, task_cap);
     const int64_t n_units = (total + kRayUnit - 1) / kRayUnit;
     const int lane = threadIdx.x & 31;
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < n_units; base += stride) {
-        const int64_t u = base + threadIdx.x;
-        const bool valid = u < n_units;
-        float p[3] = {0.f, 0.f, 0.f};
-        if (valid) {
-            const float4 q = __ldg(reinterpret_cast<const float4*>(tasks + u * kRayUnit));
-            p[0] = q.x;
-            p[1] = q.y;
-            p[2] = q.z;
-        }
-        for (int k = 0; k < rb.n; ++k) {
+    for (int k = 0; k < n_lights; ++k) {
+        const uint32_t* kk = keys + (int64_t)k * unit_cap;
+        for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < n_units; base += stride) {
+            const int64_t u = base + threadIdx.x;
+            const bool valid = u < n_units;
             // keys index the counts array (fewer than 2^31 of them, checked by
             // the host), so the cheaper 32-bit match groups them
-            const uint32_t key = valid ? (uint32_t)ray_key(rb.b[k], p, u * kRayUnit) : 0xFFFFFFFFu;
+            const uint32_t key = valid ? kk[u] : 0xFFFFFFFFu;
             const unsigned grp = __match_any_sync(0xffffffffu, key);
             if (!valid) continue;
             const int leader = __ffs(grp) - 1;
-            if (order == nullptr) {
-                if (lane == leader) atomicAdd(counts + key, __popc(grp));
-            } else {
-                int32_t pos = 0;
-                if (lane == leader) pos = atomicAdd(counts + key, __popc(grp));
-                pos = __shfl_sync(grp, pos, leader);
-                order[pos + __popc(grp & ((1u << lane) - 1u))] = (int32_t)u;
-            }
+            int32_t pos = 0;
+            if (lane == leader) pos = atomicAdd(offsets + key, __popc(grp));
+            pos = __shfl_sync(grp, pos, leader);
+            order[pos + __popc(grp & ((1u << lane) - 1u))] = (int32_t)u;
         }
     }
 }
@@ -580,9 +588,9 @@ __device__ __forceinline__ float shadow_ray_end(const RayBin& b, const float p[3
     return (r2 > 0.f ? r2 * rsqrtf(r2) : 0.f) - dmin + 2.f;
 }
 
-cudaError_t launch_ray_bins(const ShadowTask* tasks, const int32_t* total, int64_t task_cap, const RayBins& rb,
-                            int32_t* counts, int32_t* order, int sms, cudaStream_t st) {
-    k_ray_bins<<<(unsigned)sms * 8u, 256, 0, st>>>(tasks, total, task_cap, rb, counts, order);
+cudaError_t launch_ray_scatter(const uint32_t* keys, int64_t unit_cap, int n_lights, const int32_t* total,
+                               int64_t task_cap, int32_t* offsets, int32_t* order, int sms, cudaStream_t st) {
+    k_ray_scatter<<<(unsigned)sms * 8u, 256, 0, st>>>(keys, unit_cap, n_lights, total, task_cap, offsets, order);
     ++g_launch_counter;
     return cudaGetLastError();
 }
@@ -844,11 +852,11 @@ cudaError_t launch_render_count(const DevScene& sc, const DevCamera& cam, const 
     const unsigned blocks = (unsigned)std::min<int64_t>((n_ps + 127) / 128,
                                                         (int64_t)sms * primary_ctas_per_sm(false, sc.dens.dtype));
     if (sc.dens.dtype == 1)
-        k_primary<false, 1><<<blocks, 128, 0, st>>>(sc, cam, sg, counts, nullptr, nullptr, 0, nullptr, nullptr, claim);
+        k_primary<false, 1><<<blocks, 128, 0, st>>>(sc, cam, sg, counts, nullptr, nullptr, 0, nullptr, nullptr, claim, RayOrder{});
     else if (sc.dens.dtype == 2)
-        k_primary<false, 2><<<blocks, 128, 0, st>>>(sc, cam, sg, counts, nullptr, nullptr, 0, nullptr, nullptr, claim);
+        k_primary<false, 2><<<blocks, 128, 0, st>>>(sc, cam, sg, counts, nullptr, nullptr, 0, nullptr, nullptr, claim, RayOrder{});
     else
-        k_primary<false, 0><<<blocks, 128, 0, st>>>(sc, cam, sg, counts, nullptr, nullptr, 0, nullptr, nullptr, claim);
+        k_primary<false, 0><<<blocks, 128, 0, st>>>(sc, cam, sg, counts, nullptr, nullptr, 0, nullptr, nullptr, claim, RayOrder{});
     ++g_launch_counter;
     return cudaGetLastError();
 }
@@ -894,26 +902,28 @@ cudaError_t launch_render_shade(const DevScene& sc, const DevCamera& cam, const 
         if (marks && marks[k]) cudaEventRecord(marks[k], st);
     };
     cudaError_t e;
+    // the shading pass also files every unit of shadow rays under its order
+    // keys and counts them (the counts zeroed first)
+    if (ro.rb.n > 0 && (e = cudaMemsetAsync(ro.key_counts, 0, sizeof(int32_t) * ro.n_keys, st)) != cudaSuccess)
+        return e;
     if (sc.dens.dtype == 1)
         k_primary<true, 1><<<blocks, 128, 0, st>>>(sc, cam, sg, nullptr, offsets, tasks, task_cap, pss, counters,
-                                                   counters + 4);
+                                                   counters + 4, ro);
     else if (sc.dens.dtype == 2)
         k_primary<true, 2><<<blocks, 128, 0, st>>>(sc, cam, sg, nullptr, offsets, tasks, task_cap, pss, counters,
-                                                   counters + 4);
+                                                   counters + 4, ro);
     else
         k_primary<true, 0><<<blocks, 128, 0, st>>>(sc, cam, sg, nullptr, offsets, tasks, task_cap, pss, counters,
-                                                   counters + 4);
+                                                   counters + 4, ro);
     ++g_launch_counter;
     mark(0);
-    // order the shadow rays: count keys, scan, scatter task indices
+    // order the shadow rays: scan the key counts, scatter the units
     if (ro.rb.n > 0) {
-        if ((e = cudaMemsetAsync(ro.key_counts, 0, sizeof(int32_t) * ro.n_keys, st)) != cudaSuccess) return e;
-        if ((e = launch_ray_bins(tasks, total, task_cap, ro.rb, ro.key_counts, nullptr, sms, st)) != cudaSuccess)
-            return e;
         if ((e = launch_exclusive_scan(ro.key_counts, ro.n_keys, ro.key_offsets, ro.key_scan, ro.key_total, st)) !=
             cudaSuccess)
             return e;
-        if ((e = launch_ray_bins(tasks, total, task_cap, ro.rb, ro.key_offsets, ro.order, sms, st)) != cudaSuccess)
+        if ((e = launch_ray_scatter(ro.keys, ro.unit_cap, ro.rb.n, total, task_cap, ro.key_offsets, ro.order, sms,
+                                    st)) != cudaSuccess)
             return e;
     }
     mark(1);

@@ -1579,11 +1579,12 @@ lg_status Ctx::render(const lg_camera* c) {
     if (!capturing) {
         CK(d_task_direct.reserve(direct_bytes), "shadow task alloc");
         CK(d_ray_order.reserve(order_bytes), "ray order alloc");
+        CK(d_ray_keys.reserve(order_bytes), "ray order alloc");
         CK(d_ray_counts.reserve(key_bytes), "ray order alloc");
         CK(d_ray_offsets.reserve(key_bytes), "ray order alloc");
         CK(d_ray_scan.reserve(scan_bytes), "ray order alloc");
         CK(d_ray_total.reserve(sizeof(int32_t) * 2), "ray order alloc");
-    } else if (d_task_direct.bytes < direct_bytes || d_ray_order.bytes < order_bytes ||
+    } else if (d_task_direct.bytes < direct_bytes || d_ray_order.bytes < order_bytes || d_ray_keys.bytes < order_bytes ||
                d_ray_counts.bytes < key_bytes || d_ray_offsets.bytes < key_bytes || d_ray_scan.bytes < scan_bytes ||
                d_ray_total.bytes < sizeof(int32_t) * 2) {
         return fail(LG_ERR_STATE, "render buffers changed size during graph capture");
@@ -1613,6 +1614,8 @@ lg_status Ctx::render(const lg_camera* c) {
     ro.key_scan = d_ray_scan.as<int32_t>();
     ro.key_total = d_ray_total.as<int32_t>();
     ro.order = d_ray_order.as<int32_t>();
+    ro.keys = d_ray_keys.as<uint32_t>();
+    ro.unit_cap = (cap + kRayUnit - 1) / kRayUnit;
     int sms = 0;
     CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device), "device query");
     CK(launch_render_shade(sc, cam, sg, d_ps_count.as<int32_t>(), d_ps_offset.as<int32_t>(), d_ps_total.as<int32_t>(),

@@ -147,7 +147,7 @@ struct Ctx {
     DevBuf d_rgba, d_direct, d_scatter, d_emission, d_counters;
     DevBuf d_ps_count, d_ps_offset, d_ps_scan, d_ps_total, d_ps_data, d_tasks, d_task_direct;
     // shadow-ray ordering: key histogram, its scan, the ordered task indices
-    DevBuf d_ray_counts, d_ray_offsets, d_ray_scan, d_ray_total, d_ray_order;
+    DevBuf d_ray_counts, d_ray_offsets, d_ray_scan, d_ray_total, d_ray_order, d_ray_keys;
     DevBuf d_ray_bounds;  // occupancy bound tables of the lights' bins
     bool capturing = false;  // inside a CUDA graph capture: no host syncs
 

@@ -170,10 +170,11 @@ struct RayBins {
     int n;
 };
 constexpr int kRayUnit = 2;  // consecutive tasks ordered as one unit
-// Count pass (order == null: counts[key] += rays) or scatter pass (counts
-// holds the exclusive scan; order[counts[key]++] = task) over all lights.
-cudaError_t launch_ray_bins(const ShadowTask* tasks, const int32_t* total, int64_t task_cap, const RayBins& rb,
-                            int32_t* counts, int32_t* order, int sms, cudaStream_t st);
+// Scatter pass of the shadow-ray order over all lights: offsets holds the
+// exclusive scan of the per-key unit counts; order[offsets[key]++] = unit,
+// the keys read from keys (n_lights rows of unit_cap).
+cudaError_t launch_ray_scatter(const uint32_t* keys, int64_t unit_cap, int n_lights, const int32_t* total,
+                               int64_t task_cap, int32_t* offsets, int32_t* order, int sms, cudaStream_t st);
 // Fills the occupancy bounds of every light of rb with a bound table (kind 0:
 // rb.b[k].ns^2 floats, kind 1: 6 * ns^2, zeroed or set to +inf first by the
 // caller as bound_init gives): one thread per leaf-bitmap cell.
@@ -198,6 +199,10 @@ struct RayOrder {
     RayBins rb;
     int64_t n_keys;
     int32_t *key_counts, *key_offsets, *key_scan, *key_total, *order;
+    // the order key of every unit and light (light k's keys from
+    // k * unit_cap), written by the primary shading pass with the counts
+    uint32_t* keys;
+    int64_t unit_cap;
 };
 // Waves 2-5 given the exclusive scan of the counts (offsets, device total):
 // primary shading, shadow-ray ordering, shadow rays, resolve. direct holds

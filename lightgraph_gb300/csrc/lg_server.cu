@@ -144,7 +144,8 @@ extern "C" uint64_t lg_request_bytes(const lg_request* q) {
     b += P * 4 * (3 + 3 + 3 + 3 * kRowChunks);         // L, D, weights, partial sums
     b += (uint64_t)q->camera.width * q->camera.height * 64;  // four films
     // per pixel sample: shading count, offset and primary results (the shadow
-    // tasks depend on the volume and are not counted)
+    // tasks, their order keys and per-light results depend on the volume and
+    // are not counted)
     b += (uint64_t)q->camera.width * q->camera.height * (uint64_t)std::max(q->camera.samples, 1) * 44;
     b += 160ull * 160 * 160 * 12;                      // point bins (upper bound)
     if (q->env_rgb && q->env_w > 1 && q->env_h > 1)  // env map and its CDFs
