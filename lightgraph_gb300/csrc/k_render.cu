@@ -30,9 +30,13 @@
 // the launch shape; the reference's render RNG depends on TBB's row split.
 #include <atomic>
 
+#include <cooperative_groups.h>
+
 #include "lg_kernels.h"
 
 namespace lg {
+
+namespace cg = cooperative_groups;
 
 // Trilinear Vec3 sample of the coarse scatter grid (0 outside the box). A
 // footprint wholly inside the box (the common case) loads its eight corners
@@ -258,10 +262,15 @@ __device__ __forceinline__ uint32_t spread_bits16(uint32_t v) {
 }
 __device__ __forceinline__ int clamp_bin(float x, int n) { return min(max((int)x, 0), n - 1); }
 
-// Key of the shadow ray of light b for the task at index-space position p.
-__device__ __forceinline__ int64_t ray_key(const RayBin& b, const float p[3], int64_t t) {
-    if (b.kind == 2) return b.key_off + (t >> b.shift);
-    int64_t uv;
+// Key of the shadow ray of light b for the task at index-space position p:
+// its light-space bin (Morton order of the (u, v) or cube-map bins) and its
+// depth bin, after the keys of the lights before it. The host keeps every
+// key below 2^31, so the arithmetic is 32-bit; the point light's cube-map
+// coordinates and distance come from approximate reciprocals (the key only
+// decides the order in which rays are marched).
+__device__ __forceinline__ uint32_t ray_key(const RayBin& b, const float p[3], int64_t t) {
+    if (b.kind == 2) return (uint32_t)(b.key_off + (t >> b.shift));
+    uint32_t uv;
     float depth;
     if (b.kind == 0) {
         const float u = p[0] * b.U[0] + p[1] * b.U[1] + p[2] * b.U[2] - b.u0;
@@ -272,18 +281,19 @@ __device__ __forceinline__ int64_t ray_key(const RayBin& b, const float p[3], in
     } else {
         const float w0 = p[0] - b.O[0], w1 = p[1] - b.O[1], w2 = p[2] - b.O[2];
         const float a0 = fabsf(w0), a1 = fabsf(w1), a2 = fabsf(w2);
-        int face;
+        uint32_t face;
         float m, x, y;
         if (a0 >= a1 && a0 >= a2) { face = w0 < 0.f; m = a0; x = w1; y = w2; }
         else if (a1 >= a2) { face = 2 + (w1 < 0.f); m = a1; x = w0; y = w2; }
         else { face = 4 + (w2 < 0.f); m = a2; x = w0; y = w1; }
-        const float inv = m > 0.f ? 0.5f / m : 0.f;
-        uv = (int64_t)face * b.ns * b.ns +
+        const float inv = m > 0.f ? __fdividef(0.5f, m) : 0.f;
+        uv = face * (uint32_t)b.ns * (uint32_t)b.ns +
              (spread_bits16((uint32_t)clamp_bin((x * inv + 0.5f) * (float)b.ns, b.ns)) |
               (spread_bits16((uint32_t)clamp_bin((y * inv + 0.5f) * (float)b.ns, b.ns)) << 1));
-        depth = sqrtf(w0 * w0 + w1 * w1 + w2 * w2) - b.d0;
+        const float r2 = w0 * w0 + w1 * w1 + w2 * w2;
+        depth = (r2 > 0.f ? r2 * rsqrtf(r2) : 0.f) - b.d0;
     }
-    return b.key_off + uv * b.nd + clamp_bin(depth * b.inv_ds, b.nd);
+    return (uint32_t)b.key_off + uv * (uint32_t)b.nd + (uint32_t)clamp_bin(depth * b.inv_ds, b.nd);
 }
 
 // Per pixel-sample results of the primary wave.
@@ -365,10 +375,16 @@ __device__ __forceinline__ uint32_t primary_sample(const DevScene& sc, const Dev
                         // light's order key (the shadow-ray ordering's count)
                         if ((t & (kRayUnit - 1)) == 0) {
                             const int64_t u = t / kRayUnit;
-                            for (int k = 0; k < ko.rb.n; ++k) {
-                                const uint32_t key = (uint32_t)ray_key(ko.rb.b[k], p, t);
+                            // unrolled over the light slots, so each light's
+                            // bin parameters are read as constants
+#pragma unroll
+                            for (int k = 0; k < kMaxLights; ++k) {
+                                if (k >= ko.rb.n) break;
+                                const uint32_t key = ray_key(ko.rb.b[k], p, t);
                                 ko.keys[k * ko.unit_cap + u] = key;
-                                atomicAdd(ko.key_counts + key, 1);
+                                // lanes filing under the same key share one atomic
+                                const cg::coalesced_group grp = cg::labeled_partition(cg::coalesced_threads(), key);
+                                if (grp.thread_rank() == 0) atomicAdd(ko.key_counts + key, (int)grp.size());
                             }
                         }
                     }
