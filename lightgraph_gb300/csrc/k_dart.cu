@@ -77,9 +77,10 @@ __device__ float sample_exact(const DevGrid& g, double px, double py, double pz)
 // subtraction and product); the seven FP32 interpolations add under 2^-19 of
 // the largest tap. For an FP32 record (the polynomial k0 + ...) S = sum of
 // |k| over the non-constant terms stands in for the taps' spread: every
-// partial derivative is at most S and every tap lies within S of k0; its
-// coefficients (rounded once) and their four FP32 steps add under 2^-21 of
-// |k0| + S.
+// partial derivative is at most S and every tap lies within S of k0, so
+// |k0| + S bounds every tap; the coefficients' FP32 differences (54 * 2^-24
+// of the largest tap), their four evaluation steps and the exact sample's own
+// roundings stay under 4e-6 of |k0| + S, and the bound takes twice that.
 __device__ __forceinline__ bool density_passes(const DevGrid& g, const float p[3], const DartParams& prm) {
     const float ix = (p[0] - prm.wo_f[0]) * prm.inv_h_f, iy = (p[1] - prm.wo_f[1]) * prm.inv_h_f,
                 iz = (p[2] - prm.wo_f[2]) * prm.inv_h_f;
@@ -87,8 +88,9 @@ __device__ __forceinline__ bool density_passes(const DevGrid& g, const float p[3
     const float u = ix - fx, w = iy - fy, t = iz - fz;
     float v[8];
     const uint32_t rec = cell_record(g, (int)fx, (int)fy, (int)fz);
-    float val, spread, mag;
+    float val, spread, mag, rel = 2e-6f;
     if (g.dtype == 0) {
+        rel = 8e-6f;
         ld_cell<0>(g.data, rec, v);
         val = trilinear_coefs(v, u, w, t);
         float sum = 0.f;
@@ -111,7 +113,7 @@ __device__ __forceinline__ bool density_passes(const DevGrid& g, const float p[3
     }
     const float e2 = 2.f * prm.index_err;
     const bool near_face = u < e2 || u > 1.f - e2 || w < e2 || w > 1.f - e2 || t < e2 || t > 1.f - e2;
-    const float bound = 3.f * spread * prm.index_err + mag * 2e-6f + 1e-30f;
+    const float bound = 3.f * spread * prm.index_err + mag * rel + 1e-30f;
     if (!near_face) {
         if (val < prm.cutoff - bound) return false;
         if (val > prm.cutoff + bound) return true;
