@@ -240,6 +240,15 @@ extern "C" lg_status lg_create(int device, lg_ctx** out) {
         delete ctx;
         return LG_ERR_CUDA;
     }
+    if (cudaStreamCreateWithFlags(&ctx->st2, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->ev_count, cudaEventDisableTiming) != cudaSuccess) {
+        if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
+        if (ctx->st2) cudaStreamDestroy(ctx->st2);
+        cudaStreamDestroy(ctx->st);
+        delete ctx;
+        return LG_ERR_CUDA;
+    }
     // defaults: Shader() and SceneSettings() of the reference
     lg_shader& s = ctx->shader;
     std::memset(&s, 0, sizeof s);
@@ -281,6 +290,11 @@ extern "C" lg_status lg_destroy(lg_ctx* handle) {
         if (ctx->ev[k]) cudaEventDestroy(ctx->ev[k]);
     for (int k = 0; k <= Ctx::kWaves; ++k)
         if (ctx->wev[k]) cudaEventDestroy(ctx->wev[k]);
+    if (ctx->wev_shade) cudaEventDestroy(ctx->wev_shade);
+    cudaStreamSynchronize(ctx->st2);
+    cudaEventDestroy(ctx->ev_fork);
+    cudaEventDestroy(ctx->ev_count);
+    cudaStreamDestroy(ctx->st2);
     cudaStreamDestroy(ctx->st);
     delete ctx;
     return LG_OK;
@@ -1507,7 +1521,7 @@ extern "C" lg_status lg_get_scatter_grid(lg_ctx* handle, int32_t dims[3], int32_
 // stage 3: render
 // ---------------------------------------------------------------------------
 
-lg_status Ctx::render(const lg_camera* c) {
+lg_status Ctx::render_count(const lg_camera* c, cudaStream_t s) {
     Ctx* ctx = this;
     if (!c) return fail(LG_ERR_INVALID, "null camera");
     if (c->width <= 0 || c->height <= 0 || c->samples < 0) return fail(LG_ERR_INVALID, "bad image size or samples");
@@ -1515,11 +1529,65 @@ lg_status Ctx::render(const lg_camera* c) {
     if (!(c->znear > 0) || !(c->zfar > c->znear)) return fail(LG_ERR_INVALID, "need 0 < znear < zfar");
     if (!D().valid) return fail(LG_ERR_STATE, "no density grid uploaded");
     const int64_t np = (int64_t)c->width * c->height;
+    const int64_t n_ps = np * c->samples;
+    if (n_ps > INT32_MAX) return fail(LG_ERR_INVALID, "too many pixel samples");
     for (DevBuf* b : {&d_rgba, &d_direct, &d_scatter, &d_emission}) CK(b->reserve(sizeof(float4) * np), "film alloc");
     // primary samples, shadow samples, and the claim counters of the shadow
     // wave, the count pass and the shading pass
     CK(d_counters.reserve(5 * sizeof(unsigned long long)), "counter alloc");
-    CK(cudaMemsetAsync(d_counters.p, 0, 5 * sizeof(unsigned long long), st), "counter clear");
+    CK(cudaMemsetAsync(d_counters.p, 0, 5 * sizeof(unsigned long long), s), "counter clear");
+    const int64_t nps1 = std::max<int64_t>(n_ps, 1);
+    CK(d_ps_count.reserve(sizeof(int32_t) * nps1), "render alloc");
+    CK(d_ps_offset.reserve(sizeof(int32_t) * nps1), "render alloc");
+    CK(d_ps_scan.reserve(sizeof(int32_t) * (nps1 / 1024 + 2)), "render alloc");
+    CK(d_ps_total.reserve(sizeof(int32_t) * 2), "render alloc");
+    CK(d_ps_data.reserve(pixel_sample_bytes() * nps1), "render alloc");
+    const DevScene sc = scene();
+    const DevCamera cam = make_camera(*c);
+    int sms = 0;
+    CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device), "device query");
+    wmark(0, s);
+    // (the count pass reads no scatter grid)
+    CK(launch_render_count(sc, cam, DevScatterGrid{}, d_ps_count.as<int32_t>(), d_counters.as<unsigned long long>() + 3,
+                           sms, s),
+       "render count");
+    CK(launch_exclusive_scan(d_ps_count.as<int32_t>(), n_ps, d_ps_offset.as<int32_t>(), d_ps_scan.as<int32_t>(),
+                             d_ps_total.as<int32_t>(), s), "render scan");
+    wmark(1, s);
+    return LG_OK;
+}
+
+lg_status Ctx::render_count_early(const lg_camera* c) {
+    Ctx* ctx = this;
+    CK(cudaEventRecord(ev_fork, st), "fork");
+    CK(cudaStreamWaitEvent(st2, ev_fork, 0), "fork");
+    const lg_status r = render_count(c, st2);
+    CK(cudaEventRecord(ev_count, st2), "join");
+    if (r != LG_OK) {
+        // keep st2 joined to st (a capture must end with it joined)
+        CK(cudaStreamWaitEvent(st, ev_count, 0), "join");
+        return r;
+    }
+    count_early = true;
+    count_cam = *c;
+    return LG_OK;
+}
+
+lg_status Ctx::render(const lg_camera* c) {
+    Ctx* ctx = this;
+    if (!c) return fail(LG_ERR_INVALID, "null camera");
+    const bool early = count_early && std::memcmp(&count_cam, c, sizeof(lg_camera)) == 0;
+    if (count_early) {
+        // the early count ends before anything that follows on st
+        CK(cudaStreamWaitEvent(st, ev_count, 0), "join");
+        count_early = false;
+    }
+    if (!early) {
+        const lg_status r = render_count(c, st);
+        if (r != LG_OK) return r;
+    }
+    waves_recorded = false;
+    wave_split = early;
     DevScatterGrid sg{};
     if (splat_done) {
         sg.v = d_sg.as<float4>();
@@ -1537,30 +1605,16 @@ lg_status Ctx::render(const lg_camera* c) {
     film_h = c->height;
     const DevScene sc = scene();
     const DevCamera cam = make_camera(*c);
-    const int64_t n_ps = np * c->samples;
-    const int64_t nps1 = std::max<int64_t>(n_ps, 1);
-    if (n_ps > INT32_MAX) return fail(LG_ERR_INVALID, "too many pixel samples");
-    CK(d_ps_count.reserve(sizeof(int32_t) * nps1), "render alloc");
-    CK(d_ps_offset.reserve(sizeof(int32_t) * nps1), "render alloc");
-    CK(d_ps_scan.reserve(sizeof(int32_t) * (nps1 / 1024 + 2)), "render alloc");
-    CK(d_ps_total.reserve(sizeof(int32_t) * 2), "render alloc");
-    CK(d_ps_data.reserve(pixel_sample_bytes() * nps1), "render alloc");
-    waves_recorded = false;
-    wmark(0);
-    int sms_c = 0;
-    CK(cudaDeviceGetAttribute(&sms_c, cudaDevAttrMultiProcessorCount, device), "device query");
-    CK(launch_render_count(sc, cam, sg, d_ps_count.as<int32_t>(), d_counters.as<unsigned long long>() + 3, sms_c, st),
-       "render count");
-    CK(launch_exclusive_scan(d_ps_count.as<int32_t>(), n_ps, d_ps_offset.as<int32_t>(), d_ps_scan.as<int32_t>(),
-                             d_ps_total.as<int32_t>(), st), "render scan");
-    wmark(1);
     const int64_t n_lights = std::max(sc.n_lights, 1);
     if (!capturing) {
         // size the shadow-task buffers from this frame's count (a captured
-        // replay reuses the capacity of the run it was captured after)
+        // replay reuses the capacity of the run it was captured after); an
+        // early count is read on its own stream, so the host does not wait
+        // for the graph stages
         int32_t total = 0;
-        CK(cudaMemcpyAsync(&total, d_ps_total.p, sizeof total, cudaMemcpyDeviceToHost, st), "render total");
-        CK(cudaStreamSynchronize(st), "render total sync");
+        cudaStream_t rs = early ? st2 : st;
+        CK(cudaMemcpyAsync(&total, d_ps_total.p, sizeof total, cudaMemcpyDeviceToHost, rs), "render total");
+        CK(cudaStreamSynchronize(rs), "render total sync");
         if (total < 0) return fail(LG_ERR_INVALID, "more than 2^31 shading samples in one frame");
         if ((int64_t)total * n_lights > INT32_MAX)
             return fail(LG_ERR_INVALID, "more than 2^31 shadow-ray groups in one frame");
@@ -1618,6 +1672,7 @@ lg_status Ctx::render(const lg_camera* c) {
     ro.unit_cap = (cap + kRayUnit - 1) / kRayUnit;
     int sms = 0;
     CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device), "device query");
+    if (early && profiling && wev_shade) cudaEventRecord(wev_shade, st);
     CK(launch_render_shade(sc, cam, sg, d_ps_count.as<int32_t>(), d_ps_offset.as<int32_t>(), d_ps_total.as<int32_t>(),
                            d_tasks.as<ShadowTask>(), cap, d_ps_data.p, ro, d_task_direct.as<float4>(),
                            d_rgba.as<float4>(), d_direct.as<float4>(), d_scatter.as<float4>(),
@@ -1679,11 +1734,18 @@ extern "C" lg_status lg_render_frame(lg_ctx* handle, int n_graphs, const float* 
     Ctx* ctx = reinterpret_cast<Ctx*>(handle);
     GUARD(ctx);
     lg_status s = ctx->load_graphs(n_graphs, points, offsets, radius_sq, max_connect);
+    // the render's count pass runs beside the graph stages (side stream)
+    if (s == LG_OK) s = ctx->render_count_early(camera);
     if (s == LG_OK) s = ctx->build_edges();
     if (s == LG_OK) s = ctx->solve_all();
     if (s == LG_OK) s = ctx->splat(point_voxel_size);
     if (s == LG_OK) s = ctx->render(camera);
     if (s == LG_OK) s = ctx->download_films(rgba, direct, scatter, emission);
+    if (s != LG_OK && ctx->count_early) {
+        // a stage failed before render(): join the side stream again
+        cudaStreamWaitEvent(ctx->st, ctx->ev_count, 0);
+        ctx->count_early = false;
+    }
     return s;
 }
 
@@ -1737,7 +1799,9 @@ extern "C" lg_status lg_frame_device(lg_ctx* handle, int max_connect, double poi
 lg_status Ctx::frame_enqueue(double point_voxel_size, const lg_camera* camera) {
     frame_launch_base = g_launch_counter;
     mark(0);
-    lg_status s = build_edges();
+    // the render's count pass runs beside the graph stages (side stream)
+    lg_status s = render_count_early(camera);
+    if (s == LG_OK) s = build_edges();
     mark(1);
     if (s == LG_OK) s = march_edges();
     mark(2);
@@ -1750,6 +1814,11 @@ lg_status Ctx::frame_enqueue(double point_voxel_size, const lg_camera* camera) {
     if (s == LG_OK) s = splat(point_voxel_size);
     mark(6);
     if (s == LG_OK) s = render(camera);
+    if (s != LG_OK && count_early) {
+        // a stage failed before render(): join the side stream again
+        cudaStreamWaitEvent(st, ev_count, 0);
+        count_early = false;
+    }
     mark(7);
     ev_recorded = profiling && s == LG_OK;
     return s;
@@ -1763,7 +1832,10 @@ extern "C" lg_status lg_render_wave_times(lg_ctx* handle, double ms[5]) {
     CK(cudaEventSynchronize(ctx->wev[Ctx::kWaves]), "event sync");
     for (int k = 0; k < Ctx::kWaves; ++k) {
         float t = 0.f;
-        CK(cudaEventElapsedTime(&t, ctx->wev[k], ctx->wev[k + 1]), "event time");
+        // after an early count (on the side stream) the shading wave starts
+        // at its own mark
+        const cudaEvent_t from = k == 1 && ctx->wave_split ? ctx->wev_shade : ctx->wev[k];
+        CK(cudaEventElapsedTime(&t, from, ctx->wev[k + 1]), "event time");
         ms[k] = t;
     }
     return LG_OK;
@@ -1879,6 +1951,7 @@ extern "C" lg_status lg_set_profiling(lg_ctx* handle, int on) {
     if (on && !ctx->ev[0]) {
         for (int k = 0; k <= Ctx::kStages; ++k) CK(cudaEventCreate(&ctx->ev[k]), "event create");
         for (int k = 0; k <= Ctx::kWaves; ++k) CK(cudaEventCreate(&ctx->wev[k]), "event create");
+        CK(cudaEventCreate(&ctx->wev_shade), "event create");
     }
     ctx->profiling = on != 0;
     ctx->graph_valid = false;

@@ -163,9 +163,20 @@ struct Ctx {
     // render waves: count + scan, primary, ray ordering, shadow, resolve
     static constexpr int kWaves = 5;
     cudaEvent_t wev[kWaves + 1] = {};
-    void wmark(int k) {
-        if (profiling && wev[k]) cudaEventRecord(wev[k], st);
+    void wmark(int k, cudaStream_t s) {
+        if (profiling && wev[k]) cudaEventRecord(wev[k], s);
     }
+    // The render's count pass needs only the grids, the scene and the camera,
+    // so a frame runs it (and its scan) on the side stream st2 from the start,
+    // beside the graph stages: st2 waits for ev_fork (recorded on st) and
+    // render() waits for ev_count (recorded on st2). wev_shade then marks
+    // the start of the shading wave on st (wave 1 starts there, not at
+    // wev[1]).
+    cudaStream_t st2 = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_count = nullptr, wev_shade = nullptr;
+    bool count_early = false;  // a count for count_cam was enqueued on st2
+    bool wave_split = false;   // the last profiled render used wev_shade
+    lg_camera count_cam{};
 
     lg_status fail(lg_status s, const char* fmt, ...);
     lg_status cuda(cudaError_t e, const char* what);
@@ -193,6 +204,11 @@ struct Ctx {
     lg_status fw_solve_on(float* base, int choice);
     lg_status solve_rest();
     lg_status splat(double point_voxel_size);
+    // The count pass and scan of a render of camera c on stream s (films and
+    // per-sample buffers sized, counters cleared).
+    lg_status render_count(const lg_camera* c, cudaStream_t s);
+    // render_count on st2, forked from st, for the render() that follows.
+    lg_status render_count_early(const lg_camera* c);
     lg_status render(const lg_camera* c);
     lg_status download_films(float* rgba, float* direct, float* scatter, float* emission);
     lg_status copy_matrix_out(float* out);

@@ -271,6 +271,9 @@ void lg_server::run(Slot* s, Request* q) {
     lg_status st = c.set_lights(q->lights.data(), (int)q->lights.size(), q->env.empty() ? nullptr : q->env.data(),
                                 r.env_w, r.env_h);
     if (st == LG_OK) st = c.load_graphs(r.n_graphs, q->pts.data(), q->offs.data(), q->r2.data(), r.max_connect);
+    // the render's count pass runs beside the graph stages (the slot's side
+    // stream)
+    if (st == LG_OK) st = c.render_count_early(&r.camera);
     // the symmetric persistent solve at 2 CTAs per SM (correct whatever the
     // residency, so the slots' solves may share the SMs; measured 11% more
     // renders/s than 1 CTA per SM on the mixed stream), its queue in
@@ -292,6 +295,11 @@ void lg_server::run(Slot* s, Request* q) {
     }
     if (st == LG_OK) st = c.splat(r.point_voxel_size);
     if (st == LG_OK) st = c.render(&r.camera);
+    if (st != LG_OK && c.count_early) {
+        // a stage failed before render(): join the side stream again
+        cudaStreamWaitEvent(c.st, c.ev_count, 0);
+        c.count_early = false;
+    }
     if (st == LG_OK) {
         const size_t bytes = sizeof(float) * 4 * (size_t)r.camera.width * r.camera.height;
         if (s->pinned_bytes < bytes) {
