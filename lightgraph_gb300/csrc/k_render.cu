@@ -425,11 +425,14 @@ __global__ void __launch_bounds__(128, kWrite ? 5 : 6) k_primary(DevScene sc, De
                                                  int32_t* __restrict__ counts, const int32_t* __restrict__ offsets,
                                                  ShadowTask* __restrict__ tasks, int64_t task_cap,
                                                  PixelSample* __restrict__ out, unsigned long long* __restrict__ ctr,
-                                                 unsigned long long* __restrict__ claim, RayOrder ko) {
+                                                 unsigned long long* __restrict__ claim, RayOrder ko,
+                                                 int max_claims) {
     const int64_t n_ps = (int64_t)cam.width * cam.height * cam.spp;
     const int lane = threadIdx.x & 31;
     uint32_t n_primary = 0;
-    for (;;) {
+    // max_claims > 0: a warp takes at most that many claims (short-lived
+    // CTAs, whose slots free up for kernels of other streams)
+    for (int claims = 0; max_claims <= 0 || claims < max_claims; ++claims) {
         unsigned long long claimed = 0;
         if (lane == 0) claimed = atomicAdd(claim, 32ull);
         claimed = __shfl_sync(0xffffffffu, claimed, 0);
@@ -861,18 +864,22 @@ static int primary_ctas_per_sm(bool write, int dtype) {
 }
 
 cudaError_t launch_render_count(const DevScene& sc, const DevCamera& cam, const DevScatterGrid& sg, int32_t* counts,
-                                unsigned long long* claim, int sms, cudaStream_t st) {
+                                unsigned long long* claim, int sms, cudaStream_t st, bool short_ctas) {
     const int64_t n_ps = (int64_t)cam.width * cam.height * cam.spp;
     if (n_ps == 0) return cudaSuccess;
-    // one resident wave, at most one warp per 32 pixel samples
-    const unsigned blocks = (unsigned)std::min<int64_t>((n_ps + 127) / 128,
-                                                        (int64_t)sms * primary_ctas_per_sm(false, sc.dens.dtype));
+    // one resident wave, at most one warp per 32 pixel samples; or (short
+    // CTAs) one CTA per 128 pixel samples whose warps claim once each
+    const unsigned blocks =
+        short_ctas ? (unsigned)((n_ps + 127) / 128)
+                   : (unsigned)std::min<int64_t>((n_ps + 127) / 128,
+                                                 (int64_t)sms * primary_ctas_per_sm(false, sc.dens.dtype));
+    const int max_claims = short_ctas ? 1 : 0;
     if (sc.dens.dtype == 1)
-        k_primary<false, 1><<<blocks, 128, 0, st>>>(sc, cam, sg, counts, nullptr, nullptr, 0, nullptr, nullptr, claim, RayOrder{});
+        k_primary<false, 1><<<blocks, 128, 0, st>>>(sc, cam, sg, counts, nullptr, nullptr, 0, nullptr, nullptr, claim, RayOrder{}, max_claims);
     else if (sc.dens.dtype == 2)
-        k_primary<false, 2><<<blocks, 128, 0, st>>>(sc, cam, sg, counts, nullptr, nullptr, 0, nullptr, nullptr, claim, RayOrder{});
+        k_primary<false, 2><<<blocks, 128, 0, st>>>(sc, cam, sg, counts, nullptr, nullptr, 0, nullptr, nullptr, claim, RayOrder{}, max_claims);
     else
-        k_primary<false, 0><<<blocks, 128, 0, st>>>(sc, cam, sg, counts, nullptr, nullptr, 0, nullptr, nullptr, claim, RayOrder{});
+        k_primary<false, 0><<<blocks, 128, 0, st>>>(sc, cam, sg, counts, nullptr, nullptr, 0, nullptr, nullptr, claim, RayOrder{}, max_claims);
     ++g_launch_counter;
     return cudaGetLastError();
 }
@@ -924,13 +931,13 @@ cudaError_t launch_render_shade(const DevScene& sc, const DevCamera& cam, const 
         return e;
     if (sc.dens.dtype == 1)
         k_primary<true, 1><<<blocks, 128, 0, st>>>(sc, cam, sg, nullptr, offsets, tasks, task_cap, pss, counters,
-                                                   counters + 4, ro);
+                                                   counters + 4, ro, 0);
     else if (sc.dens.dtype == 2)
         k_primary<true, 2><<<blocks, 128, 0, st>>>(sc, cam, sg, nullptr, offsets, tasks, task_cap, pss, counters,
-                                                   counters + 4, ro);
+                                                   counters + 4, ro, 0);
     else
         k_primary<true, 0><<<blocks, 128, 0, st>>>(sc, cam, sg, nullptr, offsets, tasks, task_cap, pss, counters,
-                                                   counters + 4, ro);
+                                                   counters + 4, ro, 0);
     ++g_launch_counter;
     mark(0);
     // order the shadow rays: scan the key counts, scatter the units

@@ -236,11 +236,15 @@ extern "C" lg_status lg_create(int device, lg_ctx** out) {
     if (cudaSetDevice(device) != cudaSuccess) return LG_ERR_CUDA;
     Ctx* ctx = new Ctx();
     ctx->device = device;
-    if (cudaStreamCreateWithFlags(&ctx->st, cudaStreamNonBlocking) != cudaSuccess) {
+    // the main stream at the highest priority, the side stream (the render's
+    // early count pass) at the lowest: freed SMs go to the main stream first
+    int prio_least = 0, prio_greatest = 0;
+    if (cudaDeviceGetStreamPriorityRange(&prio_least, &prio_greatest) != cudaSuccess) prio_least = prio_greatest = 0;
+    if (cudaStreamCreateWithPriority(&ctx->st, cudaStreamNonBlocking, prio_greatest) != cudaSuccess) {
         delete ctx;
         return LG_ERR_CUDA;
     }
-    if (cudaStreamCreateWithFlags(&ctx->st2, cudaStreamNonBlocking) != cudaSuccess ||
+    if (cudaStreamCreateWithPriority(&ctx->st2, cudaStreamNonBlocking, prio_least) != cudaSuccess ||
         cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&ctx->ev_count, cudaEventDisableTiming) != cudaSuccess) {
         if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
@@ -1547,9 +1551,11 @@ lg_status Ctx::render_count(const lg_camera* c, cudaStream_t s) {
     int sms = 0;
     CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device), "device query");
     wmark(0, s);
-    // (the count pass reads no scatter grid)
+    // (the count pass reads no scatter grid); beside the graph stages (the
+    // side stream, of the lowest priority) as short CTAs, so that the
+    // stages' kernels take the SMs as they free up
     CK(launch_render_count(sc, cam, DevScatterGrid{}, d_ps_count.as<int32_t>(), d_counters.as<unsigned long long>() + 3,
-                           sms, s),
+                           sms, s, s != st),
        "render count");
     CK(launch_exclusive_scan(d_ps_count.as<int32_t>(), n_ps, d_ps_offset.as<int32_t>(), d_ps_scan.as<int32_t>(),
                              d_ps_total.as<int32_t>(), s), "render scan");

@@ -191,7 +191,8 @@ inline int64_t bound_entries(const RayBin& b) {
 // claim: a zeroed counter the persistent grid's warps claim pixel samples
 // from.
 cudaError_t launch_render_count(const DevScene& sc, const DevCamera& cam, const DevScatterGrid& sg, int32_t* counts,
-                                unsigned long long* claim, int sms, cudaStream_t st);
+                                unsigned long long* claim, int sms, cudaStream_t st,
+                                bool short_ctas = false);
 // Shadow-ray ordering buffers: key_counts and key_offsets hold rb's keys,
 // key_scan the scan's block sums (keys / 1024 + 2), order n_lights * units
 // (units of kRayUnit tasks).
