@@ -285,3 +285,28 @@ def test_expm1_approx_vs_library(gpu_ctx):
     ref = r.astype(np.float64)
     rel = np.abs(a.astype(np.float64) - ref) / np.maximum(np.abs(ref), 1e-38)
     assert rel.max() <= 4e-6, (float(rel.max()), float(x[np.argmax(rel)]))
+
+
+def test_frame_after_failed_frame(small_scene):
+    """A frame forks the render's count pass onto a side stream at its start;
+    one that fails there (a zero-width camera) joins it again, and the next
+    frame on the same context is bit-identical to one on a fresh context."""
+    import copy
+    from lightgraph_gb300 import Context, LightGraphError
+    sc = small_scene
+    bad = copy.deepcopy(sc.opts)
+    bad.width = 0
+    a = Context(0)
+    b = Context(0)
+    try:
+        scenes.load_into(a, sc)
+        scenes.load_into(b, sc)
+        with pytest.raises(LightGraphError):
+            a.render_frame(sc.points, sc.radius_sq, bad, sc.max_connect)
+        fa = a.render_frame(sc.points, sc.radius_sq, sc.opts, sc.max_connect)
+        fb = b.render_frame(sc.points, sc.radius_sq, sc.opts, sc.max_connect)
+        for name in ["rgba", "direct", "scatter", "emission"]:
+            assert np.array_equal(getattr(fa, name), getattr(fb, name)), name
+    finally:
+        a.close()
+        b.close()
