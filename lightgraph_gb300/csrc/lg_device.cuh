@@ -418,6 +418,10 @@ struct DevShader {
     int ramp_n;
     float ramp_pos[kMaxRamp];
     float ramp_col[kMaxRamp][3];
+    // 1 / (ramp_out - ramp_in), and per knot i the reciprocal of the interval
+    // to the next knot (the last knot: to the first, ColorRamp's wrap)
+    float ramp_inv_in;
+    float ramp_inv[kMaxRamp];
     float ramp_in, ramp_out;
 };
 
@@ -470,10 +474,13 @@ struct DevScene {
     ShadowMarch smarch;
 };
 
-// ColorRamp::getColor (src/Shader.h:63-92), including its edge behaviour.
+// ColorRamp::getColor (src/Shader.h:63-92), including its edge behaviour;
+// its two divisions as products with reciprocals made on the host (within
+// an ulp of the quotients; a temperature below the first knot still gives
+// the quotient by zero).
 __device__ __forceinline__ void ramp_color(const DevShader& sh, float temp, float out[3]) {
     if (sh.ramp_n == 0) { out[0] = out[1] = out[2] = 0.f; return; }
-    float x = (temp - sh.ramp_in) / (sh.ramp_out - sh.ramp_in);
+    float x = (temp - sh.ramp_in) * sh.ramp_inv_in;
     x = fminf(fmaxf(x, 0.f), 1.f);
     if (sh.ramp_n == 1) {
         out[0] = sh.ramp_col[0][0]; out[1] = sh.ramp_col[0][1]; out[2] = sh.ramp_col[0][2];
@@ -484,8 +491,10 @@ __device__ __forceinline__ void ramp_color(const DevShader& sh, float temp, floa
         if (sh.ramp_pos[i] <= x) prev = i;
         else { next = i; break; }
     }
-    const float range = sh.ramp_pos[next] - sh.ramp_pos[prev];
-    const float blend = (x - sh.ramp_pos[prev]) / range;
+    // next is prev + 1, or 0 when x lies past the last knot (prev = n - 1,
+    // the wrap interval) or before the first (prev = 0, an empty interval)
+    const float inv = next > 0 ? sh.ramp_inv[prev] : prev > 0 ? sh.ramp_inv[prev] : kInf;
+    const float blend = (x - sh.ramp_pos[prev]) * inv;
 #pragma unroll
     for (int c = 0; c < 3; ++c)
         out[c] = sh.ramp_col[prev][c] * (1.f - blend) + sh.ramp_col[next][c] * blend;
