@@ -412,12 +412,9 @@ __global__ void __launch_bounds__(256, 2) k_fw_update(float* __restrict__ d, int
 
 cudaError_t fw_solve(float* d, int n, int ld, cudaStream_t st) {
     if (n <= 0) return cudaSuccess;
-    static bool attr_set = false;
-    if (!attr_set) {
-        cudaError_t e = cudaFuncSetAttribute(k_fw_update, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)kUpdateSmem);
+    {
+        const cudaError_t e = raise_smem_limit(reinterpret_cast<const void*>(k_fw_update));
         if (e != cudaSuccess) return e;
-        attr_set = true;
     }
     const int nt = (n + kKB - 1) / kKB;
     const int nu = (n + kTile - 1) / kTile;
@@ -916,14 +913,9 @@ size_t fw_sync_words(const FwGraph* graphs, int n_graphs) {
 
 cudaError_t fw_solve_batched(float* base, const FwGraph* graphs, const int4* items, int n_items, uint32_t* sync,
                              size_t sync_words, int ctas, cudaStream_t st) {
-    static bool attr_set = false;
-    if (!attr_set) {
-        cudaError_t e = cudaFuncSetAttribute(k_fw_persistent, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)kUpdateSmem);
-        if (e != cudaSuccess) return e;
-        attr_set = true;
-    }
-    cudaError_t e = cudaMemsetAsync(sync, 0, sizeof(uint32_t) * sync_words, st);
+    cudaError_t e = raise_smem_limit(reinterpret_cast<const void*>(k_fw_persistent));
+    if (e != cudaSuccess) return e;
+    e = cudaMemsetAsync(sync, 0, sizeof(uint32_t) * sync_words, st);
     if (e != cudaSuccess) return e;
     if (n_items == 0) return cudaSuccess;
     k_fw_persistent<<<ctas, 256, kUpdateSmem, st>>>(base, graphs, items, n_items, sync);
@@ -933,8 +925,8 @@ cudaError_t fw_solve_batched(float* base, const FwGraph* graphs, const int4* ite
 
 int fw_persistent_ctas_per_sm() {
     int blocks = 0;
-    cudaFuncSetAttribute(k_fw_persistent, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kUpdateSmem);
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, k_fw_persistent, 256, kUpdateSmem) != cudaSuccess)
+    if (raise_smem_limit(reinterpret_cast<const void*>(k_fw_persistent)) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, k_fw_persistent, 256, kUpdateSmem) != cudaSuccess)
         return 1;
     return std::max(blocks, 1);
 }
@@ -1443,17 +1435,10 @@ __global__ void __launch_bounds__(256) k_fw_mirror(float* __restrict__ base, con
 cudaError_t fw_solve_batched_sym(float* base, const FwGraph* graphs, int n_graphs, int max_nt, const int4* items,
                                  int n_items, uint32_t* sync, size_t sync_words, float2* panels, int ctas, bool tma,
                                  cudaStream_t st) {
-    static bool attr_set = false;
-    if (!attr_set) {
-        cudaError_t e = cudaFuncSetAttribute(k_fw_persistent_sym<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)kUpdateSymSmem);
-        if (e == cudaSuccess)
-            e = cudaFuncSetAttribute(k_fw_persistent_sym<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)kUpdateSymSmem);
-        if (e != cudaSuccess) return e;
-        attr_set = true;
-    }
-    cudaError_t e = cudaMemsetAsync(sync, 0, sizeof(uint32_t) * sync_words, st);
+    cudaError_t e = raise_smem_limit(reinterpret_cast<const void*>(k_fw_persistent_sym<false>));
+    if (e == cudaSuccess) e = raise_smem_limit(reinterpret_cast<const void*>(k_fw_persistent_sym<true>));
+    if (e != cudaSuccess) return e;
+    e = cudaMemsetAsync(sync, 0, sizeof(uint32_t) * sync_words, st);
     if (e != cudaSuccess) return e;
     if (n_items == 0) return cudaSuccess;
     if (tma)
@@ -1471,10 +1456,9 @@ cudaError_t fw_solve_batched_sym(float* base, const FwGraph* graphs, int n_graph
 int fw_persistent_sym_ctas_per_sm() {
     int blocks = 0;
     int blocks_tma = 0;
-    cudaFuncSetAttribute(k_fw_persistent_sym<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)kUpdateSymSmem);
-    cudaFuncSetAttribute(k_fw_persistent_sym<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kUpdateSymSmem);
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, k_fw_persistent_sym<false>, 256, kUpdateSymSmem) !=
+    if (raise_smem_limit(reinterpret_cast<const void*>(k_fw_persistent_sym<false>)) != cudaSuccess ||
+        raise_smem_limit(reinterpret_cast<const void*>(k_fw_persistent_sym<true>)) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, k_fw_persistent_sym<false>, 256, kUpdateSymSmem) !=
             cudaSuccess ||
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_tma, k_fw_persistent_sym<true>, 256, kUpdateSymSmem) !=
             cudaSuccess)

@@ -255,12 +255,13 @@ cudaError_t launch_leaf_bits(const float* dense, const int dims[3], const int or
                              const uint8_t* leaf_mask, const DevGrid& g, uint32_t* bits, int* bbox,
                              cudaStream_t st);
 
-extern uint64_t g_launch_counter;
-// Raises a kernel's dynamic shared-memory limit, once per process, to all the
-// device allows next to the kernel's static shared memory. The limit is one
-// setting per kernel shared by every host thread, so a launcher that set it to
-// its own launch's size could lower it under another thread's larger launch
-// (the server's slots launch concurrently); it is set once, to the maximum.
-cudaError_t raise_smem_limit(const void* func);  // kernel launches issued (all contexts)
+extern uint64_t g_launch_counter;  // kernel launches issued (all contexts)
+// Raises a kernel's dynamic shared-memory limit on the current device, once
+// per (device, kernel), to all the device allows next to the kernel's static
+// shared memory. The limit is one setting per kernel and device shared by
+// every host thread, so a launcher that set it to its own launch's size could
+// lower it under another thread's larger launch (the server's slots launch
+// concurrently); it is set once, to the maximum.
+cudaError_t raise_smem_limit(const void* func);
 
 }  // namespace lg
