@@ -512,7 +512,10 @@ lg_status lg_server_add_volume(lg_server* srv, const lg_grid_desc* density,
                                const float* temperature_values,
                                int storage_dtype, int32_t* volume_id);
 /* Enqueues a request and returns at once; *ticket identifies it.
- * LG_ERR_BUSY: queue full; LG_ERR_NOMEM: larger than the whole budget. */
+ * LG_ERR_INVALID: a malformed request (the graph layout lg_build_graphs
+ * accepts, known volume, lights and env map), checked before anything is
+ * copied; LG_ERR_BUSY: queue full; LG_ERR_NOMEM: larger than the whole
+ * budget. */
 lg_status lg_server_submit(lg_server* srv, const lg_request* req, int64_t* ticket);
 /* Non-blocking: *done = 1 once the request has finished (its result waits
  * for lg_server_wait, which this call does not consume), else 0.

@@ -443,14 +443,26 @@ extern "C" lg_status lg_server_add_volume(lg_server* srv, const lg_grid_desc* de
 
 extern "C" lg_status lg_server_submit(lg_server* srv, const lg_request* req, int64_t* ticket) {
     if (!srv || !req) return LG_ERR_INVALID;
-    if (req->n_graphs < 1 || !req->offsets || !req->radius_sq || req->n_lights < 0 ||
+    if (req->n_graphs < 1 || req->n_graphs > 65535 || !req->offsets || !req->radius_sq || req->n_lights < 0 ||
         req->n_lights > LG_MAX_LIGHTS || (req->n_lights > 0 && !req->lights))
         return LG_ERR_INVALID;
+    // the point layout is checked here, before the request's arrays are
+    // copied (the same rules as lg_build_graphs)
+    auto refuse = [&](const char* why) {
+        std::lock_guard<std::mutex> lk(srv->mu);
+        srv->err = why;
+        return LG_ERR_INVALID;
+    };
+    if (req->offsets[0] != 0) return refuse("offsets[0] must be 0");
+    if (req->max_connect < 0 || req->max_connect > 255) return refuse("max_connect must be in [0, 255]");
+    for (int g = 0; g < req->n_graphs; ++g) {
+        const int64_t n = req->offsets[g + 1] - req->offsets[g];
+        if (n < 0 || n > 65535) return refuse("every graph needs 0..65535 points");
+    }
+    if (req->offsets[req->n_graphs] > 0 && !req->points) return refuse("null points");
     for (int k = 0; k < req->n_lights; ++k)
-        if (req->lights[k].type == LG_LIGHT_ENV && (!req->env_rgb || req->env_w < 2 || req->env_h < 2)) {
-            srv->err = "an environment light needs the request's env map (at least 2 x 2)";
-            return LG_ERR_INVALID;
-        }
+        if (req->lights[k].type == LG_LIGHT_ENV && (!req->env_rgb || req->env_w < 2 || req->env_h < 2))
+            return refuse("an environment light needs the request's env map (at least 2 x 2)");
     auto q = std::make_unique<Request>();
     q->r = *req;
     const int64_t P = req->offsets[req->n_graphs];
