@@ -70,15 +70,21 @@ __global__ void __launch_bounds__(256) k_candidates(const float* __restrict__ pt
 // of 64 rows, double buffered: warp 0 resolves the rows of one chunk in order
 // while warps 1-7 stage the next.
 constexpr int kGreedyChunk = 64;
+static_assert((kCandCap * sizeof(uint16_t)) % sizeof(uint4) == 0, "candidate rows are copied as 16-byte words");
 
+// A chunk's candidate rows are one contiguous block of rows * kCandCap
+// entries whose start, (pt_off + r0) * 192 bytes into the array, is 16-byte
+// aligned: it is copied as 16-byte words, every load independent of the
+// others (entries past a row's count are copied too and never read).
 __device__ __forceinline__ void greedy_stage(const GraphInfo& g, const uint16_t* __restrict__ cand,
                                              const int32_t* __restrict__ cand_cnt, int r0, int rows, uint16_t* cs,
                                              int32_t* cc, int t, int nt) {
-    for (int k = t; k < rows * kCandCap; k += nt) {
-        const int r = k / kCandCap, c = k - r * kCandCap;
-        const int total = cand_cnt[g.pt_off + r0 + r];
-        if (c < min(total, kCandCap)) cs[k] = cand[(g.pt_off + r0 + r) * kCandCap + c];
-    }
+    constexpr int kWordsPerRow = kCandCap * (int)sizeof(uint16_t) / (int)sizeof(uint4);
+    const uint4* __restrict__ src = reinterpret_cast<const uint4*>(cand + (g.pt_off + r0) * kCandCap);
+    uint4* dst = reinterpret_cast<uint4*>(cs);
+    const int words = rows * kWordsPerRow;
+#pragma unroll 4
+    for (int k = t; k < words; k += nt) dst[k] = __ldg(src + k);
     for (int k = t; k < rows; k += nt) cc[k] = cand_cnt[g.pt_off + r0 + k];
 }
 
@@ -88,7 +94,7 @@ __global__ void __launch_bounds__(256) k_greedy(const float* __restrict__ pts,
                                                 const int32_t* __restrict__ cand_cnt,
                                                 int max_connect, int2* __restrict__ edges,
                                                 int32_t* __restrict__ edge_cnt) {
-    extern __shared__ uint8_t smem[];
+    extern __shared__ __align__(16) uint8_t smem[];
     const GraphInfo g = graphs[blockIdx.x];
     const int n = g.n;
     uint16_t* cs2 = reinterpret_cast<uint16_t*>(smem);                       // 2 x chunk x cap
@@ -114,14 +120,17 @@ __global__ void __launch_bounds__(256) k_greedy(const float* __restrict__ pts,
         } else {
             for (int r = 0; r < rows; ++r) {
                 const int i = r0 + r;
+                // the row's candidate count and first 32 candidates do not
+                // depend on the edge counts: loaded beside cnt[i]
+                const int total = cc[r];
+                const int jfirst = cs[r * kCandCap + lane];
                 int need = max_connect - (int)cnt[i];
                 if (need <= 0) continue;
-                const int total = cc[r];
                 const int stored = min(total, kCandCap);
                 for (int b = 0; b < stored && need > 0; b += 32) {
                     const int c = b + lane;
                     int j = -1;
-                    if (c < stored) j = cs[r * kCandCap + c];
+                    if (c < stored) j = b == 0 ? jfirst : cs[r * kCandCap + c];
                     const bool elig = j >= 0 && (int)cnt[j] < max_connect;
                     const unsigned m = __ballot_sync(0xffffffffu, elig);
                     const int rank = __popc(m & ((1u << lane) - 1u));
@@ -157,8 +166,8 @@ __global__ void __launch_bounds__(256) k_greedy(const float* __restrict__ pts,
                         __syncwarp();
                     }
                 }
-                if (lane == 0) cnt[i] = (uint8_t)(max_connect - need);
-                __syncwarp();
+                // cnt[i] is not written back: later rows read only the
+                // counts of partners j > their own row, never row i's
             }
         }
     }

@@ -71,7 +71,7 @@ def small_oracle(small_scene):
     return po.Oracle(sc.density, sc.shader, sc.opts, sc.lights)
 
 
-@pytest.mark.parametrize("max_connect", [0, 1, 3, 12])
+@pytest.mark.parametrize("max_connect", [0, 1, 3, 12, 16, 17])
 @pytest.mark.parametrize("radius", [0.05, 0.15, 0.4])
 def test_adjacency_bitexact(gpu_ctx, small_scene, max_connect, radius):
     sc = small_scene
