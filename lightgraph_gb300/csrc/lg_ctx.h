@@ -14,7 +14,7 @@ namespace lg {
 
 // Bumped whenever any DevBuf is reallocated: a captured frame graph is only
 // replayed while its buffers are the ones it was captured with.
-extern uint64_t g_alloc_epoch;
+extern std::atomic<uint64_t> g_alloc_epoch;
 
 // Grow-only device allocation.
 struct DevBuf {

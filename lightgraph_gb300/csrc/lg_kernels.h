@@ -4,6 +4,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <atomic>
+
 #include "lg_device.cuh"
 
 namespace lg {
@@ -255,7 +257,7 @@ cudaError_t launch_leaf_bits(const float* dense, const int dims[3], const int or
                              const uint8_t* leaf_mask, const DevGrid& g, uint32_t* bits, int* bbox,
                              cudaStream_t st);
 
-extern uint64_t g_launch_counter;  // kernel launches issued (all contexts)
+extern std::atomic<uint64_t> g_launch_counter;  // kernel launches issued (all contexts, all host threads)
 // Raises a kernel's dynamic shared-memory limit on the current device, once
 // per (device, kernel), to all the device allows next to the kernel's static
 // shared memory. The limit is one setting per kernel and device shared by

@@ -349,20 +349,27 @@ extern "C" lg_status lg_server_create(const lg_server_opts* opts, lg_server** ou
     for (int k = 0; k <= opts->max_inflight + 1; ++k) {
         lg_ctx* h = nullptr;
         const lg_status st = lg_create(opts->device, &h);
-        if (st != LG_OK) return st;
+        if (st != LG_OK) {
+            // what was made so far goes the way lg_server_destroy takes it
+            // (no worker thread has started yet)
+            lg_server_destroy(srv.release());
+            return st;
+        }
         std::unique_ptr<Ctx> c(reinterpret_cast<Ctx*>(h));
         if (k == 0) {
             srv->upload_ctx = std::move(c);
         } else if (k == 1) {
             srv->paths.ctx = std::move(c);
         } else {
-            auto s = std::make_unique<Slot>();
-            s->ctx = std::move(c);
+            srv->slots.push_back(std::make_unique<Slot>());
+            Slot& s = *srv->slots.back();
+            s.ctx = std::move(c);
             cudaSetDevice(opts->device);
-            if (cudaEventCreateWithFlags(&s->marched, cudaEventDisableTiming) != cudaSuccess ||
-                cudaEventCreateWithFlags(&s->solved, cudaEventDisableTiming) != cudaSuccess)
+            if (cudaEventCreateWithFlags(&s.marched, cudaEventDisableTiming) != cudaSuccess ||
+                cudaEventCreateWithFlags(&s.solved, cudaEventDisableTiming) != cudaSuccess) {
+                lg_server_destroy(srv.release());
                 return LG_ERR_CUDA;
-            srv->slots.push_back(std::move(s));
+            }
         }
     }
     lg_server* p = srv.release();
@@ -389,8 +396,8 @@ extern "C" lg_status lg_server_destroy(lg_server* srv) {
         // the slot contexts are destroyed through the C ABI (stream, events)
         lg_destroy(reinterpret_cast<lg_ctx*>(s->ctx.release()));
     }
-    lg_destroy(reinterpret_cast<lg_ctx*>(srv->paths.ctx.release()));
-    lg_destroy(reinterpret_cast<lg_ctx*>(srv->upload_ctx.release()));
+    if (srv->paths.ctx) lg_destroy(reinterpret_cast<lg_ctx*>(srv->paths.ctx.release()));
+    if (srv->upload_ctx) lg_destroy(reinterpret_cast<lg_ctx*>(srv->upload_ctx.release()));
     delete srv;
     return LG_OK;
 }
