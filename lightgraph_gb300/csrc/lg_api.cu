@@ -1703,16 +1703,8 @@ lg_status Ctx::download_films(float* rgba, float* direct, float* scatter, float*
     const int64_t np = (int64_t)film_w * film_h;
     const void* src[4] = {d_rgba.p, d_direct.p, d_scatter.p, d_emission.p};
     float* dst[4] = {rgba, direct, scatter, emission};
-    // two films on each of the two streams, so that two copy engines share
-    // the transfer; the side stream starts after everything on st so far
-    // (the fork event is free again once a frame has rendered)
-    CK(cudaEventRecord(ev_fork, st), "film download fork");
-    CK(cudaStreamWaitEvent(st2, ev_fork, 0), "film download fork");
     for (int k = 0; k < 4; ++k)
-        if (dst[k])
-            CK(cudaMemcpyAsync(dst[k], src[k], sizeof(float4) * np, cudaMemcpyDeviceToHost, (k & 1) ? st2 : st),
-               "film download");
-    CK(cudaStreamSynchronize(st2), "sync");
+        if (dst[k]) CK(cudaMemcpyAsync(dst[k], src[k], sizeof(float4) * np, cudaMemcpyDeviceToHost, st), "film download");
     CK(cudaStreamSynchronize(st), "sync");
     return LG_OK;
 }
