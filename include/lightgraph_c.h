@@ -382,8 +382,11 @@ lg_status lg_fw_schedule(lg_ctx* ctx, int* schedule, double* tuned_ms, int n);
  * (one add and one min per update, as the roofline counts them) of their
  * inner loop alone, with its operands held in shared memory (no staging, no
  * dependency waits, no stores), 2 CTAs per SM. Enqueued on the context's
- * stream and waited for. */
-lg_status lg_fw_inner_loop_rate(lg_ctx* ctx, double* tflops);
+ * stream and waited for. sums (optional, 256 floats) receives each thread's
+ * sum of its final 8 x 8 tile in the first CTA (every CTA computes the same
+ * values), so that the loop's arithmetic (packed adds, 3-input mins over
+ * fixed operand patterns) can be checked. */
+lg_status lg_fw_inner_loop_rate(lg_ctx* ctx, double* tflops, float* sums);
 /* Accuracy check of the primary wave's e^x - 1 (a Taylor series below
  * |x| = 1/16, __expf(x) - 1 above): approx[i] is its value at x[i] and ref[i]
  * the CUDA library's expm1f there, both computed on the device (host

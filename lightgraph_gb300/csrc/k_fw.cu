@@ -1481,9 +1481,12 @@ __global__ void __launch_bounds__(256, 2) k_fw_inner_loop(float* __restrict__ ou
     float2* As = reinterpret_cast<float2*>(fw_smem);
     float2* Bs = As + 32 * kTile;
     const int tid = threadIdx.x;
+    // operand patterns whose minima differ from element to element (small
+    // integers and halves: every sum and the tile sums are exact in FP32),
+    // so that the results check the arithmetic
     for (int e = tid; e < 32 * kTile; e += 256) {
-        As[e] = make_float2(1.f + (e % 7), 2.f + (e % 5));
-        Bs[e] = make_float2(1.5f + (e % 3), 0.5f + (e % 11));
+        As[e] = make_float2((float)((e * 37) % 101), (float)((e * 53) % 97) + 0.25f);
+        Bs[e] = make_float2((float)((e * 29) % 89) + 0.5f, (float)((e * 61) % 83));
     }
     __syncthreads();
     const int warp = tid >> 5, lane = tid & 31;

@@ -1894,7 +1894,7 @@ extern "C" lg_status lg_fw_schedule(lg_ctx* handle, int* schedule, double* tuned
     return LG_OK;
 }
 
-extern "C" lg_status lg_fw_inner_loop_rate(lg_ctx* handle, double* tflops) {
+extern "C" lg_status lg_fw_inner_loop_rate(lg_ctx* handle, double* tflops, float* sums) {
     Ctx* ctx = reinterpret_cast<Ctx*>(handle);
     GUARD(ctx);
     if (!tflops) return ctx->fail(LG_ERR_INVALID, "tflops is null");
@@ -1903,6 +1903,7 @@ extern "C" lg_status lg_fw_inner_loop_rate(lg_ctx* handle, double* tflops) {
     DevBuf scratch;
     CK(scratch.reserve(sizeof(float) * 2 * sms * 256), "scratch alloc");
     CK(fw_inner_loop_rate(scratch.as<float>(), sms, tflops, ctx->st), "inner loop rate");
+    if (sums) CK(cudaMemcpy(sums, scratch.p, sizeof(float) * 256, cudaMemcpyDeviceToHost), "inner loop sums");
     return LG_OK;
 }
 

@@ -423,12 +423,18 @@ class Context:
         operands staged by TMA bulk copies."""
         self._ck(self.lib.lg_set_fw_schedule(self.h, schedule))
 
-    def fw_inner_loop_rate(self) -> float:
+    def fw_inner_loop_rate(self, want_sums: bool = False):
         """FP32 TFLOP/s (add + min per update) of the Floyd-Warshall update
-        tiles' inner loop alone: the min-plus ceiling on this GPU."""
+        tiles' inner loop alone: the min-plus ceiling on this GPU. With
+        want_sums, also each thread's sum of its final tile in the first CTA
+        (256 floats), for checking the loop's arithmetic."""
         v = C.c_double()
-        self._ck(self.lib.lg_fw_inner_loop_rate(self.h, C.byref(v)))
-        return v.value
+        if not want_sums:
+            self._ck(self.lib.lg_fw_inner_loop_rate(self.h, C.byref(v), None))
+            return v.value
+        sums = np.empty(256, np.float32)
+        self._ck(self.lib.lg_fw_inner_loop_rate(self.h, C.byref(v), sums.ctypes.data))
+        return v.value, sums
 
     def fw_schedule(self):
         s = C.c_int()

@@ -113,11 +113,40 @@ def test_graph_replay_matches_direct_launches(gpu_ctx):
     gpu_ctx.set_graph_mode(False)
 
 
+def inner_loop_sums_f32() -> np.ndarray:
+    """The inner-loop probe's per-thread results, restated in FP32 numpy: the
+    update tiles' 8 x 8 register tile per thread (rows rbase + 8q + {0, 1},
+    columns cbase + 16q + {0, 1}), 32 k-pairs over the probe's fixed operand
+    patterns, acc = min(acc, a.x + b.x, a.y + b.y), then the 64 values summed
+    row by row. Every operand and sum is a small exact FP32 value."""
+    e = np.arange(32 * 128)
+    A = np.stack([(e * 37) % 101, (e * 53) % 97 + 0.25], -1).astype(np.float32).reshape(32, 128, 2)
+    B = np.stack([(e * 29) % 89 + 0.5, (e * 61) % 83], -1).astype(np.float32).reshape(32, 128, 2)
+    out = np.empty(256, np.float32)
+    for tid in range(256):
+        warp, lane = tid >> 5, tid & 31
+        rbase = (warp >> 1) * 32 + (lane >> 3) * 2
+        cbase = (warp & 1) * 64 + (lane & 7) * 2
+        rows = np.array([rbase + 8 * (r >> 1) + (r & 1) for r in range(8)])
+        cols = np.array([cbase + 16 * (c >> 1) + (c & 1) for c in range(8)])
+        a, b = A[:, rows, :], B[:, cols, :]                      # [kp][8][2]
+        s = a[:, :, None, :] + b[:, None, :, :]                  # [kp][r][c][2], FP32
+        acc = np.minimum(np.float32(1e30), s.min(axis=(0, 3)))   # the init rounds to 1e30f
+        tot = np.float32(0.0)
+        for v in acc.reshape(-1):
+            tot = np.float32(tot + v)
+        out[tid] = tot
+    return out
+
+
 def test_fw_inner_loop_ceiling(gpu_ctx):
-    """The min-plus inner loop alone runs near half of the FMA-counted FP32
-    peak (an add and a min per update, each an FP32 lane cycle): between 20
-    and 70 TFLOP/s on a GB300 (152 SMs, ~1.9-2.07 GHz)."""
-    t = gpu_ctx.fw_inner_loop_rate()
+    """The min-plus inner loop alone: its results equal an FP32 restatement of
+    the same packed adds and 3-input mins bit for bit, and it runs near half
+    of the FMA-counted FP32 peak (an add and a min per update, each an FP32
+    lane cycle): between 20 and 70 TFLOP/s on a GB300 (152 SMs, ~1.9-2.07
+    GHz)."""
+    t, sums = gpu_ctx.fw_inner_loop_rate(want_sums=True)
+    assert np.array_equal(sums, inner_loop_sums_f32())
     assert 20.0 < t < 70.0, t
 
 
