@@ -401,6 +401,15 @@ lg_status lg_expm1_check(lg_ctx* ctx, const float* x, float* approx, float* ref,
  * and every block is written exactly once per round; LG_ERR_STATE otherwise.
  * *n_items (optional) receives the queue length. */
 lg_status lg_fw_queue_check(int n_graphs, const int32_t* sizes, int sym, int64_t* n_items);
+/* Device-side check of the bounded dependency wait the persistent solves use
+ * (no counterpart in the reference): one thread waits for a flag that
+ * nothing sets, for at most `polls` polls (1 to 2^24), and then raises the
+ * error word as a stalled solve does. Returns LG_ERR_TIMEOUT when the wait
+ * gave up as designed (the context stays usable), LG_ERR_STATE if it did not.
+ * The calls that hand results back (lg_solve_paths, lg_solve_graphs,
+ * lg_diffuse, lg_render_frame, ...) return LG_ERR_TIMEOUT the same way when
+ * a persistent solve of theirs raised its error word. */
+lg_status lg_wait_timeout_check(lg_ctx* ctx, uint32_t polls);
 
 /* ------------------------------------------------------------------------- */
 /* Image files without the OpenEXR library                                   */

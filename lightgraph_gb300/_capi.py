@@ -140,6 +140,7 @@ SIGNATURES = {
     "lg_set_fw_schedule": (I32, [P, C.c_int]),
     "lg_fw_schedule": (I32, [P, C.POINTER(C.c_int), C.POINTER(D), C.c_int]),
     "lg_fw_queue_check": (I32, [C.c_int, P, C.c_int, C.POINTER(I64)]),
+    "lg_wait_timeout_check": (I32, [P, C.c_uint32]),
     "lg_fw_inner_loop_rate": (I32, [P, C.POINTER(D), P]),
     "lg_expm1_check": (I32, [P, P, P, P, I32]),
     "lg_fw_device": (I32, [P, C.c_int, C.c_int, P]),

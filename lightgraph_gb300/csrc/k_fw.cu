@@ -466,17 +466,39 @@ __device__ __forceinline__ uint32_t ld_acquire(const uint32_t* p) {
     return v;
 }
 
-// Bounded wait for *v >= target; false (and err set) when it gives up.
-__device__ __forceinline__ bool wait_version(const uint32_t* v, uint32_t target, uint32_t* err) {
+// Bounded wait for *v >= target, at most `limit` polls; false (and err set)
+// when it gives up.
+__device__ __forceinline__ bool wait_version_limit(const uint32_t* v, uint32_t target, uint32_t* err,
+                                                   uint32_t limit) {
     uint32_t spins = 0;
     while (ld_acquire(v) < target) {
-        if (++spins > kSpinLimit || ld_acquire(err) != 0) {
+        if (++spins > limit || ld_acquire(err) != 0) {
             atomicExch(err, 1u);
             return false;
         }
         __nanosleep(100);
     }
     return true;
+}
+
+__device__ __forceinline__ bool wait_version(const uint32_t* v, uint32_t target, uint32_t* err) {
+    return wait_version_limit(v, target, err, kSpinLimit);
+}
+
+// The persistent solves' bounded wait on its own: one thread waits for
+// words[0] >= 1, which nothing sets, for at most `limit` polls and then
+// raises words[1] as the solves raise their error word; words[2] = 1 when
+// the wait gave up, 2 when it returned.
+__global__ void k_wait_probe(uint32_t* words, uint32_t limit) {
+    if (threadIdx.x != 0) return;
+    const bool ok = wait_version_limit(words, 1u, words + 1, limit);
+    words[2] = ok ? 2u : 1u;
+}
+
+cudaError_t wait_probe(uint32_t* words, uint32_t limit, cudaStream_t st) {
+    k_wait_probe<<<1, 32, 0, st>>>(words, limit);
+    ++g_launch_counter;
+    return cudaGetLastError();
 }
 
 __global__ void __launch_bounds__(256, 2) k_fw_persistent(float* __restrict__ base, const FwGraph* __restrict__ gs,

@@ -884,6 +884,21 @@ lg_status Ctx::copy_matrix_out(float* out) {
         o += (int64_t)g.n * g.n;
     }
     CK(cudaStreamSynchronize(st), "sync");
+    return fw_wait_status();
+}
+
+// The error word of this context's last persistent Floyd-Warshall launch,
+// which a bounded dependency wait raises when it gives up (the launch then
+// ends early and its matrices are incomplete): LG_ERR_TIMEOUT if raised. Read
+// where a call has synchronised the stream to hand results back.
+lg_status Ctx::fw_wait_status() {
+    Ctx* ctx = this;
+    if (!fw_flag_pending || d_fw_sync.bytes < 2 * sizeof(uint32_t)) return LG_OK;
+    fw_flag_pending = false;
+    uint32_t flags[2] = {0, 0};
+    CK(cudaMemcpyAsync(flags, d_fw_sync.p, sizeof flags, cudaMemcpyDeviceToHost, st), "fw flag read");
+    CK(cudaStreamSynchronize(st), "sync");
+    if (flags[1] != 0) return fail(LG_ERR_TIMEOUT, "batched floyd-warshall: a dependency wait timed out");
     return LG_OK;
 }
 
@@ -914,6 +929,7 @@ static lg_status run_fw_schedule(Ctx* ctx, float* base, int choice) {
     }
     int sms = 0;
     CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device), "device query");
+    ctx->fw_flag_pending = true;
     if (choice >= 3) {
         CK(fw_solve_batched_sym(base, ctx->d_fwg.as<FwGraph>(), ctx->n_graphs, ctx->fw_max_nt,
                                 ctx->d_fw_items_sym.as<int4>(), ctx->fw_items_sym_n, ctx->d_fw_sync.as<uint32_t>(),
@@ -1181,6 +1197,7 @@ extern "C" lg_status lg_diffuse(lg_ctx* handle, float* diffuse_out) {
         CK(cudaMemcpyAsync(diffuse_out, ctx->d_D.p, sizeof(float) * 3 * ctx->n_points, cudaMemcpyDeviceToHost,
                            ctx->st), "D download");
         CK(cudaStreamSynchronize(ctx->st), "sync");
+        return ctx->fw_wait_status();
     }
     return LG_OK;
 }
@@ -1211,7 +1228,7 @@ extern "C" lg_status lg_solve_graphs(lg_ctx* handle, float* diffuse_out) {
                            ctx->st), "D download");
     }
     CK(cudaStreamSynchronize(ctx->st), "sync");
-    return LG_OK;
+    return ctx->fw_wait_status();
 }
 
 extern "C" lg_status lg_get_vertex_data(lg_ctx* handle, float* light_out, float* diffuse_out) {
@@ -1228,7 +1245,7 @@ extern "C" lg_status lg_get_vertex_data(lg_ctx* handle, float* light_out, float*
                            ctx->st), "D download");
     }
     CK(cudaStreamSynchronize(ctx->st), "sync");
-    return LG_OK;
+    return ctx->fw_wait_status();
 }
 
 // ---------------------------------------------------------------------------
@@ -1706,7 +1723,7 @@ lg_status Ctx::download_films(float* rgba, float* direct, float* scatter, float*
     for (int k = 0; k < 4; ++k)
         if (dst[k]) CK(cudaMemcpyAsync(dst[k], src[k], sizeof(float4) * np, cudaMemcpyDeviceToHost, st), "film download");
     CK(cudaStreamSynchronize(st), "sync");
-    return LG_OK;
+    return fw_wait_status();
 }
 
 extern "C" lg_status lg_render(lg_ctx* handle, const lg_camera* camera, float* rgba, float* direct,
@@ -1921,6 +1938,20 @@ extern "C" lg_status lg_expm1_check(lg_ctx* handle, const float* x, float* appro
     CK(cudaMemcpyAsync(ref, dx + 2 * (size_t)n, sizeof(float) * n, cudaMemcpyDeviceToHost, ctx->st), "expm1 check read");
     CK(cudaStreamSynchronize(ctx->st), "sync");
     return LG_OK;
+}
+
+extern "C" lg_status lg_wait_timeout_check(lg_ctx* handle, uint32_t polls) {
+    Ctx* ctx = reinterpret_cast<Ctx*>(handle);
+    GUARD(ctx);
+    if (polls < 1 || polls > (1u << 24)) return ctx->fail(LG_ERR_INVALID, "polls must be in [1, 2^24]");
+    CK(ctx->small.reserve(64), "small alloc");
+    CK(cudaMemsetAsync(ctx->small.p, 0, 4 * sizeof(uint32_t), ctx->st), "probe clear");
+    CK(wait_probe(ctx->small.as<uint32_t>(), polls, ctx->st), "wait probe");
+    uint32_t w[4] = {0, 0, 0, 0};
+    CK(cudaMemcpyAsync(w, ctx->small.p, sizeof w, cudaMemcpyDeviceToHost, ctx->st), "probe read");
+    CK(cudaStreamSynchronize(ctx->st), "sync");
+    if (w[2] == 1u && w[1] != 0u) return ctx->fail(LG_ERR_TIMEOUT, "the bounded wait gave up after %u polls", polls);
+    return ctx->fail(LG_ERR_STATE, "the bounded wait did not give up (error word %u, outcome %u)", w[1], w[2]);
 }
 
 extern "C" lg_status lg_fw_queue_check(int n_graphs, const int32_t* sizes, int sym, int64_t* n_items) {

@@ -106,6 +106,8 @@ struct Ctx {
     int fw_max_nt = 0;
     size_t fw_sync_n = 2;  // uint32 words of d_fw_sync
     bool fw_queue_valid = false;
+    // a persistent solve ran since the last look at its error word (d_fw_sync)
+    bool fw_flag_pending = false;
     std::vector<int64_t> fw_queue_key;  // (graph count, then offset and padded size per graph)
     bool fw_general_built = false;      // d_fw_items holds the general queue
     bool fw_sym_built = false;          // d_fw_items_sym holds the symmetric queue
@@ -212,6 +214,7 @@ struct Ctx {
     lg_status render(const lg_camera* c);
     lg_status download_films(float* rgba, float* direct, float* scatter, float* emission);
     lg_status copy_matrix_out(float* out);
+    lg_status fw_wait_status();
 };
 
 }  // namespace lg

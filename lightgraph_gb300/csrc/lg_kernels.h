@@ -86,6 +86,10 @@ int fw_persistent_ctas_per_sm();
 // FP32 ops/s (an add and a min per update) of the update tiles' inner loop
 // alone on shared-memory operands, 2 CTAs per SM. scratch: 2 * sms * 256 floats.
 cudaError_t fw_inner_loop_rate(float* scratch, int sms, double* tflops, cudaStream_t st);
+// The persistent solves' bounded dependency wait run alone on a flag that
+// nothing sets (words: 4 zeroed words; words[1] = error word, words[2] = 1
+// when the wait gave up).
+cudaError_t wait_probe(uint32_t* words, uint32_t limit, cudaStream_t st);
 int fw_persistent_sym_ctas_per_sm();
 cudaError_t launch_set_diag(float* S, const GraphInfo* graphs, int n_graphs, int max_n,
                             cudaStream_t st);
