@@ -1048,9 +1048,17 @@ lg_status Ctx::tune_fw() {
     cands.push_back(fw_persistent_sym_ctas_per_sm() >= 2 ? 4 : 3);
     if (cands.back() == 4) cands.push_back(5);
     CK(d_fw_tune.reserve(sizeof(float) * std::max<int64_t>(s_floats, 1)), "fw tune alloc");
-    cudaEvent_t e0, e1;
-    CK(cudaEventCreate(&e0), "event");
-    CK(cudaEventCreate(&e1), "event");
+    // the trial events, destroyed on every way out
+    struct Events {
+        cudaEvent_t a = nullptr, b = nullptr;
+        ~Events() {
+            if (a) cudaEventDestroy(a);
+            if (b) cudaEventDestroy(b);
+        }
+    } ev;
+    CK(cudaEventCreate(&ev.a), "event");
+    CK(cudaEventCreate(&ev.b), "event");
+    const cudaEvent_t e0 = ev.a, e1 = ev.b;
     int best = 0;
     float best_ms = 1e30f;
     for (double& t : fw_tune_ms) t = 0.0;
@@ -1085,8 +1093,6 @@ lg_status Ctx::tune_fw() {
         if (fw_tune_ms[cand] == 0.0 || ms < fw_tune_ms[cand]) fw_tune_ms[cand] = ms;
         if (ms < best_ms) { best_ms = ms; best = cand; }
     }
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
     if (s != LG_OK) return s;
     fw_tuned.push_back({key, best});
     fw_choice = best;
