@@ -515,6 +515,8 @@ typedef struct lg_request {
  * same, bit for bit, as the request's alone. */
 lg_status lg_server_create(const lg_server_opts* opts, lg_server** out);
 lg_status lg_server_destroy(lg_server* srv);
+/* The description of the last failed server call made by the calling thread
+ * (each thread reads its own; valid until that thread's next server call). */
 const char* lg_server_last_error(const lg_server* srv);
 /* Uploads a volume (density and optional temperature) that stays resident for
  * the server's lifetime; *volume_id names it in requests. */

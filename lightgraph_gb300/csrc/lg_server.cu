@@ -107,6 +107,10 @@ struct PathBatcher {
 // How long a batch waits for slots still marching their edges.
 constexpr double kPathWaitUs = 300.0;
 
+// The description of the last failed server call made by this thread (the
+// server's calls come from many threads: each reads its own).
+thread_local std::string t_server_err;
+
 }  // namespace
 
 struct lg_server {
@@ -120,7 +124,6 @@ struct lg_server {
     uint64_t inflight_bytes = 0;
     int64_t next_ticket = 1;
     bool stop = false;
-    std::string err;
     std::unique_ptr<Ctx> upload_ctx;
     PathBatcher paths;
 
@@ -175,16 +178,16 @@ void lg_server::admit_locked() {
 void lg_server::run_path_batch(std::vector<PathJob*>& batch) {
     Ctx& b = *paths.ctx;
     lg_status st = LG_OK;
-    float* base = nullptr;
-    for (PathJob* j : batch) {
-        float* S = j->slot->ctx->d_S.as<float>();
-        if (!base || S < base) base = S;
-    }
+    // the lowest of the members' matrix buffers; each member's offset from
+    // it in floats (cudaMalloc aligns every buffer to 256 bytes)
+    uintptr_t lowest = UINTPTR_MAX;
+    for (PathJob* j : batch) lowest = std::min(lowest, reinterpret_cast<uintptr_t>(j->slot->ctx->d_S.p));
+    float* base = reinterpret_cast<float*>(lowest);
     b.h_graphs.clear();
     b.max_n = 0;
     for (PathJob* j : batch) {
         const Ctx& c = *j->slot->ctx;
-        const int64_t shift = c.d_S.as<float>() - base;
+        const int64_t shift = (int64_t)((reinterpret_cast<uintptr_t>(c.d_S.p) - lowest) / sizeof(float));
         for (GraphInfo g : c.h_graphs) {
             g.s_off += shift;
             b.h_graphs.push_back(g);
@@ -410,7 +413,7 @@ extern "C" lg_status lg_server_stats(lg_server* srv, uint64_t* path_launches, ui
     return LG_OK;
 }
 
-extern "C" const char* lg_server_last_error(const lg_server* srv) { return srv ? srv->err.c_str() : "null server"; }
+extern "C" const char* lg_server_last_error(const lg_server* srv) { return srv ? t_server_err.c_str() : "null server"; }
 
 extern "C" lg_status lg_server_add_volume(lg_server* srv, const lg_grid_desc* density, const float* density_values,
                                           const lg_grid_desc* temperature, const float* temperature_values,
@@ -421,7 +424,7 @@ extern "C" lg_status lg_server_add_volume(lg_server* srv, const lg_grid_desc* de
     cudaSetDevice(c.device);
     auto v = std::make_unique<Volume>();
     lg_status st = c.upload_grid(LG_GRID_DENSITY, density, density_values, storage_dtype);
-    if (st != LG_OK) { srv->err = c.err; return st; }
+    if (st != LG_OK) { t_server_err = c.err; return st; }
     // move the uploaded stores into the volume (the buffers change owner)
     take_buffers(v->dens, c.dens);
     v->dens.g = c.dens.g;
@@ -433,7 +436,7 @@ extern "C" lg_status lg_server_add_volume(lg_server* srv, const lg_grid_desc* de
     c.dens.valid = false;
     if (temperature && temperature_values) {
         st = c.upload_grid(LG_GRID_TEMPERATURE, temperature, temperature_values, storage_dtype);
-        if (st != LG_OK) { srv->err = c.err; return st; }
+        if (st != LG_OK) { t_server_err = c.err; return st; }
         take_buffers(v->temp, c.temp);
         v->temp.g = c.temp.g;
         v->temp.desc = c.temp.desc;
@@ -456,8 +459,7 @@ extern "C" lg_status lg_server_submit(lg_server* srv, const lg_request* req, int
     // the point layout is checked here, before the request's arrays are
     // copied (the same rules as lg_build_graphs)
     auto refuse = [&](const char* why) {
-        std::lock_guard<std::mutex> lk(srv->mu);
-        srv->err = why;
+        t_server_err = why;
         return LG_ERR_INVALID;
     };
     if (req->offsets[0] != 0) return refuse("offsets[0] must be 0");
@@ -487,15 +489,15 @@ extern "C" lg_status lg_server_submit(lg_server* srv, const lg_request* req, int
     q->bytes = lg_request_bytes(req);
     std::lock_guard<std::mutex> lk(srv->mu);
     if (req->volume < 0 || req->volume >= (int)srv->volumes.size()) {
-        srv->err = "unknown volume";
+        t_server_err = "unknown volume";
         return LG_ERR_INVALID;
     }
     if ((int)srv->queue.size() >= srv->opts.queue_capacity) {
-        srv->err = "queue full";
+        t_server_err = "queue full";
         return LG_ERR_BUSY;
     }
     if (q->bytes > srv->opts.hbm_budget_bytes) {
-        srv->err = "request exceeds the HBM budget";
+        t_server_err = "request exceeds the HBM budget";
         return LG_ERR_NOMEM;
     }
     q->ticket = srv->next_ticket++;
@@ -513,7 +515,7 @@ extern "C" lg_status lg_server_poll(lg_server* srv, int64_t ticket, int* done) {
     std::lock_guard<std::mutex> lk(srv->mu);
     auto it = srv->requests.find(ticket);
     if (it == srv->requests.end()) {
-        srv->err = "unknown ticket";
+        t_server_err = "unknown ticket";
         return LG_ERR_INVALID;
     }
     *done = it->second->done ? 1 : 0;
@@ -526,7 +528,7 @@ extern "C" lg_status lg_server_wait(lg_server* srv, int64_t ticket, int timeout_
     std::unique_lock<std::mutex> lk(srv->mu);
     auto it = srv->requests.find(ticket);
     if (it == srv->requests.end()) {
-        srv->err = "unknown ticket";
+        t_server_err = "unknown ticket";
         return LG_ERR_INVALID;
     }
     Request* q = it->second.get();
@@ -534,7 +536,7 @@ extern "C" lg_status lg_server_wait(lg_server* srv, int64_t ticket, int timeout_
     if (timeout_ms < 0) srv->cv.wait(lk, ready);
     else if (!srv->cv.wait_for(lk, std::chrono::milliseconds(timeout_ms), ready)) return LG_ERR_TIMEOUT;
     const lg_status st = q->status;
-    if (st != LG_OK) srv->err = q->err;
+    if (st != LG_OK) t_server_err = q->err;
     if (st == LG_OK && rgba) std::memcpy(rgba, q->rgba.data(), sizeof(float) * q->rgba.size());
     if (queue_us) *queue_us = q->t_admit - q->t_submit;
     if (latency_us) *latency_us = q->t_done - q->t_submit;
