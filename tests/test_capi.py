@@ -70,6 +70,59 @@ def test_server_entry_points_reject_null_handles():
     assert lib.lg_server_destroy(None) in (_capi.LG_OK, _capi.LG_ERR_INVALID)
 
 
+def request_bytes_restated(sizes, max_connect, width, height, spp, env_wh=None):
+    """The serving admission estimate (lg_request_bytes) restated: per graph
+    its padded FP32 matrix and edge slots; per point its position,
+    candidates, graph id, vertex vectors and diffusion partial sums; per pixel
+    the four films; per pixel sample its count, offset and primary results;
+    the point bins; the env map with its CDFs."""
+    b = 0
+    for n in sizes:
+        ld = (max(n, 1) + 127) // 128 * 128
+        b += ld * ld * 4 + n * max_connect // 2 * 8
+    P = sum(sizes)
+    b += P * (12 + 96 * 2 + 4 + 4) + P * 4 * (3 + 3 + 3 + 3 * 16)
+    b += width * height * 64 + width * height * max(spp, 1) * 44
+    b += 160 * 160 * 160 * 12
+    if env_wh:
+        w, h = env_wh
+        b += w * h * 4 * 5 + h * 4 * 262
+    return b
+
+
+def test_request_bytes_admission_estimate():
+    """lg_request_bytes, the HBM estimate the server admits requests by, is
+    pure host arithmetic (no GPU needed): it matches its restatement, grows
+    with the graphs and the image, and is 0 for a request without graphs."""
+    lib = _capi.load()
+
+    def make(sizes, mc, w, h, spp, env=None):
+        offs = np.zeros(len(sizes) + 1, np.int64)
+        offs[1:] = np.cumsum(sizes)
+        q = _capi.RequestC()
+        q.n_graphs = len(sizes)
+        q.offsets = offs.ctypes.data
+        q.max_connect = mc
+        q.camera.width, q.camera.height, q.camera.samples = w, h, spp
+        if env is not None:
+            q.env_rgb = env.ctypes.data
+            q.env_h, q.env_w = env.shape[0], env.shape[1]
+        return q, offs
+
+    cases = [([100, 300], 12, 64, 32, 2, None), ([4096], 12, 1024, 1024, 4, None),
+             ([0, 1, 129], 0, 16, 16, 0, None), ([512], 7, 128, 128, 1, (8, 4))]
+    for sizes, mc, w, h, spp, env_wh in cases:
+        env = np.zeros((env_wh[1], env_wh[0], 3), np.float32) if env_wh else None
+        q, offs = make(sizes, mc, w, h, spp, env)
+        assert lib.lg_request_bytes(C.byref(q)) == request_bytes_restated(sizes, mc, w, h, spp, env_wh)
+    small, _o1 = make([256], 12, 64, 64, 1)
+    big, _o2 = make([256, 2048], 12, 256, 256, 4)
+    assert lib.lg_request_bytes(C.byref(big)) > lib.lg_request_bytes(C.byref(small))
+    empty = _capi.RequestC()
+    assert lib.lg_request_bytes(C.byref(empty)) == 0
+    assert lib.lg_request_bytes(None) == 0
+
+
 def test_noalloc_diffuse_argument_checks():
     """lg_diffuse_noalloc validates its arguments before touching the device:
     bad sizes, a leading dimension below n, null buffers and a positive
