@@ -2,7 +2,7 @@
  * lightgraph_scene.h -- seeded synthetic inputs for the LightGraph path.
  *
  * The reference renders OpenVDB files and EXR environment maps that are not
- * shipped with it (scenes/*.sh point at /path/to/...). These host functions
+ * shipped with it (its scenes/ scripts point at /path/to/...). These host functions
  * build the stand-in inputs deterministically from a seed: fBm value-noise
  * volumes, interior point sets and a sky environment map. They have no
  * counterpart in the reference; the C ABI in lightgraph_c.h consumes their
