@@ -137,6 +137,68 @@ def test_env_cdf_step_function():
     assert mc[0] == 0 and mc[-1] == pytest.approx(1.0)
 
 
+def splat_kernel(K, hp):
+    """src/ScatterGrid.h:69-75: radius from the point index's voxel size
+    (voxelSize^3 first, cube root by pow) and the truncated Gaussian's
+    sigma^2 (weight 0.1 at the radius)."""
+    r = ((3.0 * K * (hp * hp * hp)) / (32.0 * np.pi)) ** (1.0 / 3.0)
+    return r, -(r * r) / (2.0 * np.log(0.1))
+
+
+def voxel_d2(wpos, p):
+    """Vec3s diff = worldPos - point, lengthSqr in float (ScatterGrid.h:86)."""
+    e = [np.float32(wpos[a] - np.float64(p[a])) for a in range(3)]
+    return np.float32(np.float32(e[0] * e[0] + e[1] * e[1]) + e[2] * e[2])
+
+
+def test_splat_single_point_known_answer():
+    """One point: every active coarse voxel whose centre lies within the
+    kernel radius takes the point's radiance (a weighted mean of one value),
+    every other voxel 0 (src/ScatterGrid.h:77-98)."""
+    g, sh, opts = slab_scene(1.0, res=32)   # every coarse voxel active
+    o = po.Oracle(g, sh, opts)
+    pts = np.array([[1.3, -0.7, 2.1]], np.float32)
+    D = np.array([[0.2, 0.5, 0.9]])
+    K, hp, f = 3.0, 8.0, 4
+    lo, dims, out, r = o.splat(pts, D, point_voxel_size=hp, factor=f, kernel_points=K)
+    r_ref, _ = splat_kernel(K, hp)
+    assert r == pytest.approx(r_ref, rel=1e-15)
+    H = 1.0 * f
+    inside = 0
+    for cz in range(dims[2]):
+        for cy in range(dims[1]):
+            for cx in range(dims[0]):
+                wpos = ((lo[0] + cx) * H, (lo[1] + cy) * H, (lo[2] + cz) * H)
+                v = out[cz, cy, cx]
+                if float(voxel_d2(wpos, pts[0])) < r_ref * r_ref:
+                    inside += 1
+                    assert np.allclose(v, D[0], rtol=1e-15, atol=0)
+                else:
+                    assert (v == 0).all()
+    assert inside > 0
+
+
+def test_splat_two_points_weighted_mean():
+    """Two points around one coarse voxel: the Gaussian-weighted mean with
+    w = exp(-d^2 / (2 sigma^2)) (src/ScatterGrid.h:84-95)."""
+    g, sh, opts = slab_scene(1.0, res=32)
+    o = po.Oracle(g, sh, opts)
+    K, hp, f = 3.0, 8.0, 4
+    r, s2 = splat_kernel(K, hp)
+    H = 1.0 * f
+    # points near the coarse voxel centred at the world origin
+    pts = np.array([[0.9, 0.4, -0.3], [-1.7, 1.1, 0.6]], np.float32)
+    D = np.array([[1.0, 0.0, 0.25], [0.0, 2.0, 0.75]])
+    lo, dims, out, _ = o.splat(pts, D, point_voxel_size=hp, factor=f, kernel_points=K)
+    c = [-lo[a] for a in range(3)]  # the coarse voxel at index 0 (world origin)
+    w = [np.exp(-(1.0 / (2.0 * s2)) * float(voxel_d2((0.0, 0.0, 0.0), p))) for p in pts]
+    assert all(float(voxel_d2((0.0, 0.0, 0.0), p)) < r * r for p in pts)
+    expect = (D[0] * w[0] + D[1] * w[1]) / (w[0] + w[1])
+    assert np.allclose(out[c[2], c[1], c[0]], expect, rtol=1e-12, atol=0)
+    # the weight at exactly the radius is the truncation tail, 0.1
+    assert np.exp(-(1.0 / (2.0 * s2)) * r * r) == pytest.approx(0.1, rel=1e-12)
+
+
 def test_render_empty_grid_is_transparent():
     res = 16
     g = Grid(np.zeros((res, res, res), np.float32), (-8,) * 3, 0.1)
