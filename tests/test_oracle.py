@@ -199,6 +199,58 @@ def test_splat_two_points_weighted_mean():
     assert np.exp(-(1.0 / (2.0 * s2)) * r * r) == pytest.approx(0.1, rel=1e-12)
 
 
+def test_vertex_light_unshadowed_known_answer():
+    """A medium thinner than the cutoff everywhere: every shadow sample is
+    skipped (src/LightGraph.h:480), so each vertex sees the light unshadowed:
+    albedo * I with I = colour * intensity for a distant light and
+    colour * intensity / (1 + 4 pi r^2) for a point light, r^2 in float
+    (src/Light.h:79-89,118-126)."""
+    g, sh, opts = slab_scene(1e-6, res=32)
+    albedo = np.array(sh.getAlbedo())
+    pts = np.array([[0.5, -3.25, 2.0], [-7.5, 6.0, -1.5], [10.25, 0.0, 4.75]], np.float32)
+    o = po.Oracle(g, sh, opts, [Light.parse("dir:0:1,0.5,0.25:2.0:-40,30,0")])
+    L = o.vertex_light(pts)
+    assert np.allclose(L, albedo * np.array([1.0, 0.5, 0.25]) * 2.0, rtol=1e-15, atol=0)
+    pos = np.array([3.0, -2.0, 25.0])
+    o = po.Oracle(g, sh, opts, [Light.parse("point:0:0.4,0.6,1.0:30:3,-2,25")])
+    L = o.vertex_light(pts)
+    for i, p in enumerate(pts):
+        r2 = float(np.float32(np.sum((p.astype(np.float64) - pos) ** 2)))
+        expect = albedo * np.array([0.4, 0.6, 1.0]) * 30.0 / (1.0 + 4.0 * np.pi * r2)
+        assert np.allclose(L[i], expect, rtol=1e-12, atol=0), (i, L[i], expect)
+
+
+def test_diffusion_known_answer():
+    """diffuseLight (src/LightGraph.h:562-579): every column of the solved
+    path matrix is divided by max(its sum, 1) per channel, then
+    D_i = sum_j L_j * P_ij. With the diagonal at 1 (floydAlgo sets it,
+    src/LightGraph.h:530-534) every column sums to at least 1; a matrix with a
+    smaller diagonal shows the max(., 1): its thin columns are left as they
+    are."""
+    T = np.zeros((3, 3, 3))
+    for i in range(3):
+        T[i, i] = 1.0
+    T[0, 1] = T[1, 0] = [0.5, 0.25, 0.125]
+    T[1, 2] = T[2, 1] = [0.0, 0.5, 0.0]
+    T[0, 2] = T[2, 0] = [0.25, 0.0, 0.75]
+    L = np.array([[1.0, 2.0, 3.0], [0.5, 0.0, 1.0], [4.0, 1.0, 0.25]])
+    o = po.Oracle(*slab_scene(0.5, res=16))
+    D = o.diffuse(T, L)
+    c = np.maximum(T.sum(axis=0), 1.0)       # per column j and channel
+    expect = np.einsum("jc,ijc->ic", L, T / c[None, :, :])
+    assert np.allclose(D, expect, rtol=1e-14, atol=0)
+    assert c[2, 1] == 1.5  # 0 + 0.5 + 1
+    # a diagonal of 0.25: column 1 sums to 0.25 + 0.5 + 0 = 0.75 in channel 0
+    # (kept as it is), 0.25 + 0.25 + 0.5 = 1.0 in channel 1
+    T2 = T.copy()
+    for i in range(3):
+        T2[i, i] = 0.25
+    D2 = o.diffuse(T2, L)
+    c2 = np.maximum(T2.sum(axis=0), 1.0)
+    assert T2.sum(axis=0)[1, 0] == 0.75 and c2[1, 0] == 1.0
+    assert np.allclose(D2, np.einsum("jc,ijc->ic", L, T2 / c2[None, :, :]), rtol=1e-14, atol=0)
+
+
 def test_render_empty_grid_is_transparent():
     res = 16
     g = Grid(np.zeros((res, res, res), np.float32), (-8,) * 3, 0.1)
