@@ -262,6 +262,35 @@ def test_render_empty_grid_is_transparent():
     assert np.all(direct == 0) and np.all(scatter == 0) and np.all(emission == 0)
 
 
+def test_render_emission_telescopes_to_alpha():
+    """No lights and no scatter grid: the beauty is the emission AOV, and its
+    per-sample sum of E * pTrans * (1 - dT), pTrans *= dT after each sample
+    (src/Renderer.h:598,653-660), telescopes to E * (1 - pTrans at the end).
+    With a grey extinction the alpha is 1 - pTrans (src/Renderer.h:674-677),
+    so the emission AOV is the emission colour times the alpha in every
+    pixel, whatever the jittered steps and early termination."""
+    res = 32
+    dens = np.zeros((res, res, res), np.float32)
+    dens[8:24, 8:24, 8:24] = 0.6
+    g = Grid(dens, (-16,) * 3, 0.05)
+    # a constant temperature over a larger box: every sample reads 700
+    temp = Grid(np.full((48, 48, 48), 700.0, np.float32), (-24,) * 3, 0.05)
+    sh = Shader()
+    sh.setScattering(0.3)
+    sh.setAbsorption(0.1)
+    sh.setEmissionScale(2.0)
+    sh.setEmissionColorRamp(ColorRamp.parse("0,1/1,0.5,0.25:1,0.5,0.25/0/1000"))
+    opts = SceneSettings(width=12, height=10, samples=2, camTranslate=(0, 0, 3), iter=1)
+    o = po.Oracle(g, sh, opts, [], temperature=temp)
+    rgba, direct, scatter, emission = o.render()
+    alpha = rgba[..., 3]
+    assert alpha.max() > 0.3 and alpha.min() == 0.0  # the cube and the background
+    assert (direct == 0).all() and (scatter == 0).all()
+    E = np.array([1.0, 0.5, 0.25]) * 2.0
+    assert np.allclose(emission[..., :3], E * alpha[..., None], rtol=1e-9, atol=1e-15)
+    assert np.allclose(rgba[..., :3], emission[..., :3], rtol=1e-15, atol=0)
+
+
 def test_small_scene_oracle_runs_and_conserves_energy():
     sc = scenes.small(n_points=200, width=16, height=16)
     o = po.Oracle(sc.density, sc.shader, sc.opts, sc.lights)
