@@ -224,6 +224,45 @@ def test_tiny_env_maps_vs_fp64_oracle(gpu_ctx, wh):
         assert e <= 1e-3, (wh, name, e)
 
 
+def test_emission_telescopes_to_alpha(gpu_ctx):
+    """The oracle's known answer on the GPU path: no lights, no scatter grid,
+    a grey medium at a constant temperature. The emission AOV is the emission
+    colour times the alpha in every pixel (the per-sample sum telescopes to
+    1 - pTrans; FP32 accumulation: 1e-4), and every AOV matches the FP64
+    oracle (rel-RMSE 1e-3)."""
+    from lightgraph_gb300 import Context
+    from lightgraph_gb300.lightgraph import ColorRamp, Grid, SceneSettings, Shader
+    res = 32
+    dens = np.zeros((res, res, res), np.float32)
+    dens[8:24, 8:24, 8:24] = 0.6
+    g = Grid(dens, (-16,) * 3, 0.05)
+    temp = Grid(np.full((48, 48, 48), 700.0, np.float32), (-24,) * 3, 0.05)
+    sh = Shader()
+    sh.setScattering(0.3)
+    sh.setAbsorption(0.1)
+    sh.setEmissionScale(2.0)
+    sh.setEmissionColorRamp(ColorRamp.parse("0,1/1,0.5,0.25:1,0.5,0.25/0/1000"))
+    opts = SceneSettings(width=12, height=10, samples=2, camTranslate=(0, 0, 3), iter=1)
+    ctx = Context(0)  # a fresh context: no scatter grid from earlier tests
+    try:
+        ctx.upload_density(g)
+        ctx.upload_temperature(temp)
+        ctx.set_shader(sh)
+        ctx.set_settings(opts)
+        ctx.set_lights([])
+        films = ctx.render(opts)
+    finally:
+        ctx.close()
+    alpha = films.rgba[..., 3].astype(np.float64)
+    assert alpha.max() > 0.3 and alpha.min() == 0.0
+    assert (films.direct == 0).all() and (films.scatter == 0).all()
+    E = np.array([1.0, 0.5, 0.25]) * 2.0
+    assert np.allclose(films.emission[..., :3], E * alpha[..., None], rtol=1e-4, atol=1e-4)
+    ref = po.Oracle(g, sh, opts, [], temperature=temp).render()
+    for got, r in ((films.rgba, ref[0]), (films.emission, ref[3])):
+        assert rel_rmse(got, r) <= 1e-3
+
+
 def test_deterministic(gpu_ctx, small_scene):
     sc = small_scene
     scenes.load_into(gpu_ctx, sc)
