@@ -263,6 +263,41 @@ def test_emission_telescopes_to_alpha(gpu_ctx):
         assert rel_rmse(got, r) <= 1e-3
 
 
+def test_vertex_light_unshadowed_known_answer():
+    """The oracle's unshadowed known answer on the GPU path: in a medium
+    thinner than the cutoff every shadow sample is skipped, so a vertex sees
+    albedo * colour * intensity from a distant light and the same over
+    1 + 4 pi r^2 from a point light (FP32: 1e-5)."""
+    if not pytest.importorskip("torch").cuda.is_available():
+        pytest.skip("no CUDA device")
+    from lightgraph_gb300 import Context
+    from lightgraph_gb300.lightgraph import Grid, Light, SceneSettings, Shader
+    g = Grid(np.full((32, 32, 32), 1e-6, np.float32), (-16,) * 3, 1.0)
+    sh = Shader()
+    sh.setScattering(0.09)
+    sh.setAbsorption(0.01)
+    albedo = np.array(sh.getAlbedo())
+    pts = np.array([[0.5, -3.25, 2.0], [-7.5, 6.0, -1.5], [10.25, 0.0, 4.75]], np.float32)
+    pos = np.array([3.0, -2.0, 25.0])
+    r2 = np.array([float(np.float32(np.sum((p.astype(np.float64) - pos) ** 2))) for p in pts])
+    cases = [("dir:0:1,0.5,0.25:2.0:-40,30,0", np.tile(albedo * np.array([1.0, 0.5, 0.25]) * 2.0, (3, 1))),
+             ("point:0:0.4,0.6,1.0:30:3,-2,25",
+              albedo * np.array([0.4, 0.6, 1.0]) * 30.0 / (1.0 + 4.0 * np.pi * r2[:, None]))]
+    ctx = Context(0)
+    try:
+        ctx.upload_density(g)
+        ctx.upload_temperature(None)
+        ctx.set_shader(sh)
+        ctx.set_settings(SceneSettings(iter=1))
+        ctx.build_graphs([pts], [np.float32(0.0)], 12)
+        for spec, expect in cases:
+            ctx.set_lights([Light.parse(spec)])
+            L = ctx.vertex_light(want=True)
+            assert np.allclose(L, expect, rtol=1e-5, atol=0), (spec, L, expect)
+    finally:
+        ctx.close()
+
+
 def test_deterministic(gpu_ctx, small_scene):
     sc = small_scene
     scenes.load_into(gpu_ctx, sc)
