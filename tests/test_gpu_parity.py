@@ -298,6 +298,41 @@ def test_vertex_light_unshadowed_known_answer():
         ctx.close()
 
 
+def test_edge_march_density_min_known_answer():
+    """The oracle's known answer on the GPU's edge march: inside existing
+    leaves of zero density an edge gathers scatterDensityMin * step per sample
+    while scatterDensityMin is at or above the cutoff, and nothing below it
+    (src/LightGraph.h:390-395)."""
+    if not pytest.importorskip("torch").cuda.is_available():
+        pytest.skip("no CUDA device")
+    from lightgraph_gb300 import Context
+    from lightgraph_gb300.lightgraph import Grid, SceneSettings, Shader
+    res = 32
+    g = Grid(np.zeros((res, res, res), np.float32), (-res // 2,) * 3, 1.0,
+             leaf_mask=np.ones((res // 8,) * 3, np.uint8))
+    p = np.array([[-12.3, 0.2, 0.1], [11.7, 0.2, 0.1]], np.float32)
+    dist = float(np.float32(np.linalg.norm(p[1].astype(np.float64) - p[0].astype(np.float64))))
+    n_samples = len(np.arange(np.ceil(1e-9 / 3.0), np.floor(dist / 3.0) + 1))
+    r2 = np.float32(30.0) * np.float32(30.0)
+    ctx = Context(0)
+    try:
+        ctx.upload_density(g)
+        ctx.upload_temperature(None)
+        ctx.set_settings(SceneSettings(iter=1))
+        for dmin, expect in ((0.025, n_samples * 0.025 * 3.0), (0.001, 0.0)):
+            sh = Shader()
+            sh.setScattering(0.09)
+            sh.setAbsorption(0.01)
+            sh.setScatterDensityMin(dmin)
+            ctx.set_shader(sh)
+            ctx.build_graphs([p], [r2], 12)
+            S = ctx.march_edges(want=True)[0]
+            assert S[0, 1] == S[1, 0]
+            assert S[0, 1] == pytest.approx(expect, rel=1e-5, abs=1e-7), (dmin, S[0, 1], expect)
+    finally:
+        ctx.close()
+
+
 def test_deterministic(gpu_ctx, small_scene):
     sc = small_scene
     scenes.load_into(gpu_ctx, sc)

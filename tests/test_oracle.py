@@ -35,6 +35,29 @@ def test_homogeneous_edge_transmittance():
     assert np.allclose(T[0, 1], np.exp(-0.1 * len(ks) * x * 3.0), rtol=1e-12)
 
 
+def test_edge_march_density_min_in_empty_leaves():
+    """Inside existing leaves of zero density an edge still gathers
+    scatterDensityMin * step per sample while scatterDensityMin is at or above
+    the cutoff (src/LightGraph.h:390-395), and nothing once it is below."""
+    res = 32
+    vals = np.zeros((res, res, res), np.float32)
+    mask = np.ones((res // 8,) * 3, np.uint8)  # every leaf exists, all voxels 0
+    g = Grid(vals, (-res // 2,) * 3, 1.0, leaf_mask=mask)
+    sh = Shader()
+    sh.setScattering(0.09)
+    sh.setAbsorption(0.01)
+    opts = SceneSettings(width=8, height=8, iter=1)
+    p = np.array([[-12.3, 0.2, 0.1], [11.7, 0.2, 0.1]], np.float32)
+    adj = np.array([[0, 1], [1, 0]], np.uint8)
+    dist = float(np.float32(np.linalg.norm(p[1].astype(np.float64) - p[0].astype(np.float64))))
+    ks = np.arange(np.ceil(1e-9 / 3.0), np.floor(dist / 3.0) + 1)
+    T, S = po.Oracle(g, sh, opts).march_edges(p, adj)
+    assert S[0, 1] == pytest.approx(len(ks) * 0.025 * 3.0, rel=1e-12)  # the default densityMin 0.025
+    sh.setScatterDensityMin(0.001)  # below the cutoff 0.005: every sample skipped
+    T, S = po.Oracle(g, sh, opts).march_edges(p, adj)
+    assert S[0, 1] == 0.0 and np.allclose(T[0, 1], 1.0)
+
+
 def test_edge_dropout_and_miss():
     g, sh, opts = slab_scene(1.0)
     sh.setScatterDensityScale(10.0)
