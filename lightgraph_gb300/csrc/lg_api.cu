@@ -549,8 +549,6 @@ DevScene Ctx::scene() const {
     d.ramp_in = (float)s.ramp_in;
     d.ramp_out = (float)s.ramp_out;
     {
-        const float span = d.ramp_out - d.ramp_in;
-        d.ramp_inv_in = 1.0f / span;
         const int n = std::min(s.ramp_n, kMaxRamp);
         for (int k = 0; k < n; ++k) {
             const float gap = k + 1 < n ? d.ramp_pos[k + 1] - d.ramp_pos[k] : d.ramp_pos[0] - d.ramp_pos[k];

@@ -418,9 +418,8 @@ struct DevShader {
     int ramp_n;
     float ramp_pos[kMaxRamp];
     float ramp_col[kMaxRamp][3];
-    // 1 / (ramp_out - ramp_in), and per knot i the reciprocal of the interval
-    // to the next knot (the last knot: to the first, ColorRamp's wrap)
-    float ramp_inv_in;
+    // per knot i the reciprocal of the interval to the next knot (the last
+    // knot: to the first, ColorRamp's wrap)
     float ramp_inv[kMaxRamp];
     float ramp_in, ramp_out;
 };
@@ -474,13 +473,17 @@ struct DevScene {
     ShadowMarch smarch;
 };
 
-// ColorRamp::getColor (src/Shader.h:63-92), including its edge behaviour;
-// its two divisions as products with reciprocals made on the host (within
-// an ulp of the quotients; a temperature below the first knot still gives
-// the quotient by zero).
+// ColorRamp::getColor (src/Shader.h:63-92), including its edge behaviour.
+// The remap to [0, 1] is a division, so a temperature that maps exactly onto
+// a knot lands on it as the reference's does (a product with a reciprocal of
+// the range can land a rounding below the first knot, in the empty interval
+// whose quotient is 0/0); the blend inside an interval is a product with the
+// interval's reciprocal made on the host (within an ulp of the quotient, and
+// exactly 0 on a knot; a temperature below the first knot still gives the
+// quotient by zero).
 __device__ __forceinline__ void ramp_color(const DevShader& sh, float temp, float out[3]) {
     if (sh.ramp_n == 0) { out[0] = out[1] = out[2] = 0.f; return; }
-    float x = (temp - sh.ramp_in) * sh.ramp_inv_in;
+    float x = (temp - sh.ramp_in) / (sh.ramp_out - sh.ramp_in);
     x = fminf(fmaxf(x, 0.f), 1.f);
     if (sh.ramp_n == 1) {
         out[0] = sh.ramp_col[0][0]; out[1] = sh.ramp_col[0][1]; out[2] = sh.ramp_col[0][2];

@@ -333,6 +333,35 @@ def test_edge_march_density_min_known_answer():
         ctx.close()
 
 
+def test_color_ramp_wrap_on_gpu():
+    """ColorRamp::getColor's blend past the last knot (towards the first knot,
+    with a negative weight) and between knots, through the GPU's vertex
+    emission (no lights: L = ramp(temperature) * emissionScale), against the
+    same known answers as the oracle's test (FP32: 1e-5)."""
+    if not pytest.importorskip("torch").cuda.is_available():
+        pytest.skip("no CUDA device")
+    from lightgraph_gb300 import Context
+    from lightgraph_gb300.lightgraph import ColorRamp, Grid, SceneSettings, Shader
+    from .test_oracle import ramp_wrap_cases
+    res = 32
+    sh = Shader()
+    sh.setEmissionScale(2.0)
+    sh.setEmissionColorRamp(ColorRamp([0.2, 0.8], [[1, 0, 0], [0, 0, 1]], 100.0, 300.0))
+    ctx = Context(0)
+    try:
+        ctx.upload_density(Grid(np.full((res, res, res), 0.5, np.float32), (-16,) * 3, 1.0))
+        ctx.set_shader(sh)
+        ctx.set_settings(SceneSettings(iter=1))
+        ctx.set_lights([])
+        ctx.build_graphs([np.zeros((1, 3), np.float32)], [np.float32(0.0)], 12)
+        for temp, expect in ramp_wrap_cases():
+            ctx.upload_temperature(Grid(np.full((res, res, res), temp, np.float32), (-16,) * 3, 1.0))
+            L = ctx.vertex_light(want=True)
+            assert np.allclose(L[0], 2.0 * expect, rtol=1e-5, atol=1e-6), (temp, L[0], expect)
+    finally:
+        ctx.close()
+
+
 def test_deterministic(gpu_ctx, small_scene):
     sc = small_scene
     scenes.load_into(gpu_ctx, sc)

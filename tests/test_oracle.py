@@ -142,6 +142,43 @@ def test_color_ramp_knots_via_vertex_emission():
         assert np.allclose(L[0], 2.0 * np.array(expect)), temp
 
 
+def ramp_wrap_cases():
+    """ColorRamp::getColor (src/Shader.h:63-92) with knots at 0.2 and 0.8 over
+    temperatures 100..300: between the knots a linear blend; at a knot its
+    colour; past the last knot the blend runs towards the FIRST knot (next
+    stays at index 0), with a negative weight. Returns (temperature,
+    expected colour) pairs."""
+    pos, col = [0.2, 0.8], np.array([[1.0, 0.0, 0.0], [0.0, 0.0, 1.0]])
+    out = []
+    for t in (200.0, 140.0, 260.0, 280.0, 300.0):
+        x = min(max((t - 100.0) / (300.0 - 100.0), 0.0), 1.0)
+        prev, nxt = 0, 0
+        for i, p in enumerate(pos):
+            if p <= x:
+                prev = i
+            else:
+                nxt = i
+                break
+        b = (x - pos[prev]) / (pos[nxt] - pos[prev])
+        out.append((t, col[prev] * (1.0 - b) + col[nxt] * b))
+    return out
+
+
+def test_color_ramp_wraps_past_the_last_knot():
+    res = 32
+    g = Grid(np.full((res, res, res), 0.5, np.float32), (-16,) * 3, 1.0)
+    sh = Shader()
+    sh.setEmissionScale(2.0)
+    sh.setEmissionColorRamp(ColorRamp([0.2, 0.8], [[1, 0, 0], [0, 0, 1]], 100.0, 300.0))
+    opts = SceneSettings(iter=1)
+    cases = ramp_wrap_cases()
+    assert np.allclose(cases[3][1], [-1.0 / 6.0, 0.0, 7.0 / 6.0])  # x = 0.9: weight -1/6 on the first knot
+    for temp, expect in cases:
+        tg = Grid(np.full((res, res, res), temp, np.float32), (-16,) * 3, 1.0)
+        L = po.Oracle(g, sh, opts, [], temperature=tg).vertex_light(np.zeros((1, 3), np.float32))
+        assert np.allclose(L[0], 2.0 * expect, rtol=1e-12, atol=1e-15), (temp, L[0], expect)
+
+
 def test_env_cdf_step_function():
     """Distribution1D over a step function (src/Sampling.h:81-93): the CDF is
     the normalised running sum of func/n."""
