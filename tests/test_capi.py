@@ -218,3 +218,27 @@ def test_fw_queue_cannot_deadlock(sizes, sym):
     else:
         want = sum(nt * (2 * nt - 1) + (nt * nu * nu if nt >= 2 else 0) for nt, nu in zip(nts, nus))
     assert n.value == want
+
+
+# the reference's command-line flags (src/main.cc:359-470)
+REFERENCE_FLAGS = [
+    "-absorption", "-camPos", "-camRot", "-camYRot", "-cutoff", "-densityMax", "-densityScale", "-emissionScale",
+    "-exrOut", "-focal", "-geoDump", "-h", "-help", "-iter", "-light", "-primaryStep", "-ptsPerKernel", "-resHeight",
+    "-resWidth", "-samples", "-scatterDensityMaskPower", "-scatterDensityMin", "-scatterDensityScale",
+    "-scatterGridResFactor", "-scatterScale", "-scattering", "-shadowDensityScale", "-shadowStep",
+    "-tempColorRamp", "-v", "-vdbIn", "-volumeColor",
+]
+
+
+def test_cli_help_lists_every_reference_flag():
+    """The command-line renderer keeps the reference's flags (its scene
+    scripts run unchanged apart from the input): its help, which needs no
+    GPU, names every one of them (-vdbIn as unsupported without OpenVDB)."""
+    import subprocess
+    from lightgraph_gb300 import build
+    build.build_library()
+    r = subprocess.run([build.cli_path(), "-h"], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 0, r.stderr
+    words = set(re.findall(r"-[A-Za-z]+", r.stdout))
+    missing = [f for f in REFERENCE_FLAGS if f not in words]
+    assert not missing, missing
