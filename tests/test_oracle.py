@@ -126,6 +126,55 @@ def test_greedy_graph_cap_order():
     assert adj2.sum() == 0
 
 
+def build_graph_restated(pts, r2, max_connect):
+    """LightGraph::buildGraph's loop as the reference writes it
+    (src/LightGraph.h:297-310): for i, for j, stop row i once it is full, skip
+    a full j, connect i < j when the FP64 lengthSqr of the difference is below
+    the FP32 radius squared."""
+    n = len(pts)
+    P = pts.astype(np.float64)
+    cnt = [0] * n
+    adj = np.zeros((n, n), np.uint8)
+    edges = 0
+    r2d = float(np.float32(r2))
+    for i in range(n):
+        for j in range(n):
+            if cnt[i] >= max_connect:
+                break
+            if cnt[j] >= max_connect:
+                continue
+            if i < j:
+                d = P[i] - P[j]
+                if (d[0] * d[0] + d[1] * d[1]) + d[2] * d[2] < r2d:
+                    adj[i, j] = adj[j, i] = 1
+                    cnt[i] += 1
+                    cnt[j] += 1
+                    edges += 1
+    return adj, edges
+
+
+def test_graph_build_against_the_reference_loop():
+    """The oracle's graph build equals the reference's loop restated line by
+    line, bit for bit, on random point sets: clustered and spread, radii that
+    connect few or most pairs, caps from 0 to beyond any row's degree, and
+    points on a lattice (exact ties at the radius)."""
+    rng = np.random.default_rng(17)
+    for case in range(60):
+        n = int(rng.integers(1, 80))
+        if case % 3 == 0:
+            pts = (rng.integers(-3, 4, (n, 3)) * 0.25).astype(np.float32)  # lattice: exact distances
+        elif case % 3 == 1:
+            pts = (rng.normal(size=(n, 3)) * 0.1).astype(np.float32)
+        else:
+            pts = rng.random((n, 3)).astype(np.float32)
+        r2 = np.float32(rng.choice([0.0625, 0.125, 0.25, 0.5]) ** 2 * (1 if case % 3 else 4))
+        cap = int(rng.choice([0, 1, 2, 3, 12, 100]))
+        adj, ne = po.build_graph(pts, r2, cap)
+        ref, ne_ref = build_graph_restated(pts, r2, cap)
+        assert np.array_equal(adj, ref), case
+        assert ne == ne_ref, case
+
+
 def test_color_ramp_knots_via_vertex_emission():
     res = 32
     vals = np.full((res, res, res), 0.5, np.float32)
