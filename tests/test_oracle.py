@@ -109,6 +109,46 @@ def test_maxtimes_equals_minplus():
     assert np.allclose(Tm, expect, rtol=1e-12, atol=1e-300)
 
 
+def floyd_restated(T):
+    """LightGraph::floydAlgo as the reference writes it (src/LightGraph.h:
+    516-534): for k, for i with |T_ik|^2 > 0, for j with |T_kj|^2 > 0,
+    T_ij = max per channel (T_ij, T_ik * T_kj), in place; then the diagonal is
+    1. |v|^2 is the FP64 lengthSqr (x*x + y*y) + z*z, so a transmittance
+    whose square underflows counts as no path."""
+    T = T.copy()
+    n = T.shape[0]
+
+    def len2(v):
+        return (v[0] * v[0] + v[1] * v[1]) + v[2] * v[2]
+
+    for k in range(n):
+        for i in range(n):
+            if len2(T[i, k]) > 0:
+                for j in range(n):
+                    if len2(T[k, j]) > 0:
+                        T[i, j] = np.maximum(T[i, j], T[i, k] * T[k, j])
+    for i in range(n):
+        T[i, i] = 1.0
+    return T
+
+
+def test_floyd_against_the_reference_loop():
+    """The oracle's max-times Floyd-Warshall equals floydAlgo's loop restated,
+    bit for bit, on random symmetric RGB transmittance matrices, including
+    entries so small that their squared length underflows (no path)."""
+    rng = np.random.default_rng(23)
+    o = po.Oracle(*slab_scene(0.5, res=16))
+    for case in range(12):
+        n = int(rng.integers(1, 18))
+        T = rng.random((n, n, 3)) * (rng.random((n, n, 1)) < 0.35)
+        if case % 4 == 3:
+            T[rng.random((n, n)) < 0.2] = 1e-170  # |T|^2 underflows to 0
+        T = np.maximum(T, T.transpose(1, 0, 2))
+        for i in range(n):
+            T[i, i] = 0.0
+        assert np.array_equal(o.fw_maxtimes(T), floyd_restated(T)), case
+
+
 def test_greedy_graph_cap_order():
     # five points on a line, all within the radius: the cap is spent in (i, j) order
     p = np.array([[0, 0, 0], [0.1, 0, 0], [0.2, 0, 0], [0.3, 0, 0], [0.4, 0, 0]], np.float32)
@@ -358,6 +398,73 @@ def test_diffusion_known_answer():
     c2 = np.maximum(T2.sum(axis=0), 1.0)
     assert T2.sum(axis=0)[1, 0] == 0.75 and c2[1, 0] == 1.0
     assert np.allclose(D2, np.einsum("jc,ijc->ic", L, T2 / c2[None, :, :]), rtol=1e-14, atol=0)
+
+
+def diffuse_restated(T, L):
+    """LightGraph::diffuseLight as the reference writes it (src/LightGraph.h:
+    562-579): column sums over i in order, maxComponent(sum, 1), the column
+    divided by it, then D_i += L_j * P_ij over j in order."""
+    P = T.copy()
+    n = P.shape[0]
+    for j in range(n):
+        acc = np.zeros(3)
+        for i in range(n):
+            acc = acc + P[i, j]
+        acc = np.maximum(acc, 1.0)
+        for i in range(n):
+            P[i, j] = P[i, j] / acc
+    D = np.zeros((n, 3))
+    for i in range(n):
+        for j in range(n):
+            D[i] = D[i] + L[j] * P[i, j]
+    return D
+
+
+def test_diffusion_against_the_reference_loop():
+    """The oracle's diffusion equals diffuseLight's loops restated, bit for
+    bit, on random solved path matrices and vertex radiance."""
+    rng = np.random.default_rng(29)
+    o = po.Oracle(*slab_scene(0.5, res=16))
+    for case in range(10):
+        n = int(rng.integers(1, 30))
+        T = rng.random((n, n, 3)) * (rng.random((n, n, 1)) < 0.5)
+        T = np.maximum(T, T.transpose(1, 0, 2))
+        for i in range(n):
+            T[i, i] = 1.0 if case % 2 == 0 else 0.3  # the solved diagonal, or a thin one
+        L = rng.random((n, 3)) * 4.0
+        assert np.array_equal(o.diffuse(T, L), diffuse_restated(T, L)), case
+
+
+def test_splat_against_brute_force():
+    """ScatterGrid::operator() (src/ScatterGrid.h:61-98) over every active
+    coarse voxel with a brute-force search over all points: the oracle's cell
+    search finds the same points (the same weighted means to rounding)."""
+    g, sh, opts = slab_scene(1.0, res=32)
+    o = po.Oracle(g, sh, opts)
+    rng = np.random.default_rng(31)
+    pts = ((rng.random((300, 3)) - 0.5) * 30.0).astype(np.float32)
+    D = rng.random((300, 3))
+    K, hp, f = 3.0, 6.0, 4
+    lo, dims, out, r = o.splat(pts, D, point_voxel_size=hp, factor=f, kernel_points=K)
+    r_ref, s2 = splat_kernel(K, hp)
+    H = 1.0 * f
+    P = pts.astype(np.float64)
+    found = 0
+    for cz in range(dims[2]):
+        for cy in range(dims[1]):
+            for cx in range(dims[0]):
+                w = np.array([(lo[0] + cx) * H, (lo[1] + cy) * H, (lo[2] + cz) * H])
+                e = (w[None, :] - P).astype(np.float32)
+                d2 = (e[:, 0] * e[:, 0] + e[:, 1] * e[:, 1]) + e[:, 2] * e[:, 2]   # float32, left to right
+                near = d2.astype(np.float64) < r_ref * r_ref
+                if near.any():
+                    found += 1
+                    wt = np.exp(-(1.0 / (2.0 * s2)) * d2[near].astype(np.float64))
+                    expect = (D[near] * wt[:, None]).sum(0) / wt.sum()
+                    assert np.allclose(out[cz, cy, cx], expect, rtol=1e-12, atol=0)
+                else:
+                    assert (out[cz, cy, cx] == 0).all()
+    assert found > 50
 
 
 def test_render_empty_grid_is_transparent():
