@@ -268,6 +268,47 @@ def test_color_ramp_wraps_past_the_last_knot():
         assert np.allclose(L[0], 2.0 * expect, rtol=1e-12, atol=1e-15), (temp, L[0], expect)
 
 
+def ramp_restated(pos, col, t_in, t_out, t):
+    """ColorRamp::getColor (src/Shader.h:56-92) line by line in FP64."""
+    if len(pos) == 0:
+        return np.zeros(3)
+    x = min(max((t - t_in) / (t_out - t_in), 0.0), 1.0)
+    if len(pos) == 1:
+        return np.array(col[0], np.float64)
+    prev = nxt = 0
+    for i, p in enumerate(pos):
+        if p <= x:
+            prev = i
+        else:
+            nxt = i
+            break
+    rng_ = pos[nxt] - pos[prev]
+    with np.errstate(divide="ignore", invalid="ignore"):
+        b = (x - pos[prev]) / rng_ if rng_ != 0 else ((x - pos[prev]) * np.inf if x != pos[prev] else np.nan)
+    return np.array(col[prev], np.float64) * (1.0 - b) + np.array(col[nxt], np.float64) * b
+
+
+def test_color_ramp_against_the_reference_code():
+    """The oracle's emission ramp equals getColor restated, bit for bit, on
+    random ramps (1 to 5 sorted knots starting at 0, so no temperature falls
+    below the first) and temperatures inside, at and past the range."""
+    rng = np.random.default_rng(37)
+    res = 16
+    g = Grid(np.full((res, res, res), 0.5, np.float32), (-8,) * 3, 1.0)
+    opts = SceneSettings(iter=1)
+    for case in range(25):
+        k = int(rng.integers(1, 6))
+        pos = [0.0] + sorted(float(v) for v in rng.random(k - 1))
+        col = [[float(c) for c in rng.random(3)] for _ in range(k)]
+        sh = Shader()
+        sh.setEmissionScale(1.0)
+        sh.setEmissionColorRamp(ColorRamp(pos, col, 100.0, 900.0))
+        for t in (float(np.float32(rng.uniform(0.0, 1200.0))), 100.0, 900.0, float(np.float32(100.0 + 800.0 * pos[-1]))):
+            tg = Grid(np.full((res, res, res), t, np.float32), (-8,) * 3, 1.0)
+            L = po.Oracle(g, sh, opts, [], temperature=tg).vertex_light(np.zeros((1, 3), np.float32))
+            assert np.array_equal(L[0], ramp_restated(pos, col, 100.0, 900.0, t)), (case, t)
+
+
 def test_env_cdf_step_function():
     """Distribution1D over a step function (src/Sampling.h:81-93): the CDF is
     the normalised running sum of func/n."""
