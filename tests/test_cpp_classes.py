@@ -44,3 +44,15 @@ def test_classes_frame_matches_c_abi(tmp_path):
     r = subprocess.run([exe, "frame"], capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stdout + r.stderr
     assert r.stdout.startswith("match"), r.stdout
+
+
+def test_c_headers_compile_as_c99(tmp_path):
+    """The C ABI's headers are plain C: a C99 caller includes them with
+    strict warnings (no C++ in them, no compiler extensions)."""
+    src = tmp_path / "check.c"
+    src.write_text('#include "lightgraph_c.h"\n#include "lightgraph_scene.h"\n'
+                   "int main(void) { lg_shader s; lg_shader_default(&s); return (int)s.ramp_n; }\n")
+    r = subprocess.run(["gcc", "-std=c99", "-Wall", "-Wextra", "-Wpedantic", "-Werror",
+                        "-I" + os.path.join(ROOT, "include"), "-c", str(src), "-o", str(tmp_path / "check.o")],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
